@@ -1,0 +1,264 @@
+/*
+ * pqmc_gb300.h -- C-ABI of the GB300 projector-DQMC hot path.
+ *
+ * Every entry point replaces one Fortran subroutine of the reference
+ * (LEOMMM816/PQMC_allinone) on its local-update / B-string / measurement
+ * path.  The Fortran side keeps its subroutine signatures and forwards to
+ * these functions through an ISO_C_BINDING shim (the shim source is shown in
+ * INTEGRATION.md).  All state the reference keeps as module globals
+ * (src/input.f90:72-96) lives on the device inside an opaque handle; the
+ * host passes plain pointers and sizes.
+ *
+ * Conventions
+ *   - complex numbers are interleaved (re, im) doubles, i.e. complex(dp);
+ *   - matrices are column-major like Fortran arrays;
+ *   - site, plaquette and boson indices inside the tables are 0-based
+ *     (the shim subtracts 1); `time`, `pf_id` arguments are 1-based, exactly
+ *     as the Fortran callers pass them;
+ *   - every function returns an int status: PQMC_OK or one of PQMC_ERR_*.
+ *     The reference stops the program on LAPACK failures
+ *     (src/mod_matrixlib.f90:405-503); the shim maps a non-zero status to
+ *     `error stop`.
+ *   - one host thread per handle (the reference is single-threaded per
+ *     process, scripts/mpi_32c_copilot.sh:74-75).
+ */
+#ifndef PQMC_GB300_H
+#define PQMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PQMC_OK 0
+#define PQMC_ERR_ARG 1        /* bad argument or size out of range            */
+#define PQMC_ERR_CUDA 2       /* a CUDA runtime call failed                   */
+#define PQMC_ERR_SINGULAR 3   /* LU found an exact zero pivot (zgetrf info>0) */
+#define PQMC_ERR_TIMEOUT 4    /* a bounded device-side wait gave up           */
+#define PQMC_ERR_STATE 5      /* call order violated (e.g. no init_g yet)      */
+#define PQMC_ERR_NOMEM 6      /* device allocation failed                     */
+
+/* expKV generator, the procedure pointer get_expKV bound in
+ * setup_expKV (src/mod_phonon_field.f90:472-496). */
+#define PQMC_EXPKV_GENERAL 0      /* get_expKV_general, expm via eigen :497-532 */
+#define PQMC_EXPKV_EPSOCZ 1       /* get_expKV_epsocz closed form      :534-569 */
+#define PQMC_EXPKV_EPSOC 2        /* get_expKV_epsoc closed form       :572-604 */
+#define PQMC_EXPKV_EPSOCZ_BLOCK 3 /* epsocz form with the norm taken from the
+                                     actual 2x2 hopping block; valid for any
+                                     block with h^H h proportional to 1 (static
+                                     spin-orbit term added to Kmatrix).  No
+                                     reference counterpart.                    */
+
+/* proposal law for the local move */
+#define PQMC_PROPOSAL_UNIFORM 0   /* jump_distance*ran_sysm(), mod_update.f90:84 */
+#define PQMC_PROPOSAL_GAUSSIAN 1  /* jump_distance*N(0,1) by Box-Muller on two
+                                     ran2 draws (extension, not in reference)   */
+
+#define PQMC_MAX_DIM 4            /* largest plaquette dimension supported     */
+
+/* Flattened model: the module globals of src/input.f90:48-96 after
+ * set_pf_main / init / init_pf_para, in the flat layout of
+ * set_pf_expKV_mat (src/mod_phonon_field.f90:605-636). */
+typedef struct pqmc_model {
+  int32_t ns;            /* Ns                                              */
+  int32_t nelec;         /* nelec = nint(Ns*filling)                        */
+  int32_t ntime;         /* Lt                                              */
+  int32_t ngroup;        /* slices between QDR stabilisations               */
+  int32_t n_pf;          /* n_phonon_field (checkerboard families)          */
+  int32_t max_dim;       /* pdim = max plaquette dim, <= PQMC_MAX_DIM        */
+  int32_t max_pla;       /* max n_plaquette over families                   */
+  int32_t n_bf;          /* n_boson_field = bf_sets*N_cell                  */
+  int32_t expkv_kind;    /* PQMC_EXPKV_*                                    */
+  int32_t ncopy;         /* flavours: weight ratio raised to ncopy          */
+  int32_t tr_weight;     /* TR_weight: ratio multiplied by its conjugate    */
+  int32_t metropolis;    /* Metropolis (1) or heat bath (0)                 */
+  int32_t greatest_decent; /* floor(prob) when set                          */
+  int32_t local_update;  /* local_update flag of the sweep driver           */
+  int32_t proposal_kind; /* PQMC_PROPOSAL_*                                 */
+  int32_t reserved;
+  double delt;           /* dtau                                            */
+  double mass;           /* M                                               */
+  double stiff;          /* D                                               */
+  double biased_phonon;  /* linear term of the phonon action               */
+  double jump_distance;  /* already scaled as in init (input.f90:183)       */
+  /* per family (length n_pf) */
+  const int32_t* pf_dim;
+  const int32_t* pf_npla;
+  const int32_t* pf_k_exist;
+  const int32_t* pf_v_exist;
+  const double* pf_k_coe;   /* complex, after init_pf_para (K_coe*(-hop)) */
+  const double* pf_v_coe;   /* complex, after init_pf_para (V_coe*lambda) */
+  const double* pf_kmat;    /* complex (max_dim,max_dim,n_pf)             */
+  const double* pf_vmat;    /* complex (max_dim,max_dim,n_pf)             */
+  /* plaquette tables */
+  const int32_t* pla_site_list;     /* (max_dim,max_pla,n_pf), 0-based sites */
+  const int32_t* bf_list;           /* (max_pla,n_pf), 0-based boson index   */
+  const int32_t* boundary_crossing; /* (max_pla,n_pf)                        */
+  const double* bc_phases;          /* complex (max_dim,max_dim,max_pla,n_pf)*/
+} pqmc_model;
+
+/* Lattice tables for the equal-time measurement (ms_take_measurement,
+ * src/mod_meas.f90:210-544).  Two sub-sites per cell (spin up, spin down)
+ * and two boson fields per cell (x bond, y bond), as the reference code
+ * assumes there (mod_meas.f90:244-247). */
+typedef struct pqmc_meas_layout {
+  int32_t n_cell;
+  int32_t reserved;
+  const int32_t* cell_sites;   /* (2,n_cell) 0-based site of sub-site 1,2   */
+  const int32_t* cell_bf;      /* (2,n_cell) 0-based boson x, y             */
+  const int32_t* cell_xnb;     /* (n_cell) 0-based cell at dpos+(1,0)       */
+  const int32_t* cell_ynb;     /* (n_cell) 0-based cell at dpos+(0,1)       */
+  const int32_t* cell_cross;   /* (2,n_cell) dpos(i)==L_i-1                 */
+  const int32_t* rel_index;    /* (n_cell,n_cell) 0-based relative index of
+                                  c2 seen from c1: rel_index[c1+n*c2]       */
+  const double* bc_phase;      /* complex (2) Lat%BC_phase                 */
+  const double* k_phase;       /* complex (n_cell,n_cell) Lat%k_phase      */
+  double hop;
+  double ep_parameter;
+} pqmc_meas_layout;
+
+/* Observable slots of one measurement record (per-measurement vector,
+ * like MeasurementSystem%data(:,m,b)).  Scalars first, then fields of
+ * width n_cell each, each field followed by its _k transform. */
+#define PQMC_OBS_BF_KE 0
+#define PQMC_OBS_BF_PE 1
+#define PQMC_OBS_BF_X 2
+#define PQMC_N_SCALAR 3
+/* field order */
+#define PQMC_F_BFX_BFX 0
+#define PQMC_F_BFX_BFY 1
+#define PQMC_F_BFY_BFY 2
+#define PQMC_F_BFXY_BFXY 3
+#define PQMC_F_JXX_JXX 4
+#define PQMC_F_JXY_JXY 5
+#define PQMC_F_JYX_JYX 6
+#define PQMC_F_JYY_JYY 7
+#define PQMC_F_JXX_JYX 8
+#define PQMC_F_JXY_JYY 9
+#define PQMC_F_JXXH_JXXH 10
+#define PQMC_F_JXYH_JXYH 11
+#define PQMC_F_JYXH_JYXH 12
+#define PQMC_F_JYYH_JYYH 13
+#define PQMC_F_JXXH_JYXH 14
+#define PQMC_F_JXYH_JYYH 15
+#define PQMC_F_JXXH_JYYH 16
+#define PQMC_F_JXYH_JYXH 17
+#define PQMC_F_DEN_DEN 18
+#define PQMC_F_SC_SC 19
+#define PQMC_F_SZ_SZ 20
+#define PQMC_F_SX_SX 21
+#define PQMC_F_SY_SY 22
+#define PQMC_F_CJYX_CJYX 23
+#define PQMC_F_CJXY_CJXY 24
+#define PQMC_N_FIELD 25
+/* record width (complex entries): PQMC_N_SCALAR + 2*PQMC_N_FIELD*n_cell
+ * (r-space block of all fields, then k-space block of all fields). */
+
+/* Per-chain scalar state (module globals of input.f90:7,53,72). */
+typedef struct pqmc_state {
+  double ln_cw[2];          /* complex ln_cw                               */
+  double err_fast_max;      /* largest fast-vs-scratch error so far         */
+  double err_fast;          /* last fast-vs-scratch error (G or ln_cw)      */
+  int64_t positive_accept;  /* local moves accepted                          */
+  int64_t negative_accept;  /* local moves rejected                          */
+  int32_t rng[5];           /* iran0,jran0,kran0,mran0,nran0 of ran2_s       */
+  int32_t reserved;
+} pqmc_state;
+
+typedef struct pqmc_chain pqmc_chain; /* opaque, one Markov chain on the GPU */
+
+/* ---- lifetime ------------------------------------------------------- */
+/* Allocates the device copies of every module global the hot path uses.
+ * Replaces the allocations of init_g_T0 (mod_evolution.f90:57-62) and of
+ * set_pf_expKV_mat (mod_phonon_field.f90:612-619). */
+int pqmc_create(const pqmc_model* model, pqmc_chain** out);
+int pqmc_destroy(pqmc_chain* chain);
+/* Attach the measurement lattice tables (ms_init_meas, mod_meas.f90:577). */
+int pqmc_set_meas_layout(pqmc_chain* chain, const pqmc_meas_layout* layout);
+
+/* ---- state transfer ------------------------------------------------- */
+/* boson_field(n_bf,ntime) in (input.f90:86); import_ph_field path of
+ * init_boson_field (Main_PQMC.f90:355-369) with exact doubles. */
+int pqmc_set_field(pqmc_chain* chain, const double* boson_field);
+int pqmc_get_field(pqmc_chain* chain, double* boson_field);
+/* slater_Q(Ns,nelec), slater_D(nelec) complex, from set_nelec_occupied
+ * (Main_PQMC.f90:279-305). */
+int pqmc_set_slater(pqmc_chain* chain, const double* slater_q,
+                    const double* slater_d);
+/* g_h(Ns,Ns) complex (input.f90:88). */
+int pqmc_get_g(pqmc_chain* chain, double* g_h);
+int pqmc_set_g(pqmc_chain* chain, const double* g_h);
+int pqmc_get_state(pqmc_chain* chain, pqmc_state* state);
+/* ran2 state words; replaces init_rng_by_seed (mod_ranstate.f90:267-283)
+ * when called with the five seeded words. */
+int pqmc_set_rng(pqmc_chain* chain, const int32_t rng[5]);
+/* Q_string(:,:,block) and D_string(:,block), block 1-based. */
+int pqmc_get_qd(pqmc_chain* chain, int block, double* q, double* d);
+
+/* ---- hot path: one call per reference subroutine --------------------- */
+/* init_expKV for every family + set_pf_expKV_mat
+ * (mod_phonon_field.f90:423-450, 605-636). */
+int pqmc_init_expkv(pqmc_chain* chain);
+/* init_g_T0(start_time) (mod_evolution.f90:46-111). */
+int pqmc_init_g(pqmc_chain* chain, int start_time);
+/* update_phonon_field(ppf_list(pf_id), time) (mod_update.f90:13-201). */
+int pqmc_update_phonon_field(pqmc_chain* chain, int pf_id, int time);
+/* left_evolve(time, g_h, Ns, pf_id, two_way) (mod_evolution.f90:236-285). */
+int pqmc_left_evolve_g(pqmc_chain* chain, int time, int pf_id, int two_way);
+/* right_evolve(time, g_h, Ns, pf_id, two_way) (mod_evolution.f90:287-328). */
+int pqmc_right_evolve_g(pqmc_chain* chain, int time, int pf_id, int two_way);
+/* left_evolve(time, mat(Ns,n), n, pf_id, .false.) on a caller matrix. */
+int pqmc_left_evolve(pqmc_chain* chain, int time, int pf_id, double* mat,
+                     int n);
+/* right_evolve(time, mat(n,Ns), n, pf_id, .false.) on a caller matrix. */
+int pqmc_right_evolve(pqmc_chain* chain, int time, int pf_id, double* mat,
+                      int n);
+/* get_g_scratch_T0(time, forward, loop) (mod_evolution.f90:113-195);
+ * err_out (may be NULL) receives max|gfast-g| and |Re(dln_cw)|. */
+int pqmc_get_g_scratch(pqmc_chain* chain, int time, int forward, int loop,
+                       double* err_out);
+/* cal_new_weight_T0() (mod_evolution.f90:359-408); ln_cw_out complex. */
+int pqmc_cal_new_weight(pqmc_chain* chain, double* ln_cw_out);
+/* Meas_sys%take_measurement(time) (mod_meas.f90:210-544): adds one
+ * record into the device accumulator. */
+int pqmc_take_measurement(pqmc_chain* chain, int time);
+/* Meas_sys%begin_measure(forward,time) (mod_meas.f90:729-763): takes the
+ * measurement and, at the last slice of the window, divides by
+ * 2*meas_number+1, adds the k-space transform (ms_k_space_obs :546-566)
+ * and copies the finished record to `record_out` (may be NULL); *done is
+ * set to 1 when a record was finished. */
+int pqmc_begin_measure(pqmc_chain* chain, int forward, int time,
+                       int meas_number, double* record_out, int* done);
+/* The sweep loop body of Main_PQMC.f90:81-156 for `n_sweeps` consecutive
+ * values of `loop` starting at `first_loop` (global updates excluded).
+ * Measurements are taken when loop>warmup and mod(loop-warmup,
+ * meas_interval)==0; finished records are appended to `records`
+ * (n_records_cap entries of record width), *n_records is their count. */
+int pqmc_sweep(pqmc_chain* chain, int first_loop, int n_sweeps, int warmup,
+               int meas_interval, int meas_number, double* records,
+               int n_records_cap, int* n_records);
+
+/* ---- batched, mixed precision --------------------------------------- */
+typedef struct pqmc_batch pqmc_batch; /* many chains in one device context */
+#define PQMC_PREC_FP64 0   /* every product in FP64                        */
+#define PQMC_PREC_MIXED 1  /* split-BF16 tensor-core delayed-update and
+                              B-string products, FP32 accumulation; FP64
+                              QR, recompute and log-det                    */
+int pqmc_batch_create(const pqmc_model* const* models, int n_chains,
+                      int precision, pqmc_batch** out);
+int pqmc_batch_destroy(pqmc_batch* batch);
+int pqmc_batch_chain(pqmc_batch* batch, int i, pqmc_chain** chain);
+/* one sweep of every chain (Main_PQMC.f90:99-154), no measurement */
+int pqmc_batch_sweep(pqmc_batch* batch, int loop);
+
+/* ---- introspection --------------------------------------------------- */
+const char* pqmc_version(void);
+const char* pqmc_last_error(void);
+/* number of kernel launches issued by this library since load */
+int64_t pqmc_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PQMC_GB300_H */

@@ -1,0 +1,186 @@
+"""Host mirror of the reference's Fortran hot-path interfaces on the GPU.
+
+:class:`PqmcChain` exposes one method per reference subroutine, with the
+reference's argument meaning (1-based ``time`` and ``pf_id``):
+
+=========================  ===============================================
+method                     reference
+=========================  ===============================================
+``init_expkv``             init_expKV + set_pf_expKV_mat
+                           (src/mod_phonon_field.f90:423-450, 605-636)
+``init_g(start_time)``     init_g_T0 (src/mod_evolution.f90:46-111)
+``update_phonon_field``    update_phonon_field(ppf,time)
+                           (src/mod_update.f90:13-201)
+``left_evolve_g``          left_evolve(time,g_h,Ns,pf,.true.) (:236-285)
+``right_evolve_g``         right_evolve(time,g_h,Ns,pf,.true.) (:287-328)
+``left_evolve``            left_evolve(time,mat,n,pf,.false.)
+``right_evolve``           right_evolve(time,mat,n,pf,.false.)
+``get_g_scratch``          get_g_scratch_T0(time,forward,loop) (:113-195)
+``cal_new_weight``         cal_new_weight_T0 (:359-408)
+``take_measurement``       Meas_sys%take_measurement (mod_meas.f90:210)
+``begin_measure``          Meas_sys%begin_measure (mod_meas.f90:729-763)
+``sweep``                  the loop body of src/Main_PQMC.f90:81-156
+=========================  ===============================================
+
+Every call goes through the C-ABI of include/pqmc_gb300.h; a non-zero
+status raises :class:`PqmcError` (the reference stops the program).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from .abi import MeasStruct, ModelStruct, PqmcError, PqmcState, check, load_library
+from .model import Model, record_width
+
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+def _c128(a) -> np.ndarray:
+    return np.asfortranarray(np.asarray(a, dtype=np.complex128))
+
+
+class PqmcChain:
+    """One Markov chain resident on the GPU."""
+
+    def __init__(self, m: Model, *, field: np.ndarray, rng_words, meas: bool = True,
+                 proposal_kind: int | None = None, handle: ctypes.c_void_p | None = None):
+        self.m = m
+        self.lib = load_library()
+        self.ms = ModelStruct(m, proposal_kind=proposal_kind)
+        self._owned = handle is None
+        if handle is None:
+            h = ctypes.c_void_p()
+            self._chk(self.lib.pqmc_create(ctypes.byref(self.ms.s), ctypes.byref(h)), "pqmc_create")
+            self.h = h
+        else:
+            self.h = handle
+        self.set_field(field)
+        q = _c128(m.slater_q)
+        d = np.ascontiguousarray(m.slater_d, dtype=np.complex128)
+        self._chk(self.lib.pqmc_set_slater(self.h, q.ctypes.data_as(_f64p), d.ctypes.data_as(_f64p)),
+                  "pqmc_set_slater")
+        self.set_rng(rng_words)
+        self.meas = None
+        if meas:
+            self.meas = MeasStruct(m)
+            self._chk(self.lib.pqmc_set_meas_layout(self.h, ctypes.byref(self.meas.s)),
+                      "pqmc_set_meas_layout")
+
+    def _chk(self, st, what):
+        check(self.lib, st, what)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self._owned:
+            self.lib.pqmc_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state -------------------------------------------------------
+    def set_field(self, f):
+        f = np.asfortranarray(f, dtype=np.float64)
+        assert f.shape == (self.m.n_bf, self.m.ntime)
+        self._chk(self.lib.pqmc_set_field(self.h, f.ctypes.data_as(_f64p)), "pqmc_set_field")
+
+    def field(self) -> np.ndarray:
+        f = np.zeros((self.m.n_bf, self.m.ntime), order="F")
+        self._chk(self.lib.pqmc_get_field(self.h, f.ctypes.data_as(_f64p)), "pqmc_get_field")
+        return f
+
+    def set_rng(self, words):
+        w = (ctypes.c_int32 * 5)(*[int(x) for x in words])
+        self._chk(self.lib.pqmc_set_rng(self.h, w), "pqmc_set_rng")
+
+    def g(self) -> np.ndarray:
+        g = np.zeros((self.m.ns, self.m.ns), dtype=np.complex128, order="F")
+        self._chk(self.lib.pqmc_get_g(self.h, g.ctypes.data_as(_f64p)), "pqmc_get_g")
+        return g
+
+    def set_g(self, g):
+        g = _c128(g)
+        self._chk(self.lib.pqmc_set_g(self.h, g.ctypes.data_as(_f64p)), "pqmc_set_g")
+
+    def state(self) -> dict:
+        s = PqmcState()
+        self._chk(self.lib.pqmc_get_state(self.h, ctypes.byref(s)), "pqmc_get_state")
+        return s.as_dict()
+
+    def qd(self, blk: int):
+        q = np.zeros((self.m.ns, self.m.nelec), dtype=np.complex128, order="F")
+        d = np.zeros(self.m.nelec, dtype=np.complex128)
+        self._chk(self.lib.pqmc_get_qd(self.h, blk, q.ctypes.data_as(_f64p), d.ctypes.data_as(_f64p)),
+                  "pqmc_get_qd")
+        return q, d
+
+    # ---- hot path ------------------------------------------------------
+    def init_expkv(self):
+        self._chk(self.lib.pqmc_init_expkv(self.h), "init_expKV")
+
+    def init_g(self, start_time: int = 1):
+        self._chk(self.lib.pqmc_init_g(self.h, start_time), "init_g_T0")
+
+    def update_phonon_field(self, pf_id: int, time: int):
+        self._chk(self.lib.pqmc_update_phonon_field(self.h, pf_id, time), "update_phonon_field")
+
+    def left_evolve_g(self, time: int, pf_id: int, two_way: bool = True):
+        self._chk(self.lib.pqmc_left_evolve_g(self.h, time, pf_id, int(two_way)), "left_evolve")
+
+    def right_evolve_g(self, time: int, pf_id: int, two_way: bool = True):
+        self._chk(self.lib.pqmc_right_evolve_g(self.h, time, pf_id, int(two_way)), "right_evolve")
+
+    def left_evolve(self, time: int, pf_id: int, mat) -> np.ndarray:
+        mat = _c128(mat).copy(order="F")
+        self._chk(self.lib.pqmc_left_evolve(self.h, time, pf_id, mat.ctypes.data_as(_f64p), mat.shape[1]),
+                  "left_evolve")
+        return mat
+
+    def right_evolve(self, time: int, pf_id: int, mat) -> np.ndarray:
+        mat = _c128(mat).copy(order="F")
+        self._chk(self.lib.pqmc_right_evolve(self.h, time, pf_id, mat.ctypes.data_as(_f64p), mat.shape[0]),
+                  "right_evolve")
+        return mat
+
+    def get_g_scratch(self, time: int, forward: bool, loop: int = 1) -> np.ndarray:
+        e = np.zeros(2)
+        self._chk(self.lib.pqmc_get_g_scratch(self.h, time, int(forward), loop, e.ctypes.data_as(_f64p)),
+                  "get_g_scratch_T0")
+        return e
+
+    def cal_new_weight(self) -> complex:
+        o = np.zeros(2)
+        self._chk(self.lib.pqmc_cal_new_weight(self.h, o.ctypes.data_as(_f64p)), "cal_new_weight_T0")
+        return complex(o[0], o[1])
+
+    def take_measurement(self, time: int):
+        self._chk(self.lib.pqmc_take_measurement(self.h, time), "take_measurement")
+
+    def begin_measure(self, forward: bool, time: int, meas_number: int = 0):
+        rec = np.zeros(record_width(self.m), dtype=np.complex128)
+        done = ctypes.c_int(0)
+        self._chk(self.lib.pqmc_begin_measure(self.h, int(forward), time, meas_number,
+                                              rec.ctypes.data_as(_f64p), ctypes.byref(done)),
+                  "begin_measure")
+        return rec if done.value else None
+
+    def sweep(self, first_loop: int, n_sweeps: int = 1, *, warmup: int = 1 << 30, meas_interval: int = 1,
+              meas_number: int = 0, cap: int = 0) -> np.ndarray:
+        w = record_width(self.m)
+        recs = np.zeros((max(cap, 1), w), dtype=np.complex128)
+        n = ctypes.c_int(0)
+        self._chk(self.lib.pqmc_sweep(self.h, first_loop, n_sweeps, warmup, meas_interval, meas_number,
+                                      recs.ctypes.data_as(_f64p), cap, ctypes.byref(n)), "sweep")
+        return recs[: n.value]
+
+
+def kernel_launches() -> int:
+    return int(load_library().pqmc_kernel_launches())
+
+
+__all__ = ["PqmcChain", "PqmcError", "kernel_launches"]

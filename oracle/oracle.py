@@ -63,7 +63,7 @@ def c128(a) -> np.ndarray:
 class OracleChain:
     """One chain on the CPU oracle, driven with the same calls as the GPU."""
 
-    def __init__(self, m: Model, *, field: np.ndarray, seed_words=None, meas: bool = True,
+    def __init__(self, m: Model, *, field: np.ndarray, seed_words=None, meas: bool | None = None,
                  proposal_kind: int | None = None):
         self.m = m
         self.L = lib()
@@ -79,6 +79,8 @@ class OracleChain:
         if seed_words is not None:
             self.set_rng(seed_words)
         self.meas = None
+        if meas is None:
+            meas = m.lat.dim == 2 and m.lat.n_sub == 2 and m.spec.bf_sets == 2
         if meas:
             self.meas = MeasStruct(m)
             self.L.oracle_set_meas_layout(self.h, self.meas.ref)

@@ -45,7 +45,7 @@ def _c128(a) -> np.ndarray:
 class PqmcChain:
     """One Markov chain resident on the GPU."""
 
-    def __init__(self, m: Model, *, field: np.ndarray, rng_words, meas: bool = True,
+    def __init__(self, m: Model, *, field: np.ndarray, rng_words, meas: bool | None = None,
                  proposal_kind: int | None = None, handle: ctypes.c_void_p | None = None):
         self.m = m
         self.lib = load_library()
@@ -64,6 +64,8 @@ class PqmcChain:
                   "pqmc_set_slater")
         self.set_rng(rng_words)
         self.meas = None
+        if meas is None:
+            meas = m.lat.dim == 2 and m.lat.n_sub == 2 and m.spec.bf_sets == 2
         if meas:
             self.meas = MeasStruct(m)
             self._chk(self.lib.pqmc_set_meas_layout(self.h, ctypes.byref(self.meas.s)),

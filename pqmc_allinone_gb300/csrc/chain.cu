@@ -63,254 +63,6 @@ int launch_init_expkv(pqmc_chain* c) {
 }
 
 // ---------------------------------------------------------------------------
-// update_phonon_field(ppf,time) as one cooperative kernel.
-//
-// Block 0 (warp 0) is the proposer: it walks the family's plaquettes in the
-// reference's Markov order, evaluates det(I + G_SS Delta) and the Metropolis
-// test with the bit-exact ran2 stream, and publishes every accepted move as
-// (S, T = Delta R^-1).  All other blocks apply the previously published move
-// to G out of place, G' = G + G(:,S) T (I - G)(S,:), while the proposer
-// scans ahead using G plus the pending move's correction on the 4x4 block it
-// needs.  One grid barrier per accepted move; rejected proposals cost no
-// barrier.  G ping-pongs between two buffers and ends in the first.
-__device__ __forceinline__ double energy_diff(const DevModel& M, const double* field, int b, int t, double jump) {
-  // cal_energy_difference (src/mod_update.f90:203-228), t 0-based
-  const int nt = M.ntime;
-  double be = field[b + (size_t)M.n_bf * ((t - 1 + nt) % nt)];
-  double af = field[b + (size_t)M.n_bf * ((t + 1) % nt)];
-  double now = field[b + (size_t)M.n_bf * t];
-  double nw = now + jump;
-  double dt2 = M.delt * M.delt;
-  double e1 = ((0.5 * M.mass) * ((be - now) * (be - now) + (af - now) * (af - now))) / dt2 +
-              (0.5 * M.stiff) * (now * now) - M.biased * now;
-  double e2 = ((0.5 * M.mass) * ((be - nw) * (be - nw) + (af - nw) * (af - nw))) / dt2 +
-              (0.5 * M.stiff) * (nw * nw) - M.biased * nw;
-  return e2 - e1;
-}
-
-__global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdCtl* ctl, double* field,
-                                                 cplx* expkv, cplx* expkv_inv, cplx* gA, cplx* gB, int pf,
-                                                 int t) {
-  cg::grid_group grid = cg::this_grid();
-  const int ns = M.ns, dim = M.pf_dim[pf], npla = M.pf_npla[pf], pd = M.pdim;
-  __shared__ cplx s_g[16], s_delta[16], s_r[16], s_e[16], s_t[16], s_c1[16], s_tp[16], s_w[16];
-  __shared__ int s_S[4], s_Sp[4];
-  __shared__ int s_dec;
-  __shared__ cplx s_relec;
-  cplx* gcur = gA;
-  cplx* gnext = gB;
-  int prev = -1, step = 0;
-  // proposer state (block 0, thread 0)
-  Ran2Dev rng;
-  cplx lncw = mk(0.0);
-  long long pa = 0, na = 0;
-  int next = 0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    rng.iran = sc->rng[0]; rng.jran = sc->rng[1]; rng.kran = sc->rng[2];
-    rng.mran = sc->rng[3]; rng.nran = sc->rng[4];
-    lncw = sc->ln_cw;
-  }
-  for (;;) {
-    UpdCtl* cw = ctl + (step & 1);
-    const UpdCtl* cr = ctl + ((step + 1) & 1);
-    if (blockIdx.x == 0) {
-      if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        const bool has_prev = step > 0;
-        int found = -1;
-        for (int p = next; p < npla; ++p) {
-          if (lane < dim) s_S[lane] = M.site[lane + pd * (p + M.max_pla * pf)];
-          __syncwarp();
-          const int i = lane % dim, j = lane / dim;
-          const bool act = lane < dim * dim;
-          // g_h_sub = G(S,S) (+ pending move's correction)   mod_update.f90:73
-          cplx gv = mk(0.0);
-          if (act) {
-            gv = ldg_c(gcur + s_S[i] + (size_t)ns * s_S[j]);
-            if (has_prev) {
-              cplx a = mk(0.0);
-              for (int m = 0; m < dim; ++m) a = cadd(a, cmul(ldg_c(gcur + s_S[i] + (size_t)ns * s_Sp[m]), s_tp[m + dim * j]));
-              s_c1[lane] = a;
-            }
-          }
-          __syncwarp();
-          if (act && has_prev) {
-            cplx a = mk(0.0);
-            for (int l = 0; l < dim; ++l) {
-              cplx v = cneg(ldg_c(gcur + s_Sp[l] + (size_t)ns * s_S[j]));
-              if (s_Sp[l] == s_S[j]) v = cadd(v, mk(1.0));
-              a = cadd(a, cmul(s_c1[i + dim * l], v));
-            }
-            gv = cadd(gv, a);
-          }
-          if (act) s_g[lane] = gv;
-          // proposal and new propagator (lane 0)
-          double jump = 0.0, xnew = 0.0, dE = 0.0;
-          const int b = M.bf[p + M.max_pla * pf];
-          if (lane == 0) {
-            if (M.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
-              double u1 = (double)rng.next(), u2 = (double)rng.next();
-              jump = M.jump * (sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
-            } else {
-              jump = M.jump * (double)rng.ran_sysm();            // :84
-            }
-            dE = -M.delt * energy_diff(M, field, b, t, jump);    // :87-88
-            xnew = field[b + (size_t)M.n_bf * t] + jump;         // :92
-            dev_get_expkv(M, pf, p, xnew, false, s_e);           // calculate_Delta :239
-          }
-          __syncwarp();
-          // Delta = expKV_inv(old) * expKV(new) - I    :240-243
-          if (act) {
-            const size_t base = M.kv_base(p, pf, t);
-            cplx a = mk(0.0);
-            for (int k = 0; k < dim; ++k) a = cadd(a, cmul(expkv_inv[base + i + pd * k], s_e[k + dim * j]));
-            if (i == j) a = csub(a, mk(1.0));
-            s_delta[lane] = a;
-          }
-          __syncwarp();
-          // R = I + g_h_sub * Delta    :97-100
-          if (act) {
-            cplx a = mk(0.0);
-            for (int k = 0; k < dim; ++k) a = cadd(a, cmul(s_g[i + dim * k], s_delta[k + dim * j]));
-            if (i == j) a = cadd(a, mk(1.0));
-            s_r[lane] = a;
-          }
-          __syncwarp();
-          if (lane == 0) {
-            cplx relec = dev_det_small(dim, s_r);                // :101
-            if (M.tr_weight) relec = cmul(relec, cconj(relec));  // :103
-            cplx base = relec, acc = mk(1.0);
-            for (int k = 0; k < M.ncopy; ++k) acc = cmul(acc, base);
-            relec = acc;                                         // :104
-            cplx w = cadd(mk(dE), clog_(relec));                 // :108
-            double rt = exp(fmin(10.0, w.x));                    // cal_prob :491
-            double prob;
-            if (M.metropolis) {
-              prob = fmin(1.0, rt);
-              if (M.greatest_decent) prob = floor(prob);
-            } else {
-              prob = rt / (1.0 + rt);
-            }
-            double r = (double)rng.next();                       // :117
-            int acc_ok = !(prob < r);
-            s_dec = acc_ok;
-            s_relec = relec;
-            if (acc_ok) {
-              pa++;
-              lncw = cadd(lncw, mk(log(relec.x)));               // :142
-              field[b + (size_t)M.n_bf * t] = xnew;
-              const size_t base2 = M.kv_base(p, pf, t);
-              for (int jj = 0; jj < pd; ++jj)
-                for (int ii = 0; ii < pd; ++ii)
-                  expkv[base2 + ii + pd * jj] = (ii < dim && jj < dim) ? s_e[ii + dim * jj] : mk(0.0);
-              dev_get_expkv(M, pf, p, xnew, true, s_w);          // :126-127
-              for (int jj = 0; jj < pd; ++jj)
-                for (int ii = 0; ii < pd; ++ii)
-                  expkv_inv[base2 + ii + pd * jj] = (ii < dim && jj < dim) ? s_w[ii + dim * jj] : mk(0.0);
-              for (int k = 0; k < dim * dim; ++k) s_c1[k] = s_r[k];
-              dev_inverse_small(dim, s_c1);                      // :171
-            } else {
-              na++;
-            }
-          }
-          __syncwarp();
-          if (s_dec) {
-            // T = Delta * R^-1    :173
-            if (act) {
-              cplx a = mk(0.0);
-              for (int k = 0; k < dim; ++k) a = cadd(a, cmul(s_delta[i + dim * k], s_c1[k + dim * j]));
-              s_t[lane] = a;
-              cw->T[lane] = a;
-            }
-            if (lane < dim) cw->S[lane] = s_S[lane];
-            __syncwarp();
-            if (act) s_tp[lane] = s_t[lane];
-            if (lane < dim) s_Sp[lane] = s_S[lane];
-            found = p;
-            __syncwarp();
-            break;
-          }
-        }
-        if (lane == 0) {
-          cw->p = found;
-          cw->dim = dim;
-          next = (found >= 0) ? found + 1 : npla;
-        }
-        next = __shfl_sync(0xffffffffu, next, 0);
-      }
-    } else if (prev >= 0) {
-      // G' = G + G(:,S) W,  W = T (I - G)(S,:)     mod_update.f90:146-187
-      __shared__ cplx s_wc[4];
-      __shared__ int s_s[4];
-      __shared__ cplx s_T[16];
-      if (threadIdx.x < dim) s_s[threadIdx.x] = cr->S[threadIdx.x];
-      if (threadIdx.x < dim * dim) s_T[threadIdx.x] = ldg_c(&cr->T[threadIdx.x]);
-      __syncthreads();
-      const long total = (long)ns * ns;
-      const int nw = gridDim.x - 1;
-      const long chunk = (total + nw - 1) / nw;
-      const long e0 = (long)(blockIdx.x - 1) * chunk;
-      const long e1 = (e0 + chunk < total) ? e0 + chunk : total;
-      if (e0 < e1) {
-        const int c0 = (int)(e0 / ns), c1 = (int)((e1 - 1) / ns);
-        for (int col = c0; col <= c1; ++col) {
-          if (threadIdx.x < dim) {
-            const int k = threadIdx.x;
-            cplx a = mk(0.0);
-            for (int l = 0; l < dim; ++l) {
-              cplx v = cneg(ldg_c(gcur + s_s[l] + (size_t)ns * col));
-              if (s_s[l] == col) v = cadd(v, mk(1.0));
-              a = cadd(a, cmul(s_T[k + dim * l], v));
-            }
-            s_wc[k] = a;
-          }
-          __syncthreads();
-          long lo = (long)col * ns, hi = lo + ns;
-          if (lo < e0) lo = e0;
-          if (hi > e1) hi = e1;
-          for (long e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-            const int r = (int)(e - (long)col * ns);
-            cplx a = ldg_c(gcur + e);
-            for (int k = 0; k < dim; ++k) a = cadd(a, cmul(ldg_c(gcur + r + (size_t)ns * s_s[k]), s_wc[k]));
-            gnext[e] = a;
-          }
-          __syncthreads();
-        }
-      }
-    }
-    grid.sync();
-    if (prev >= 0) {
-      cplx* tmp = gcur;
-      gcur = gnext;
-      gnext = tmp;
-    }
-    prev = __ldcg(&cw->p);
-    ++step;
-    if (prev < 0) break;
-  }
-  if (gcur != gA) {
-    const long total = (long)ns * ns;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x)
-      gA[e] = ldg_c(gcur + e);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    sc->rng[0] = rng.iran; sc->rng[1] = rng.jran; sc->rng[2] = rng.kran;
-    sc->rng[3] = rng.mran; sc->rng[4] = rng.nran;
-    sc->ln_cw = lncw;
-    sc->pos_acc += pa;
-    sc->neg_acc += na;
-  }
-}
-
-int launch_update(pqmc_chain* c, int pf, int time) {
-  int t = time - 1;
-  void* args[] = {&c->M, &c->sc, &c->ctl, &c->field, &c->expkv, &c->expkv_inv, &c->g, &c->g_alt, &pf, &t};
-  PQMC_CUDA(cudaLaunchCooperativeKernel((const void*)k_update, c->upd_blocks, 256, args, 0, c->stream));
-  PQMC_LAUNCHED();
-  return PQMC_OK;
-}
-
-// ---------------------------------------------------------------------------
 // Two-way wrap of G by one family (left_evolve/right_evolve with two_way,
 // src/mod_evolution.f90:236-328): out(Sr,Sc) = A_r G(Sr,Sc) B_c over all
 // pairs of cover items; left: A = expKV, B = expKV_inv; right: swapped.
@@ -443,6 +195,43 @@ __global__ void k_sumlog(int n, const cplx* __restrict__ d, cplx* out, int accum
   if (threadIdx.x == 0) out[0] = accumulate ? cadd(out[0], mk(rr[0], ri[0])) : mk(rr[0], ri[0]);
 }
 
+// sum of log D over one block of the D string, written to out[0]
+__global__ void k_blocklog(int n, const cplx* __restrict__ d, cplx* out) {
+  __shared__ double rr[256], ri[256];
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    cplx l = clog_(d[i]);
+    a += l.x;
+    b += l.y;
+  }
+  rr[threadIdx.x] = a;
+  ri[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      rr[threadIdx.x] += rr[threadIdx.x + s];
+      ri[threadIdx.x] += ri[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = mk(rr[0], ri[0]);
+}
+
+// sumlogd = sum over blocks of the per-block sums (sum(log(D_string)), :346)
+__global__ void k_sumvec(int n, const cplx* __restrict__ v, cplx* out) {
+  if (threadIdx.x != 0) return;
+  cplx s = mk(0.0);
+  for (int i = 0; i < n; ++i) s = cadd(s, v[i]);
+  out[0] = s;
+}
+
+int block_log(pqmc_chain* c, int blk1) {
+  k_blocklog<<<1, 256, 0, c->stream>>>(c->nelec, c->d_string + (size_t)c->nelec * (blk1 - 1),
+                                        c->d_logsum + (blk1 - 1));
+  PQMC_LAUNCHED();
+  return PQMC_OK;
+}
+
 __device__ __forceinline__ cplx branch_reduce(cplx z) {
   // cmplx(real(z), mod(aimag(z), 2*pi)) with PI of nrtype in REAL(SP)
   const double two_pi_sp = (double)(2.0f * 3.14159265358979323846f);
@@ -499,7 +288,7 @@ static int cal_g_and_det(pqmc_chain* c, const cplx* X, const cplx* R, bool compa
   PQMC_TRY(zgemm(s, 'C', 'N', ne, ne, ns, mk(1.0), X, ns, R, ns, mk(0.0), c->pbp, ne));
   PQMC_TRY(lu_factor(s, ne, c->pbp, c->ipiv, &c->sc->lu_info, c->lcol));
   PQMC_TRY(lu_logdet(s, ne, c->pbp, c->ipiv, &c->sc->logdet));
-  k_sumlog<<<1, 256, 0, s>>>(ne * c->nblock, c->d_string, &c->sc->sumlogd, 0);
+  k_sumvec<<<1, 32, 0, s>>>(c->nblock, c->d_logsum, &c->sc->sumlogd);
   PQMC_LAUNCHED();
   PQMC_TRY(herm_t(s, ns, ne, X, c->lmat));
   PQMC_TRY(lu_solve(s, ne, ns, c->pbp, c->ipiv, c->lmat, ne));
@@ -543,6 +332,7 @@ int do_init_g(pqmc_chain* c, int start_time) {
   PQMC_CUDA(cudaMemcpyAsync(Qblk(c, nb), c->slater_q, qb, cudaMemcpyDeviceToDevice, s));
   PQMC_CUDA(cudaMemcpyAsync(Dblk(c, 1), c->slater_d, sizeof(cplx) * ne, cudaMemcpyDeviceToDevice, s));
   PQMC_CUDA(cudaMemcpyAsync(Dblk(c, nb), c->slater_d, sizeof(cplx) * ne, cudaMemcpyDeviceToDevice, s));
+  for (int b = 1; b <= nb; ++b) PQMC_TRY(block_log(c, b));
   int start_block = start_time / c->ngroup + 1;
   int start_by_block = (start_block - 1) * c->ngroup + 1;
   if (start_by_block > start_time) {
@@ -558,6 +348,7 @@ int do_init_g(pqmc_chain* c, int start_time) {
     if (end % c->ngroup == 0) {
       int blk = (end - 1) / c->ngroup + 2;
       PQMC_TRY(house_qr(s, ns, ne, c->rmat, c->tau, Dblk(c, blk)));
+      PQMC_TRY(block_log(c, blk));
       PQMC_CUDA(cudaMemcpyAsync(Qblk(c, blk), c->rmat, qb, cudaMemcpyDeviceToDevice, s));
     }
     p = end + 1;
@@ -583,6 +374,7 @@ int do_g_scratch(pqmc_chain* c, int time, bool forward, int loop) {
     PQMC_CUDA(cudaMemcpyAsync(c->rmat, Qblk(c, blk - 1), qb, cudaMemcpyDeviceToDevice, s));
     PQMC_TRY(launch_propagate(c, c->rmat, ne, time - c->ngroup, time - 1, true));
     PQMC_TRY(house_qr(s, ns, ne, c->rmat, c->tau, Dblk(c, blk)));
+    PQMC_TRY(block_log(c, blk));
     PQMC_CUDA(cudaMemcpyAsync(Qblk(c, blk), c->rmat, qb, cudaMemcpyDeviceToDevice, s));
     return cal_g_and_det(c, Qblk(c, blk + 1), c->rmat, true);
   }
@@ -592,6 +384,7 @@ int do_g_scratch(pqmc_chain* c, int time, bool forward, int loop) {
   PQMC_CUDA(cudaMemcpyAsync(c->xmat, Qblk(c, blk + 1), qb, cudaMemcpyDeviceToDevice, s));
   PQMC_TRY(launch_propagate(c, c->xmat, ne, time + c->ngroup - 1, time, false));
   PQMC_TRY(house_qr(s, ns, ne, c->xmat, c->tau, Dblk(c, blk)));
+  PQMC_TRY(block_log(c, blk));
   PQMC_CUDA(cudaMemcpyAsync(Qblk(c, blk), c->xmat, qb, cudaMemcpyDeviceToDevice, s));
   return cal_g_and_det(c, c->xmat, Qblk(c, blk - 1), true);
 }
@@ -723,6 +516,8 @@ int chain_alloc(pqmc_chain* c, const pqmc_model* m, cudaStream_t s) {
   PQMC_TRY(dalloc(&c->g_alt, (size_t)c->ns * c->ns));
   PQMC_TRY(dalloc(&c->q_string, (size_t)c->ns * c->nelec * c->nblock));
   PQMC_TRY(dalloc(&c->d_string, (size_t)c->nelec * c->nblock));
+  PQMC_TRY(dalloc(&c->d_logsum, (size_t)c->nblock));
+  PQMC_CUDA(cudaMemset(c->d_logsum, 0, sizeof(cplx) * (size_t)c->nblock));
   PQMC_TRY(dalloc(&c->slater_q, (size_t)c->ns * c->nelec));
   PQMC_TRY(dalloc(&c->slater_d, (size_t)c->nelec));
   PQMC_TRY(dalloc(&c->rmat, (size_t)c->ns * c->nelec));
@@ -779,17 +574,23 @@ int chain_alloc(pqmc_chain* c, const pqmc_model* m, cudaStream_t s) {
     PQMC_CUDA(cudaMemcpy(w.d_sites, isites.data(), sizeof(int) * isites.size(), cudaMemcpyHostToDevice));
     PQMC_CUDA(cudaMemcpy(w.d_dim, idim.data(), sizeof(int) * idim.size(), cudaMemcpyHostToDevice));
   }
-  // cooperative grid of the update kernel
-  long elems = (long)c->ns * c->ns;
-  int want = 1 + (int)((elems + 1023) / 1024);
-  if (want < 2) want = 2;
-  c->upd_blocks = coop_grid((const void*)k_update, 256, want);
-  if (c->upd_blocks < 2) { set_error("update kernel needs two co-resident blocks"); return PQMC_ERR_CUDA; }
-  return PQMC_OK;
+  // one boson per plaquette within a family: the proposals of a family are
+  // then independent of each other until the determinant ratio
+  for (int f = 0; f < npf; ++f) {
+    if (!m->pf_v_exist[f]) continue;
+    std::vector<int> seen(c->n_bf, 0);
+    for (int p = 0; p < m->pf_npla[f]; ++p)
+      if (seen[m->bf_list[p + mp * f]]++) {
+        set_error("pqmc_create: family %d couples boson %d to two plaquettes", f + 1, m->bf_list[p + mp * f]);
+        return PQMC_ERR_ARG;
+      }
+  }
+  PQMC_TRY(dalloc(&c->pre, (size_t)mp));
+  return update_setup(c);
 }
 
 int chain_free(pqmc_chain* c) {
-  void* ptrs[] = {c->d_model_blob, c->field, c->expkv, c->expkv_inv, c->g, c->g_alt, c->q_string, c->d_string,
+  void* ptrs[] = {c->d_logsum, c->pre, c->d_model_blob, c->field, c->expkv, c->expkv_inv, c->g, c->g_alt, c->q_string, c->d_string,
                   c->slater_q, c->slater_d, c->rmat, c->xmat, c->lmat, c->pbp, c->tau, c->dtmp, c->lcol,
                   c->ipiv, c->ctl, c->sc, c->m_cell_sites, c->m_cell_bf, c->m_cell_xnb, c->m_cell_ynb,
                   c->m_cell_cross, c->m_c2_of, c->m_kphase, c->m_acc, c->m_gtmp};

@@ -34,6 +34,21 @@ struct UpdCtl {
   cplx T[16];
 };
 
+// Per-plaquette proposal data of one family step, computed in parallel
+// before the sequential Metropolis scan (every proposal consumes a fixed
+// number of ran2 draws, so jumps, energies and propagators do not depend on
+// earlier accepts).
+struct PlaqPre {
+  cplx delta[16];   // Delta = expKV_inv(old) expKV(new) - I
+  cplx enew[16];    // expKV(new)
+  cplx einv[16];    // expKV_inv(new)
+  float2 deltaf[16];// Delta rounded to FP32 for the fast test
+  double dE;        // -dtau * (E_new - E_old)
+  double xnew;
+  double r;         // acceptance draw rands()
+  double thr;       // accept iff |det R|^2 >= thr (the Metropolis test of cal_prob)
+};
+
 struct WrapItems {        // cover of all sites by one family: plaquettes + singletons
   int n_items;
   int* d_pla;             // (n_items) plaquette index or -1
@@ -57,6 +72,7 @@ struct pqmc_chain {
   cplx* g_alt = nullptr;            // ping-pong partner
   cplx* q_string = nullptr;         // (Ns,nelec,nblock)
   cplx* d_string = nullptr;         // (nelec,nblock)
+  cplx* d_logsum = nullptr;         // (nblock) sum_i log D(i,block)
   cplx* slater_q = nullptr;
   cplx* slater_d = nullptr;
   cplx* rmat = nullptr;             // (Ns,nelec)
@@ -68,6 +84,7 @@ struct pqmc_chain {
   cplx* lcol = nullptr;             // (nelec)
   int* ipiv = nullptr;              // (nelec)
   pqmc::UpdCtl* ctl = nullptr;      // [2]
+  pqmc::PlaqPre* pre = nullptr;     // (max_pla)
   pqmc::DevScalars* sc = nullptr;
   std::vector<pqmc::WrapItems> wrap;
   int upd_blocks = 0;
@@ -94,11 +111,13 @@ int chain_alloc(pqmc_chain* c, const pqmc_model* m, cudaStream_t s);
 int chain_free(pqmc_chain* c);
 int launch_init_expkv(pqmc_chain* c);
 int launch_update(pqmc_chain* c, int pf, int time);
+int update_setup(pqmc_chain* c);
 int launch_wrap(pqmc_chain* c, int pf, int time, bool left);
 int launch_propagate(pqmc_chain* c, cplx* X, int n, int t_from, int t_to, bool forward);
 int do_init_g(pqmc_chain* c, int start_time);
 int do_g_scratch(pqmc_chain* c, int time, bool forward, int loop);
 int do_new_weight(pqmc_chain* c);
+int block_log(pqmc_chain* c, int blk1);
 int do_measure(pqmc_chain* c, int time);
 int do_finish_record(pqmc_chain* c, int meas_number);
 }  // namespace pqmc

@@ -1,0 +1,44 @@
+// recompute_b.cuh -- batched stabilised recompute (recompute_b.cu)
+#pragma once
+#include <vector>
+#include "chain.cuh"
+
+struct dfc;
+
+namespace pqmc {
+struct GemmArgs;
+struct CholArgs;
+struct GJArgs;
+struct PropArgs;
+struct WeightArgs;
+
+struct BatchRecompute {
+  int C = 0, ns = 0, ne = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<pqmc_chain*> cs;
+  GemmArgs* d_gemm = nullptr;
+  CholArgs* d_chol = nullptr;
+  GJArgs* d_gj = nullptr;
+  PropArgs* d_prop = nullptr;
+  WeightArgs* d_weight = nullptr;
+  ::dfc* work_df = nullptr;
+  cplx* tmpX = nullptr;
+  cplx* gram = nullptr;
+  cplx* rinv = nullptr;
+  cplx* pbp = nullptr;
+  cplx* wmat = nullptr;
+  cplx* logdet = nullptr;
+  cplx* piv = nullptr;
+  int* perm = nullptr;
+  int* status = nullptr;
+
+  ~BatchRecompute();
+  int setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s);
+  int gemm(char ta, char tb, int m, int n, int k, const std::vector<GemmArgs>& a, int slot, int accumulate);
+  int cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*>& D);
+  int g_and_det(const std::vector<cplx*>& XL, const std::vector<cplx*>& R, const std::vector<cplx*>& Gcur,
+                const std::vector<cplx*>& Gnew, bool compare, int blk1);
+  int propagate(const std::vector<cplx*>& X, int t_from, int t_to, bool forward);
+  int scratch(int time, bool forward);
+};
+}  // namespace pqmc

@@ -185,4 +185,49 @@ def kernel_launches() -> int:
     return int(load_library().pqmc_kernel_launches())
 
 
-__all__ = ["PqmcChain", "PqmcError", "kernel_launches"]
+__all__ = ["PqmcChain", "PqmcBatch", "PqmcError", "kernel_launches"]
+
+
+class PqmcBatch:
+    """Many chains advanced together (PQMC_PREC_FP64 or PQMC_PREC_MIXED).
+
+    Each chain keeps the single-chain interface (``chains[i]``) for set-up,
+    inspection and measurement; ``sweep(loop)`` advances every chain by one
+    sweep of Main_PQMC.f90:99-154 (no measurement)."""
+
+    def __init__(self, models, fields, rng_words, *, precision: int = 1, meas: bool | None = False):
+        self.lib = load_library()
+        self.models = list(models)
+        self._ms = [ModelStruct(m) for m in self.models]
+        arr = (ctypes.POINTER(type(self._ms[0].s)) * len(self._ms))(
+            *[ctypes.pointer(x.s) for x in self._ms])
+        h = ctypes.c_void_p()
+        check(self.lib, self.lib.pqmc_batch_create(arr, len(self._ms), precision, ctypes.byref(h)),
+              "pqmc_batch_create")
+        self.h = h
+        self.chains = []
+        for i, (m, f, w) in enumerate(zip(self.models, fields, rng_words)):
+            ch = ctypes.c_void_p()
+            check(self.lib, self.lib.pqmc_batch_chain(self.h, i, ctypes.byref(ch)), "pqmc_batch_chain")
+            self.chains.append(PqmcChain(m, field=f, rng_words=w, meas=meas, handle=ch))
+
+    def init(self):
+        for c in self.chains:
+            c.init_expkv()
+            c.init_g(1)
+
+    def sweep(self, loop: int):
+        check(self.lib, self.lib.pqmc_batch_sweep(self.h, loop), "pqmc_batch_sweep")
+
+    def close(self):
+        if getattr(self, "h", None) is not None:
+            for c in self.chains:
+                c.h = None
+            self.lib.pqmc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

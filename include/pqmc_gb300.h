@@ -252,6 +252,28 @@ int pqmc_batch_chain(pqmc_batch* batch, int i, pqmc_chain** chain);
 /* one sweep of every chain (Main_PQMC.f90:99-154), no measurement */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
 
+/* ---- recompute without device allocation ---------------------------- */
+/* No counterpart in the reference.  g_out = R (X^H R)^-1 X^H and
+ * logdet_out = log det(X^H R) (complex), i.e. cal_g_and_det_T0 without the
+ * D-string and TR/ncopy terms, for callers that cannot call cudaMalloc (code
+ * running under CUDA-graph stream capture, hosts that give the device to a
+ * fixed memory arena, Fortran drivers bound only to this library).  All
+ * pointers are DEVICE pointers: x_left and rmat are Ns x nelec complex,
+ * column-major; g_out is Ns x Ns; logdet_out holds 2 doubles.  `stream` is a
+ * cudaStream_t (NULL: legacy default stream); the call returns after the
+ * stream has finished it.
+ * Work space: one file-scope device array of about 3.2 MB, reserved when the
+ * library loads and held by every GPU that loads it until the process exits.
+ * Sizes above PQMC_NOALLOC_MAX_NS / PQMC_NOALLOC_MAX_NELEC return
+ * PQMC_ERR_ARG.  Every call shares that array: calls that overlap on the GPU
+ * race.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture begins. */
+#define PQMC_NOALLOC_MAX_NS 512
+#define PQMC_NOALLOC_MAX_NELEC 256
+int pqmc_cal_g_and_det_noalloc(const double* x_left, const double* rmat, int ns, int nelec, double* g_out,
+                               double* logdet_out, void* stream);
+
 /* ---- introspection --------------------------------------------------- */
 const char* pqmc_version(void);
 const char* pqmc_last_error(void);

@@ -239,6 +239,22 @@ int pqmc_sweep(pqmc_chain* chain, int first_loop, int n_sweeps, int warmup,
                int meas_interval, int meas_number, double* records,
                int n_records_cap, int* n_records);
 
+/* ---- differentiable log-weight ---------------------------------------- */
+/* boson_field from a DEVICE pointer (n_bf, ntime), e.g. a torch tensor. */
+int pqmc_set_field_device(pqmc_chain* chain, const double* boson_field_dev);
+/* Value and gradient of the projector log-weight
+ *   W = Re log det(P^H B(Lt..1) P)  (cal_new_weight_T0, mod_evolution.f90:359)
+ * with respect to every boson_field(b,tau).  The value goes to logw_out
+ * (host, complex, as cal_new_weight_T0 returns it); the gradient of Re W
+ * goes to grad_dev (DEVICE, (n_bf, ntime) doubles).  The gradient is the
+ * Green's-function trace formula Re Tr[E^-1 dE/dx G] per plaquette, by a
+ * right-to-left pass that checkpoints the orthonormal left factor every
+ * ngroup slices and a left-to-right pass that recomputes G from the
+ * checkpoints and wraps it through each block.  Needs init_expkv/init_g
+ * (with the current field) first; leaves G and the Q/D strings as they were
+ * (the rank's fast-update state is not disturbed). */
+int pqmc_logweight_grad(pqmc_chain* chain, double* logw_out, double* grad_dev);
+
 /* ---- batched, mixed precision --------------------------------------- */
 typedef struct pqmc_batch pqmc_batch; /* many chains in one device context */
 #define PQMC_PREC_FP64 0   /* every product in FP64                        */
@@ -249,6 +265,9 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains,
                       int precision, pqmc_batch** out);
 int pqmc_batch_destroy(pqmc_batch* batch);
 int pqmc_batch_chain(pqmc_batch* batch, int i, pqmc_chain** chain);
+/* delay depth of the mixed-precision update: panel columns folded into G
+ * per tensor-core flush (default 64, at most 512) */
+int pqmc_batch_set_delay(pqmc_batch* batch, int depth);
 /* one sweep of every chain (Main_PQMC.f90:99-154), no measurement */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
 

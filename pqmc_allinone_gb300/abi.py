@@ -170,11 +170,14 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                                 ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "pqmc_sweep": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                         _f64p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "pqmc_set_field_device": ([vp, ctypes.c_void_p], ctypes.c_int),
+        "pqmc_logweight_grad": ([vp, _f64p, ctypes.c_void_p], ctypes.c_int),
         "pqmc_batch_create": ([ctypes.POINTER(ctypes.POINTER(PqmcModel)), ctypes.c_int, ctypes.c_int,
                                ctypes.POINTER(vp)], ctypes.c_int),
         "pqmc_batch_destroy": ([vp], ctypes.c_int),
         "pqmc_batch_chain": ([vp, ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
         "pqmc_batch_sweep": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_set_delay": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_version": ([], ctypes.c_char_p),
         "pqmc_last_error": ([], ctypes.c_char_p),
         "pqmc_kernel_launches": ([], ctypes.c_int64),

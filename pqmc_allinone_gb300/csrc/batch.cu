@@ -55,7 +55,7 @@ __device__ __forceinline__ float2 fsb(float2 a, float2 b) { return make_float2(a
 __global__ void k_bdraw(BDesc* D, int C, int pf) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
-  BDesc& d = D[c];
+  const BDesc d = D[c];
   const int npla = d.M.pf_npla[pf];
   Ran2Dev rng;
   rng.iran = d.sc->rng[0]; rng.jran = d.sc->rng[1]; rng.kran = d.sc->rng[2];
@@ -88,8 +88,11 @@ __device__ __forceinline__ double b_threshold(const DevModel& M, double dE, doub
   return pow(q, 2.0 / n);
 }
 
-__global__ void __launch_bounds__(256) k_bprep(BDesc* D, int pf, int t) {
-  BDesc& d = D[blockIdx.y];
+__global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf, int t) {
+  __shared__ BDesc sd;
+  if (threadIdx.x == 0) sd = D[blockIdx.y];
+  __syncthreads();
+  const BDesc& d = sd;
   const DevModel& M = d.M;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int npla = M.pf_npla[pf], dim = M.pf_dim[pf], pd = M.pdim;
@@ -153,113 +156,175 @@ __global__ void __launch_bounds__(256) k_bprep(BDesc* D, int pf, int t) {
 }
 
 // ---------------------------------------------------------------------------
-// Sequential scan with delayed updates, one CTA per chain.
+// Sequential scan with delayed updates, one CTA per chain.  The scan resumes
+// at the chain's next plaquette and stops when the panels hold `kd` columns
+// (the delay depth); k_bflush then folds them into G and the next round
+// continues.  Ratios, R^-1 and T are FP32 (the panels are FP32); the weight
+// ln_cw is accumulated in FP64.
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_KSTAGE = 512;   // panel columns staged in shared memory (4*Kmax)
+constexpr int SCAN_KSTAGE = 512;   // max delay depth (panel columns)
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_bscan(BDesc* D, int pf, int t, int parity) {
-  BDesc& d = D[blockIdx.x];
+__device__ __forceinline__ float2 fdiv1(float2 a) {   // 1/a
+  float n = a.x * a.x + a.y * a.y;
+  return make_float2(a.x / n, -a.y / n);
+}
+
+// 4x4 (or smaller) complex inverse in FP32 by Gauss-Jordan with partial
+// pivoting on one thread
+__device__ void finv_small(int n, float2* a) {
+  float2 inv[16];
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) inv[i + n * j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+  for (int j = 0; j < n; ++j) {
+    int jp = j;
+    float best = -1.f;
+    for (int i = j; i < n; ++i) {
+      float v = fabsf(a[i + n * j].x) + fabsf(a[i + n * j].y);
+      if (v > best) { best = v; jp = i; }
+    }
+    if (jp != j)
+      for (int k = 0; k < n; ++k) {
+        float2 t = a[j + n * k]; a[j + n * k] = a[jp + n * k]; a[jp + n * k] = t;
+        t = inv[j + n * k]; inv[j + n * k] = inv[jp + n * k]; inv[jp + n * k] = t;
+      }
+    float2 r = fdiv1(a[j + n * j]);
+    for (int k = 0; k < n; ++k) { a[j + n * k] = fm(a[j + n * k], r); inv[j + n * k] = fm(inv[j + n * k], r); }
+    for (int i = 0; i < n; ++i) {
+      if (i == j) continue;
+      float2 f = a[i + n * j];
+      for (int k = 0; k < n; ++k) {
+        a[i + n * k] = fsb(a[i + n * k], fm(f, a[j + n * k]));
+        inv[i + n * k] = fsb(inv[i + n * k], fm(f, inv[j + n * k]));
+      }
+    }
+  }
+  for (int k = 0; k < n * n; ++k) a[k] = inv[k];
+}
+
+__device__ float2 fdet_small(int n, const float2* a) {
+  if (n == 1) return a[0];
+  if (n == 2) return fsb(fm(a[0], a[3]), fm(a[2], a[1]));
+  // Gauss elimination with partial pivoting on a copy
+  float2 b[16];
+  for (int k = 0; k < n * n; ++k) b[k] = a[k];
+  float2 det = make_float2(1.f, 0.f);
+  for (int j = 0; j < n; ++j) {
+    int jp = j;
+    float best = -1.f;
+    for (int i = j; i < n; ++i) {
+      float v = fabsf(b[i + n * j].x) + fabsf(b[i + n * j].y);
+      if (v > best) { best = v; jp = i; }
+    }
+    if (jp != j) {
+      for (int k = 0; k < n; ++k) { float2 t = b[j + n * k]; b[j + n * k] = b[jp + n * k]; b[jp + n * k] = t; }
+      det = make_float2(-det.x, -det.y);
+    }
+    det = fm(det, b[j + n * j]);
+    float2 r = fdiv1(b[j + n * j]);
+    for (int i = j + 1; i < n; ++i) {
+      float2 f = fm(b[i + n * j], r);
+      for (int k = j; k < n; ++k) b[i + n * k] = fsb(b[i + n * k], fm(f, b[j + n * k]));
+    }
+  }
+  return det;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int t, int parity, int kd, int* next_p) {
+  __shared__ BDesc sd;
+  if (threadIdx.x == 0) sd = D[blockIdx.x];
+  __syncthreads();
+  const BDesc& d = sd;
   const DevModel& M = d.M;
   const int ns = M.ns, npla = M.pf_npla[pf], dim = M.pf_dim[pf], pd = M.pdim;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int p0 = next_p[blockIdx.x];
+  if (p0 >= npla) {
+    if (tid == 0) *d.kcount = 0;
+    return;
+  }
   const cplx* G = parity ? d.g_alt : d.g;
   float2* A = d.A;
   float2* B = d.B;
   PlaqPre* pre = d.pre;
   __shared__ int s_S[4];
-  __shared__ float2 s_corr[16];
-  __shared__ cplx s_r[16], s_cof[16], s_inv[16], s_T[16];
-  __shared__ float2 s_Tf[16];
+  __shared__ float2 s_g[16], s_r[16], s_T[16];
   __shared__ int s_dec;
-  __shared__ float2 s_BS[4 * SCAN_KSTAGE];   // B(q, S_m) for q < K, m < dim
+  __shared__ float2 s_BS[4 * SCAN_KSTAGE];   // B(q, S_m)
   __shared__ float2 s_AS[4 * SCAN_KSTAGE];   // A(S_l, q)
   int K = 0;
   double lprod = 1.0;
   long long lexp = 0, pa = 0, na = 0;
-  for (int p = 0; p < npla; ++p) {
+  int p = p0;
+  for (; p < npla; ++p) {
+    if (K + dim > kd) break;
     if (tid < dim) s_S[tid] = M.site[tid + pd * (p + M.max_pla * pf)];
     __syncthreads();
-    // correction of G_SS by the delayed panels: (A B)(S_i, S_j)
-    {
-      const int e = tid >> 4, part = tid & 15;
-      float2 acc = make_float2(0.f, 0.f);
-      if (e < dim * dim) {
-        const int si = s_S[e % dim], sj = s_S[e / dim];
-        for (int q = part; q < K; q += 16) acc = fa(acc, fm(A[(size_t)q * ns + si], B[(size_t)q * ns + sj]));
-      }
-      for (int o = 8; o > 0; o >>= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-      }
-      if (part == 0 && e < dim * dim) s_corr[e] = acc;
+    // stage A(S,:), B(:,S) for q < K (one round trip), and G(S,S)
+    for (int e = tid; e < K * dim; e += blockDim.x) {
+      int q = e / dim, m = e % dim;
+      s_BS[e] = B[(size_t)q * ns + s_S[m]];
+      s_AS[e] = A[(size_t)q * ns + s_S[m]];
     }
+    if (tid < dim * dim) s_g[tid] = f2(G[s_S[tid % dim] + (size_t)ns * s_S[tid / dim]]);
     __syncthreads();
     const PlaqPre* pp = pre + p;
     if (warp == 0) {
       const int i = lane % dim, j = lane / dim;
       const bool act = lane < dim * dim;
-      // R = I + (G_SS + corr) Delta in FP64
-      cplx gv = mk(0.0);
+      // G_eff(S,S) = G(S,S) + (A B)(S,S)
+      float2 gv = make_float2(0.f, 0.f);
       if (act) {
-        gv = G[s_S[i] + (size_t)ns * s_S[j]];
-        gv = cadd(gv, mk((double)s_corr[lane].x, (double)s_corr[lane].y));
-        s_cof[lane] = gv;
+        gv = s_g[lane];
+        for (int q = 0; q < K; ++q) gv = fa(gv, fm(s_AS[q * dim + i], s_BS[q * dim + j]));
       }
       __syncwarp();
+      if (act) s_g[lane] = gv;
+      __syncwarp();
+      // R = I + G_eff(S,S) Delta
       if (act) {
-        cplx a = mk(0.0);
-        for (int k = 0; k < dim; ++k) a = cadd(a, cmul(s_cof[i + dim * k], pp->delta[k + dim * j]));
-        if (i == j) a = cadd(a, mk(1.0));
+        float2 a = make_float2(i == j ? 1.f : 0.f, 0.f);
+        for (int k = 0; k < dim; ++k) a = fa(a, fm(s_g[i + dim * k], pp->deltaf[k + dim * j]));
         s_r[lane] = a;
       }
       __syncwarp();
-      cplx det = warp_det(dim, s_r, lane);
-      int acc = (det.x * det.x + det.y * det.y) >= pp->thr;
-      if (acc) {
-        // inverse and T = Delta R^-1 (FP64)
-        if (dim == 4) {
-          const int ci = lane & 3, cj = lane >> 2;
-          if (lane < 16) {
-            int r3[3], c3[3], n = 0;
-            for (int k = 0; k < 4; ++k)
-              if (k != ci) r3[n++] = k;
-            n = 0;
-            for (int k = 0; k < 4; ++k)
-              if (k != cj) c3[n++] = k;
-#define S3(a_, b_) s_r[r3[a_] + 4 * c3[b_]]
-            cplx cof = cadd(csub(cmul(S3(0, 0), csub(cmul(S3(1, 1), S3(2, 2)), cmul(S3(1, 2), S3(2, 1)))),
-                                 cmul(S3(0, 1), csub(cmul(S3(1, 0), S3(2, 2)), cmul(S3(1, 2), S3(2, 0))))),
-                            cmul(S3(0, 2), csub(cmul(S3(1, 0), S3(2, 1)), cmul(S3(1, 1), S3(2, 0)))));
-#undef S3
-            if ((ci + cj) & 1) cof = cneg(cof);
-            cplx rd = cdiv(mk(1.0), det);
-            s_inv[cj + 4 * ci] = cmul(cof, rd);
-          }
-          __syncwarp();
-        } else {
-          if (lane < dim * dim) s_inv[lane] = s_r[lane];
-          __syncwarp();
-          if (lane == 0) dev_inverse_small(dim, s_inv);
-          __syncwarp();
-        }
-        if (act) {
-          cplx a = mk(0.0);
-          for (int k = 0; k < dim; ++k) a = cadd(a, cmul(pp->delta[i + dim * k], s_inv[k + dim * j]));
-          s_T[lane] = a;
-          s_Tf[lane] = f2(a);
-        }
-        if (lane == 0) {
+      int acc = 0;
+      if (lane == 0) {
+        float2 det = fdet_small(dim, s_r);
+        double d2 = (double)det.x * det.x + (double)det.y * det.y;
+        acc = d2 >= pp->thr;
+        if (acc) {
           pa++;
-          cplx relec = det;
-          if (M.tr_weight) relec = cmul(relec, cconj(relec));
-          cplx base = relec, ac = mk(1.0);
-          for (int k = 0; k < M.ncopy; ++k) ac = cmul(ac, base);
+          double relr;
+          {
+            double dr = det.x, di = det.y;
+            double rr = dr, ri = di;
+            if (M.tr_weight) { rr = dr * dr + di * di; ri = 0.0; }
+            double ar = 1.0, ai = 0.0;
+            for (int k = 0; k < M.ncopy; ++k) {
+              double tr = ar * rr - ai * ri;
+              ai = ar * ri + ai * rr;
+              ar = tr;
+            }
+            relr = ar;
+          }
           int ex;
-          lprod *= frexp(ac.x, &ex);
+          lprod *= frexp(relr, &ex);
           lexp += ex;
           lprod = frexp(lprod, &ex);
           lexp += ex;
           d.field[M.bf[p + M.max_pla * pf] + (size_t)M.n_bf * t] = pp->xnew;
+          finv_small(dim, s_r);   // R^-1
+        } else {
+          na++;
+        }
+      }
+      acc = __shfl_sync(0xffffffffu, acc, 0);
+      __syncwarp();
+      if (acc) {
+        if (act) {
+          float2 a = make_float2(0.f, 0.f);
+          for (int k = 0; k < dim; ++k) a = fa(a, fm(pp->deltaf[i + dim * k], s_r[k + dim * j]));
+          s_T[lane] = a;
         }
         const size_t base2 = M.kv_base(p, pf, t);
         if (lane < pd * pd) {
@@ -268,24 +333,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(BDesc* D, int pf, int t,
           d.expkv[base2 + lane] = in ? pp->enew[ii + dim * jj] : mk(0.0);
           d.expkv_inv[base2 + lane] = in ? pp->einv[ii + dim * jj] : mk(0.0);
         }
-      } else if (lane == 0) {
-        na++;
       }
       if (lane == 0) s_dec = acc;
     }
     __syncthreads();
     if (!s_dec) continue;
-    if (K + dim > d.kmax) {   // cannot happen: kmax = n_plaquette * dim of the largest family
-      if (tid == 0) d.sc->status = PQMC_ERR_STATE;
-      continue;
-    }
-    // stage B(q, S_m) and A(S_l, q) for q < K
-    for (int e = tid; e < K * dim; e += blockDim.x) {
-      int q = e / dim, m = e % dim;
-      s_BS[e] = B[(size_t)q * ns + s_S[m]];
-      s_AS[e] = A[(size_t)q * ns + s_S[m]];
-    }
-    __syncthreads();
     // new panel block: a(r,l) = sum_m Geff(r,S_m) T(m,l),  b(l,c) = delta(S_l,c) - Geff(S_l,c)
     for (int r = tid; r < ns; r += blockDim.x) {
       float2 gm[4], bl[4];
@@ -293,6 +345,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(BDesc* D, int pf, int t,
         gm[m] = f2(G[r + (size_t)ns * s_S[m]]);
         bl[m] = f2(G[s_S[m] + (size_t)ns * r]);
       }
+#pragma unroll 4
       for (int q = 0; q < K; ++q) {
         float2 ar = A[(size_t)q * ns + r];
         float2 bc = B[(size_t)q * ns + r];
@@ -303,7 +356,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(BDesc* D, int pf, int t,
       }
       for (int l = 0; l < dim; ++l) {
         float2 a = make_float2(0.f, 0.f);
-        for (int m = 0; m < dim; ++m) a = fa(a, fm(gm[m], s_Tf[m + dim * l]));
+        for (int m = 0; m < dim; ++m) a = fa(a, fm(gm[m], s_T[m + dim * l]));
         A[(size_t)(K + l) * ns + r] = a;
         float2 bv = make_float2(-bl[l].x, -bl[l].y);
         if (r == s_S[l]) bv.x += 1.f;
@@ -315,6 +368,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(BDesc* D, int pf, int t,
   }
   if (tid == 0) {
     *d.kcount = K;
+    next_p[blockIdx.x] = p;
     if (pa > 0) {
       double l = (lprod > 0.0) ? log(lprod) + (double)lexp * 0.69314718055994530942 : log(lprod);
       d.sc->ln_cw = cadd(d.sc->ln_cw, mk(l));
@@ -347,8 +401,11 @@ __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-__global__ void __launch_bounds__(256) k_bflush(BDesc* D, int parity) {
-  BDesc& d = D[blockIdx.y];
+__global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
+  __shared__ BDesc sd;
+  if (threadIdx.x == 0) sd = D[blockIdx.y];
+  __syncthreads();
+  const BDesc& d = sd;
   const int K = *d.kcount;
   if (K == 0) return;
   const int ns = d.M.ns;
@@ -432,8 +489,11 @@ __global__ void __launch_bounds__(256) k_bflush(BDesc* D, int parity) {
 
 // ---------------------------------------------------------------------------
 // Two-way wrap with an FP32 correction on the FP64 G (left: A=expKV, B=expKV_inv).
-__global__ void k_bwrap(BDesc* D, int pf, int t, int left, int n_items, int parity) {
-  BDesc& d = D[blockIdx.y];
+__global__ void k_bwrap(const BDesc* D, int pf, int t, int left, int n_items, int parity) {
+  __shared__ BDesc sd;
+  if (threadIdx.x == 0) sd = D[blockIdx.y];
+  __syncthreads();
+  const BDesc& d = sd;
   const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (pair >= (long)n_items * n_items) return;
   const DevModel& M = d.M;
@@ -496,6 +556,8 @@ struct pqmc_batch {
   std::vector<float2*> panels;
   std::vector<int*> kcounts;
   int parity = 0;
+  int kd = 64;            // delay depth (panel columns per flush)
+  int* d_next = nullptr;  // per chain: next plaquette of the current family step
   cudaStream_t stream = nullptr;
   pqmc::BatchRecompute rec;
 };
@@ -553,16 +615,22 @@ static int bwrap(pqmc_batch* b, int pf, int time, bool left) {
 static int bupdate(pqmc_batch* b, int pf, int time) {
   const int C = (int)b->chains.size();
   pqmc_chain* c0 = b->chains[0];
-  const int npla = c0->h_pf_npla[pf];
+  const int npla = c0->h_pf_npla[pf], dim = c0->h_pf_dim[pf];
   k_bdraw<<<(C + 63) / 64, 64, 0, b->stream>>>(b->d_desc, C, pf);
   PQMC_LAUNCHED();
   k_bprep<<<dim3((npla + 7) / 8, C), 256, 0, b->stream>>>(b->d_desc, pf, time - 1);
   PQMC_LAUNCHED();
-  k_bscan<<<C, SCAN_THREADS, 0, b->stream>>>(b->d_desc, pf, time - 1, b->parity);
-  PQMC_LAUNCHED();
+  PQMC_CUDA(cudaMemsetAsync(b->d_next, 0, sizeof(int) * C, b->stream));
+  const int kd = std::max(dim, std::min(b->kd, b->h_desc[0].kmax));
+  // enough rounds for the worst case (every proposal accepted)
+  const int rounds = (npla * dim + (kd / dim) * dim - 1) / ((kd / dim) * dim);
   const int tiles = ((c0->ns + FB_M - 1) / FB_M) * ((c0->ns + FB_N - 1) / FB_N);
-  k_bflush<<<dim3(tiles, C), 256, 0, b->stream>>>(b->d_desc, b->parity);
-  PQMC_LAUNCHED();
+  for (int r = 0; r < rounds; ++r) {
+    k_bscan<<<C, SCAN_THREADS, 0, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->d_next);
+    PQMC_LAUNCHED();
+    k_bflush<<<dim3(tiles, C), 256, 0, b->stream>>>(b->d_desc, b->parity);
+    PQMC_LAUNCHED();
+  }
   return PQMC_OK;
 }
 
@@ -634,6 +702,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     b->kcounts.push_back(kc);
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
+  PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
   if (precision == PQMC_PREC_MIXED) PQMC_TRY(b->rec.setup(b->chains, b->stream));
   PQMC_TRY(batch_refresh(b));
   PQMC_CUDA(cudaStreamSynchronize(b->stream));
@@ -650,8 +719,15 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   for (auto* k : b->kcounts)
     if (k) cudaFree(k);
   if (b->d_desc) cudaFree(b->d_desc);
+  if (b->d_next) cudaFree(b->d_next);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
+  return PQMC_OK;
+}
+
+int pqmc_batch_set_delay(pqmc_batch* b, int kd) {
+  if (!b || kd < 1 || kd > SCAN_KSTAGE) { set_error("batch_set_delay: depth must be in 1..%d", SCAN_KSTAGE); return PQMC_ERR_ARG; }
+  b->kd = kd;
   return PQMC_OK;
 }
 

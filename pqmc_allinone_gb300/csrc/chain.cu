@@ -89,7 +89,7 @@ __global__ void k_wrap(DevModel M, int pf, int t, int left, int n_items, const i
       cplx s;
       if (A) {
         s = mk(0.0);
-        for (int k = 0; k < dr; ++k) s = cadd(s, cmul(A[a + pd * k], g[k + 4 * b]));
+        for (int k = 0; k < dr; ++k) s = cfma(A[a + pd * k], g[k + 4 * b], s);
       } else {
         s = g[a + 4 * b];
       }
@@ -100,7 +100,7 @@ __global__ void k_wrap(DevModel M, int pf, int t, int left, int n_items, const i
       cplx s;
       if (B) {
         s = mk(0.0);
-        for (int k = 0; k < dc; ++k) s = cadd(s, cmul(h[a + 4 * k], B[k + pd * b]));
+        for (int k = 0; k < dc; ++k) s = cfma(h[a + 4 * k], B[k + pd * b], s);
       } else {
         s = h[a + 4 * b];
       }
@@ -153,7 +153,7 @@ __global__ void k_propagate(DevModel M, cplx* X, int ldx, int t_from, int t_to, 
           cplx s = mk(0.0);
           for (int k = 0; k < dim; ++k) {
             cplx e = forward ? E[a + pd * k] : cconj(E[k + pd * a]);
-            s = cadd(s, cmul(e, v[k]));
+            s = cfma(e, v[k], s);
           }
           col[S[a]] = s;
         }
@@ -887,7 +887,7 @@ __global__ void k_propagate_one(DevModel M, cplx* X, int ldx, int t, int pf, int
       cplx s = mk(0.0);
       for (int k = 0; k < dim; ++k) {
         cplx e = forward ? E[a + pd * k] : cconj(E[k + pd * a]);
-        s = cadd(s, cmul(e, v[k]));
+        s = cfma(e, v[k], s);
       }
       col[S[a]] = s;
     }

@@ -17,6 +17,11 @@ __host__ __device__ __forceinline__ cplx cmul(cplx a, cplx b) {
   return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __host__ __device__ __forceinline__ cplx cscale(cplx a, double s) { return mk(a.x * s, a.y * s); }
+// a + x*y with four fused multiply-adds (the FP64 pipe issues one warp
+// instruction per 32 ns on GB300, so instruction count is what matters)
+__host__ __device__ __forceinline__ cplx cfma(cplx x, cplx y, cplx a) {
+  return mk(fma(x.x, y.x, fma(-x.y, y.y, a.x)), fma(x.x, y.y, fma(x.y, y.x, a.y)));
+}
 __host__ __device__ __forceinline__ cplx cconj(cplx a) { return mk(a.x, -a.y); }
 // conj(a)*b
 __host__ __device__ __forceinline__ cplx cmulc(cplx a, cplx b) {

@@ -46,10 +46,10 @@ __global__ void __launch_bounds__(256) k_zgemm(int m, int n, int k, cplx alpha, 
     for (int q = 0; q < 16; ++q) {
       cplx a0 = sA[q][tx], a1 = sA[q][tx + 16];
       cplx b0 = sB[q][ty], b1 = sB[q][ty + 16];
-      acc[0][0] = cadd(acc[0][0], cmul(a0, b0));
-      acc[1][0] = cadd(acc[1][0], cmul(a1, b0));
-      acc[0][1] = cadd(acc[0][1], cmul(a0, b1));
-      acc[1][1] = cadd(acc[1][1], cmul(a1, b1));
+      acc[0][0] = cfma(a0, b0, acc[0][0]);
+      acc[1][0] = cfma(a1, b0, acc[1][0]);
+      acc[0][1] = cfma(a0, b1, acc[0][1]);
+      acc[1][1] = cfma(a1, b1, acc[1][1]);
     }
     __syncthreads();
   }
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256) k_zgemm(int m, int n, int k, cplx alpha, 
       if (r < m && c < n) {
         cplx* p = C + r + (size_t)ldc * c;
         cplx v = cmul(alpha, acc[i][j]);
-        if (beta.x != 0.0 || beta.y != 0.0) v = cadd(v, cmul(beta, *p));
+        if (beta.x != 0.0 || beta.y != 0.0) v = cfma(beta, *p, v);
         *p = v;
       }
     }
@@ -280,7 +280,7 @@ __global__ void k_lu_solve(int n, int nrhs, const cplx* __restrict__ LU, const i
   // forward: unit lower
   for (int i = 1; i < n; ++i) {
     cplx s = mk(0.0);
-    for (int j = lane; j < i; j += 32) s = cadd(s, cmul(LU[i + (size_t)n * j], b[j]));
+    for (int j = lane; j < i; j += 32) s = cfma(LU[i + (size_t)n * j], b[j], s);
     for (int o = 16; o > 0; o >>= 1) {
       s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
       s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
@@ -290,7 +290,7 @@ __global__ void k_lu_solve(int n, int nrhs, const cplx* __restrict__ LU, const i
   }
   for (int i = n - 1; i >= 0; --i) {
     cplx s = mk(0.0);
-    for (int j = i + 1 + lane; j < n; j += 32) s = cadd(s, cmul(LU[i + (size_t)n * j], b[j]));
+    for (int j = i + 1 + lane; j < n; j += 32) s = cfma(LU[i + (size_t)n * j], b[j], s);
     for (int o = 16; o > 0; o >>= 1) {
       s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
       s.y += __shfl_xor_sync(0xffffffffu, s.y, o);

@@ -41,8 +41,8 @@ __device__ inline void wick(const MeasView& V, const int (*ls)[2], const int (*r
   for (int i = 0; i < N; ++i)
     for (int j = 0; j < N; ++j) {
       cplx m = mk(0.0);
-      m = cadd(m, cmul(GH(V, ls[i][1], ls[i][0]), GH(V, rs[j][1], rs[j][0])));
-      if (!hartree) m = cadd(m, cmul(GH(V, rs[j][1], ls[i][0]), GG(V, ls[i][1], rs[j][0])));
+      m = cfma(GH(V, ls[i][1], ls[i][0]), GH(V, rs[j][1], rs[j][0]), m);
+      if (!hartree) m = cfma(GH(V, rs[j][1], ls[i][0]), GG(V, ls[i][1], rs[j][0]), m);
       mat[i + N * j] = m;
     }
 }
@@ -82,8 +82,8 @@ __device__ __forceinline__ cplx contract(const cplx* vl, const cplx* m, const cp
   cplx tot = mk(0.0);
   for (int i = 0; i < N; ++i) {
     cplx w = mk(0.0);
-    for (int j = 0; j < N; ++j) w = cadd(w, cmul(m[i + N * j], vr[j]));
-    tot = cadd(tot, cmul(vl[i], w));
+    for (int j = 0; j < N; ++j) w = cfma(m[i + N * j], vr[j], w);
+    tot = cfma(vl[i], w, tot);
   }
   return tot;
 }
@@ -227,7 +227,7 @@ __global__ void k_meas_finish(int nc, double div, const cplx* __restrict__ kphas
   for (int i = 0; i < nc; ++i) {
     cplx rv = r[i];
     rv = mk(rv.x / div, rv.y / div);
-    s = cadd(s, cmul(kphase[ik + (size_t)nc * i], rv));
+    s = cfma(kphase[ik + (size_t)nc * i], rv, s);
   }
   cplx* kd = acc + PQMC_N_SCALAR + (size_t)(PQMC_N_FIELD + f) * nc;
   kd[ik] = cadd(kd[ik], mk(s.x / (double)nc, s.y / (double)nc));

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
       cplx a = mk(0.0);
       for (int k = 0; k < dim; ++k) {
         cplx ekj = shfl_c(en, k + dim * j);
-        if (act) a = cadd(a, cmul(expkv_inv[base + i + pd * k], ekj));
+        if (act) a = cfma(expkv_inv[base + i + pd * k], ekj, a);
       }
       if (act) {
         if (i == j) a = csub(a, mk(1.0));
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
           cplx gv = g0;
           if (act && has_prev) {
             cplx a = mk(0.0);
-            for (int m = 0; m < dim; ++m) a = cadd(a, cmul(s_G1[i + dim * m], s_tp[m + dim * j]));
+            for (int m = 0; m < dim; ++m) a = cfma(s_G1[i + dim * m], s_tp[m + dim * j], a);
             s_c1[lane] = a;
           }
           __syncwarp();
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
             for (int l = 0; l < dim; ++l) {
               cplx v = cneg(s_G2[l + dim * j]);
               if (s_Sp[l] == Sp[j]) v = cadd(v, mk(1.0));
-              a = cadd(a, cmul(s_c1[i + dim * l], v));
+              a = cfma(s_c1[i + dim * l], v, a);
             }
             gv = cadd(gv, a);
           }
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
           // R = I + g_h_sub * Delta    :97-100
           if (act) {
             cplx a = mk(0.0);
-            for (int k = 0; k < dim; ++k) a = cadd(a, cmul(s_g[i + dim * k], s_D[k + dim * j]));
+            for (int k = 0; k < dim; ++k) a = cfma(s_g[i + dim * k], s_D[k + dim * j], a);
             if (i == j) a = cadd(a, mk(1.0));
             s_r[lane] = a;
           }
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
             }
             __syncwarp();
             det = mk(0.0);
-            for (int k = 0; k < 4; ++k) det = cadd(det, cmul(s_r[0 + 4 * k], s_cof[0 + 4 * k]));
+            for (int k = 0; k < 4; ++k) det = cfma(s_r[0 + 4 * k], s_cof[0 + 4 * k], det);
           } else {
             det = warp_det(dim, s_r, lane);
           }
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
           }
           if (act) {
             cplx a = mk(0.0);
-            for (int k = 0; k < dim; ++k) a = cadd(a, cmul(s_D[i + dim * k], s_c1[k + dim * j]));
+            for (int k = 0; k < dim; ++k) a = cfma(s_D[i + dim * k], s_c1[k + dim * j], a);
             s_tp[lane] = a;                                                  // T = Delta R^-1  :173
             s_tpf[lane] = cf(a);
             cw->T[lane] = a;
@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
             for (int l = 0; l < dim; ++l) {
               cplx v = cneg(ldg_c(gcur + s_s[l] + (size_t)ns * col));
               if (s_s[l] == col) v = cadd(v, mk(1.0));
-              a = cadd(a, cmul(s_T[k + dim * l], v));
+              a = cfma(s_T[k + dim * l], v, a);
             }
             s_wc[k] = a;
           }
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
           for (long e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const int r = (int)(e - (long)col * ns);
             cplx a = ldg_c(gcur + e);
-            for (int k = 0; k < dim; ++k) a = cadd(a, cmul(ldg_c(gcur + r + (size_t)ns * s_s[k]), s_wc[k]));
+            for (int k = 0; k < dim; ++k) a = cfma(ldg_c(gcur + r + (size_t)ns * s_s[k]), s_wc[k], a);
             gnext[e] = a;
           }
           __syncthreads();

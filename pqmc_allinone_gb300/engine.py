@@ -160,6 +160,18 @@ class PqmcChain:
         self._chk(self.lib.pqmc_cal_new_weight(self.h, o.ctypes.data_as(_f64p)), "cal_new_weight_T0")
         return complex(o[0], o[1])
 
+    def set_field_device(self, ptr: int):
+        """boson_field from a device pointer (n_bf, ntime) column-major."""
+        self._chk(self.lib.pqmc_set_field_device(self.h, ctypes.c_void_p(ptr)), "pqmc_set_field_device")
+
+    def logweight_grad_device(self, grad_ptr: int) -> complex:
+        """Re log det(P^H B P) and its gradient (written to the device
+        buffer at grad_ptr, (n_bf, ntime) doubles)."""
+        o = np.zeros(2)
+        self._chk(self.lib.pqmc_logweight_grad(self.h, o.ctypes.data_as(_f64p), ctypes.c_void_p(grad_ptr)),
+                  "pqmc_logweight_grad")
+        return complex(o[0], o[1])
+
     def take_measurement(self, time: int):
         self._chk(self.lib.pqmc_take_measurement(self.h, time), "take_measurement")
 
@@ -218,6 +230,9 @@ class PqmcBatch:
 
     def sweep(self, loop: int):
         check(self.lib, self.lib.pqmc_batch_sweep(self.h, loop), "pqmc_batch_sweep")
+
+    def set_delay(self, depth: int):
+        check(self.lib, self.lib.pqmc_batch_set_delay(self.h, depth), "pqmc_batch_set_delay")
 
     def close(self):
         if getattr(self, "h", None) is not None:

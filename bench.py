@@ -1,15 +1,23 @@
-"""Benchmark of the projector-DQMC hot path: sweeps/s at 14x14, Lt=1000.
+"""Benchmark of the projector-DQMC hot path at 14x14 (Ns=392), Lt=1000.
 
-A step is one sweep (src/Main_PQMC.f90:99-154: Lt slices of local updates,
-two-way wraps, stabilised recompute every ngroup slices and the
-equal-time measurement) of every chain of the workload.
+Headline (default ``--workload c4_mixed``): chain-sweeps/s of 64 chains
+advanced together by the batched mixed-precision form (FP32 delayed-update
+panels, split-BF16 tensor-core flush into an FP64 G, FP64-class recompute
+every ngroup slices), next to the plain single-chain FP64 form on the same
+GPU (``plain_fp64``) and the CPU oracle on the host cores.
+
+A step is one stabilisation block: ngroup=10 consecutive slices of the
+sweep loop (src/Main_PQMC.f90:99-154: per slice the four families' local
+updates and two-way wraps, then one stabilised recompute) for every chain.
+100 steps make one sweep at Lt=1000; a sweep of 64 chains takes tens of
+seconds, so a block is the unit that keeps the run within minutes.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--workload c2_fp64|c4_mixed]
+                    [--workload c4_mixed|c2_fp64|small] [--chains C]
 
-Prints one JSON line (rank 0).  Under torchrun each rank runs its own
-independent replica chains (the path does not shard: chains are
-independent Markov processes), timing is max over ranks.
+Prints one JSON line (rank 0).  Under torchrun each rank advances its own
+independent chains (chains are independent Markov processes: replicas, no
+collective on the data path); the step time is the max over ranks.
 """
 from __future__ import annotations
 
@@ -26,19 +34,35 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FP64_PEAK_GFLOPS = 1010.8   # measured DFMA rate on this GB300 pool (profiles/fp64_peak_probe.md)
+# DFMA throughput of this GB300 pool measured with a dependent-free FP64 FMA
+# loop over all SMs (MEASURED_PEAKS.json holds no FP64 figure)
+FP64_PEAK_GFLOPS = 1010.8
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="c2_fp64", choices=["c2_fp64", "c4_mixed", "small"])
+    p.add_argument("--workload", default="c4_mixed", choices=["c4_mixed", "c2_fp64", "small"])
+    p.add_argument("--chains", type=int, default=0, help="chains per GPU of the mixed batch (default 64)")
+    p.add_argument("--delay", type=int, default=64, help="delay depth of the mixed batch")
+    p.add_argument("--plain-steps", type=int, default=3, help="timed blocks of the plain FP64 chain")
     p.add_argument("--cpu-slices", type=int, default=0, help="slices per chain in the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
     return p.parse_args()
+
+
+def peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d["bf16_tflops_sustained"], "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
 
 
 # ---------------------------------------------------------------------------
@@ -51,22 +75,26 @@ def workload_model(name: str):
         # dtau=0.1, lambda=0.8, omega=1, static SOC alpha=0.3, ngroup=10
         spec = M.epsocz_spec(14, lam=0.8, alpha=0.3, ntime=1000, ngroup=10, filling=0.5,
                              jump_distance=0.5)
-    m = M.build_model(spec, twist_seed=11, twist=1e-3)
-    return m
+    return M.build_model(spec, twist_seed=11, twist=1e-3)
 
 
-def config_of(name: str, m, n_gpus: int, chains: int) -> dict:
-    return {
+def config_of(name: str, m, n_gpus: int, chains: int, extra: dict | None = None) -> dict:
+    d = {
         "workload": {"c2_fp64": "14x14 SOC EPSOCZ, Lt=1000, plain FP64, 1 chain per GPU",
-                     "c4_mixed": "14x14 SOC EPSOCZ, Lt=1000, batched mixed precision",
-                     "small": "6x6 SOC EPSOCZ, Lt=100, plain FP64"}[name],
+                     "c4_mixed": f"14x14 SOC EPSOCZ, Lt=1000, batched mixed precision, {chains} chains per GPU",
+                     "small": f"6x6 SOC EPSOCZ, Lt=100, batched mixed precision, {chains} chains per GPU"}[name],
         "L": int(m.lat.dlength[0]), "ns": m.ns, "nelec": m.nelec, "ntime": m.ntime,
         "ngroup": m.ngroup, "dtau": m.spec.delt, "lambda": m.spec.ep_parameter, "alpha": 0.3,
         "omega": m.spec.omega, "chains_per_gpu": chains, "parallelism": f"replicas x{n_gpus}",
-        "field_init": "x ~ N(0, 0.5^2), numpy PCG64 seed 2+rank",
-        "proposal": "uniform, half-width 0.5",
-        "l2": "working set per chain 0.33 GB (expKV 0.2 GB + Q string 0.125 GB) > 129 MB L2; no flush",
+        "step": f"{m.ngroup} slices (one stabilisation block) of every chain; {m.ntime // m.ngroup} steps = 1 sweep",
+        "proposal": "uniform, half-width 0.5 (mod_update.f90:84)",
+        "measurement": "not in the timed region (equal-time measurement runs once per sweep)",
+        "l2": "no flush: G alone is 2.46 MB per chain (x2 buffers) and expKV 0.2 GB per chain, "
+              "well above the 129 MB L2",
     }
+    if extra:
+        d.update(extra)
+    return d
 
 
 # ---------------------------------------------------------------------------
@@ -104,7 +132,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        sm, smax, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
@@ -113,12 +141,14 @@ class ClockSampler:
             try:
                 sm.append(float(parts[1]))
                 smax.append(float(parts[2]))
+                pw.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, parts[4:8]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_median": float(np.median(pw)) if pw else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -153,8 +183,9 @@ def max_over_ranks(world, v: float) -> float:
 
 # ---------------------------------------------------------------------------
 def cpu_baseline(m, field, words, slices: int) -> dict:
-    """The oracle (FP64 restatement of the reference CPU path) on all host
-    cores, one independent chain per core, for a bounded sample of slices."""
+    """The oracle (line-cited FP64 restatement of the reference CPU path) on
+    all host cores, one independent chain per core, for a bounded sample of
+    slices of one backward sweep."""
     from oracle.oracle import OracleChain
     cores = os.cpu_count() or 1
     o = OracleChain(m, field=field, seed_words=words, meas=False)
@@ -163,170 +194,257 @@ def cpu_baseline(m, field, words, slices: int) -> dict:
     secs = o.time_parallel(cores, cores, 1, slices)
     sweeps = cores * slices / m.ntime
     return {"value": sweeps / secs, "unit": "sweeps/s", "cores": cores, "kind": "port",
-            "sample": f"{cores} chains x {slices} slices of one backward sweep ({slices}/{m.ntime} sweep each), "
-                      f"{secs:.1f} s wall", "per_core": sweeps / secs / cores}
+            "sample": f"{cores} chains x {slices} slices of one backward sweep ({slices}/{m.ntime} sweep each, "
+                      f"incl. {slices // m.ngroup} recomputes), {secs:.1f} s wall",
+            "per_core": sweeps / secs / cores}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    m = workload_model(args.workload if args.workload != "c4_mixed" else "c2_fp64")
     from pqmc_allinone_gb300 import model as M
     from pqmc_allinone_gb300.rng import seed_words
+    name = "small" if args.workload == "small" else "c2_fp64"
+    m = workload_model(name)
     f = M.field_gaussian(m, 2)
-    slices = args.cpu_slices or (2 if m.ntime >= 1000 else 20)
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(m, f, seed_words(42), max(1, slices // 2))
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(m, f, seed_words(42), slices))
+    slices = args.cpu_slices or (10 if m.ntime >= 1000 else 20)
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline(m, f, seed_words(42), max(1, slices // 5))
+    vals = [cpu_baseline(m, f, seed_words(42), slices) for _ in range(args.steps)]
     v = float(np.mean([x["value"] for x in vals]))
     cb = dict(vals[-1])
     cb["value"] = v
     out = {"metric": "sweeps/s @14x14 Lt=1000", "value": v, "unit": "sweeps/s", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v if v else None,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * (m.ngroup / m.ntime) / v,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-           "data": "synthetic", "config": config_of("c2_fp64", m, args.gpus, 1), "impl": "reference",
+           "data": "synthetic", "config": config_of(name, m, args.gpus, cb["cores"]), "impl": "reference",
            "cpu_baseline": cb, "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0,
                                        "d2h_bytes_per_step": 0},
-           "note": "reference Fortran cannot be built here (no Fortran compiler); this is the oracle's "
-                   "line-cited C++ FP64 restatement of the same path"}
+           "note": "the reference Fortran cannot be built here or on the GPU box (no Fortran compiler, no "
+                   "LAPACK); this arm times the oracle, the line-cited C++ FP64 restatement of the same path, "
+                   "one chain per host core"}
     print(json.dumps(out))
 
 
 # ---------------------------------------------------------------------------
-def algorithmic_update_flops(m, n_acc: int, n_prop: int) -> float:
-    """FP64 flops of update_phonon_field: per proposal the 4x4 ratio
-    (G_SS Delta, Delta, det: ~3*dim^3 CMAC), per accepted move the rank-dim
-    update Ns*dim*dim + Ns*Ns*dim CMAC (src/mod_update.f90:146-187);
-    1 CMAC = 8 flop."""
-    d = m.pdim
-    return 8.0 * (n_prop * 3.0 * d ** 3 + n_acc * (m.ns * d * d + m.ns * m.ns * d))
+class Cursor:
+    """(loop, first slice) of the next block in the sweep order."""
+
+    def __init__(self, m):
+        self.m = m
+        self.loop, self.tc = 1, 1
+
+    def next(self):
+        out = (self.loop, self.tc)
+        self.tc += self.m.ngroup
+        if self.tc > self.m.ntime:
+            self.loop += 1
+            self.tc = 1
+        return out
 
 
-def run_gpu(args, world, rank, local):
-    import ctypes
-    from pqmc_allinone_gb300 import model as M
-    from pqmc_allinone_gb300.engine import PqmcChain, kernel_launches
-    from pqmc_allinone_gb300.rng import seed_words
+def run_plain(m, steps: int, rank: int) -> dict:
+    """Plain single-chain FP64 form on this GPU (bit-identical decisions to
+    the oracle), same block definition; wall time between device syncs (every
+    C-ABI call synchronises its stream)."""
     import torch
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.engine import PqmcChain
+    from pqmc_allinone_gb300.rng import seed_words
+    ch = PqmcChain(m, field=M.field_gaussian(m, 2 + rank), rng_words=seed_words(1000 + rank))
+    ch.init_expkv()
+    ch.init_g(1)
+    cur = Cursor(m)
+    loop, tc = cur.next()
+    ch.sweep_slices(loop, tc, m.ngroup)          # warm-up block
+    torch.cuda.synchronize()
+    s0 = ch.state()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        loop, tc = cur.next()
+        ch.sweep_slices(loop, tc, m.ngroup)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    s1 = ch.state()
+    acc = s1["positive_accept"] - s0["positive_accept"]
+    prop = acc + s1["negative_accept"] - s0["negative_accept"]
+    ch.close()
+    return {"value": (m.ngroup / m.ntime) / dt, "unit": "sweeps/s", "ms_per_step": dt * 1000.0,
+            "steps": steps, "accept_ratio": acc / max(1, prop), "err_g_rel_max": s1["err_g_rel_max"]}
+
+
+def run_mixed(args, world, rank, local):
+    import torch
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.engine import PqmcBatch, kernel_launches
+    from pqmc_allinone_gb300.rng import seed_words
 
     torch.cuda.set_device(local)
     m = workload_model(args.workload)
-    field = M.field_gaussian(m, 2 + rank)
-    words = seed_words(1000 + rank)
-    ch = PqmcChain(m, field=field, rng_words=words)
-    ch.init_expkv()
-    ch.init_g(1)
-    loop = 1
+    C = args.chains or (64 if args.workload == "c4_mixed" else 8)
+    seeds = [3000 + i + 1000 * rank for i in range(C)]
+    fields = [M.field_gaussian(m, s) for s in seeds]
+    b = PqmcBatch([m] * C, fields, [seed_words(s) for s in seeds], precision=1)
+    b.set_delay(args.delay)
+    t0 = time.perf_counter()
+    b.init()
+    t_init = time.perf_counter() - t0
+    cur = Cursor(m)
     for _ in range(args.warmup):
-        ch.sweep(loop, 1)
-        loop += 1
+        b.sweep_slices(*cur.next(), m.ngroup)
     torch.cuda.synchronize()
-    s0 = ch.state()
+    st0 = [c.state() for c in b.chains]
+    n0 = kernel_launches()
+    stream = torch.cuda.ExternalStream(b.stream())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    b.set_timing(True)
+    clk = ClockSampler(local)
+    barrier(world)
+    clk.start()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.sweep_slices(*cur.next(), m.ngroup)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier(world)
+    launches = kernel_launches() - n0
+    phases = b.timing()
+    b.set_timing(False)
+    t_step = max_over_ranks(world, ev0.elapsed_time(ev1) / 1000.0 / args.steps)
+    per_gpu = C * (m.ngroup / m.ntime) / t_step
+    value = world * per_gpu
+    st1 = [c.state() for c in b.chains]
+    acc = sum(s1["positive_accept"] - s0["positive_accept"] for s0, s1 in zip(st0, st1))
+    rej = sum(s1["negative_accept"] - s0["negative_accept"] for s0, s1 in zip(st0, st1))
+    drift = max(s["err_g_rel_max"] for s in st1)
+
+    # dominant contraction: the rank-K flush G += A B on the tensor cores.
+    # Algorithmic flops counted once (complex GEMM, 8 flop per CMAC): every
+    # accepted move adds dim panel columns, each flushed column costs Ns^2 CMAC.
+    pk = peaks()
+    dim = 4
+    flush_ms, flush_n = phases["flush"]
+    flops = 8.0 * m.ns * m.ns * dim * acc
+    per_launch = flops / max(1, flush_n)
+    achieved = per_launch / (flush_ms / max(1, flush_n) * 1e-3) / 1e12 if flush_ms > 0 else 0.0
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tj = json.load(f).get("k_bflush")
+            if tj and tj.get("ns") == m.ns:
+                # bytes per launch scale with the chains in the launch
+                traffic = tj["bytes_per_launch"] * C / tj["chains"]
+    except Exception:
+        pass
+    roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
+            "frac": achieved / pk["bf16_tflops_sustained"], "traffic": traffic,
+            "kernel": "k_bflush (rank-K flush G += A B, split-BF16 mma, FP32 accumulate)",
+            "algorithmic": "8*Ns^2*dim flop per accepted move (complex GEMM counted once, not the 6 split "
+                           "products)", "peak_source": f"{pk['source']} bf16 sustained (timed inside a long step)"}
+    total_ms = sum(v[0] for v in phases.values())
+    phase_out = {k: {"ms_per_step": v[0] / args.steps, "share": v[0] / total_ms if total_ms else None,
+                     "launch_groups": v[1]} for k, v in phases.items()}
+
+    # end to end through the C-ABI with host buffers: every chain's field block
+    # for the step goes host->device (the host copy, kept in step), the block
+    # runs, the updated block and each chain's state come back
+    e2e = run_e2e_mixed(b, m, cur, min(args.steps, 5))
+
+    plain = None if args.no_plain else run_plain(m, args.plain_steps, rank)
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from pqmc_allinone_gb300 import model as M2
+        from pqmc_allinone_gb300.rng import seed_words as sw
+        cb = cpu_baseline(m, M2.field_gaussian(m, 2), sw(42), args.cpu_slices or 10)
+    b.close()
+    if rank != 0:
+        return
+    out = {"metric": "sweeps/s @14x14 Lt=1000: batched mixed-prec vs plain FP64 on GB300",
+           "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp32/bf16 fast path on an FP64 G",
+           "data": "synthetic (x ~ N(0,0.5^2), seeds 3000+i)",
+           "config": config_of(args.workload, m, world, C, {"delay_depth": args.delay}),
+           "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "clocks": clocks,
+           "cpu_baseline": cb, "plain_fp64": plain,
+           "speedup_vs_plain_fp64": (per_gpu / plain["value"]) if plain else None,
+           "g_error": {"fast_path_drift_rel_max": drift,
+                       "definition": "max over chains and recomputes in the timed region of "
+                                     "||G_fast - G_recomputed||_F / ||G_recomputed||_F (drift of the FP32 "
+                                     "fast path over one ngroup block; the recompute is FP64-class)"},
+           "accept_ratio": acc / max(1, acc + rej), "phases": phase_out, "init_s": t_init}
+    print(json.dumps(out))
+
+
+def run_e2e_mixed(b, m, cur, steps: int) -> dict:
+    import torch
+    C = len(b.chains)
+    nb, blk = m.n_bf, m.ngroup
+    host = torch.empty((C, m.ntime, nb), dtype=torch.float64, pin_memory=True)   # (n_bf, ntime) per chain
+    hv = host.numpy()
+    for i, c in enumerate(b.chains):
+        hv[i] = c.field().T
+    state_bytes = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        loop, tc = cur.next()
+        first_time = tc if loop % 2 == 0 else m.ntime - (tc + blk - 1) + 1
+        for i, c in enumerate(b.chains):
+            c.set_field_slices(first_time, hv[i, first_time - 1:first_time - 1 + blk].T)
+        b.sweep_slices(loop, tc, blk)
+        for i, c in enumerate(b.chains):
+            c.get_field_slices(first_time, blk, out=hv[i, first_time - 1:first_time - 1 + blk].T)
+        states = [c.state() for c in b.chains]
+        state_bytes = len(states) * 104
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    blk_bytes = C * nb * blk * 8
+    return {"value": C * (blk / m.ntime) / dt, "unit": "chain-sweeps/s", "h2d_bytes_per_step": int(blk_bytes),
+            "d2h_bytes_per_step": int(blk_bytes + state_bytes), "steps": steps,
+            "path": "pqmc_set_field_slices (pinned host) + pqmc_batch_sweep_slices + pqmc_get_field_slices + "
+                    "pqmc_get_state per chain"}
+
+
+def run_plain_headline(args, world, rank, local):
+    """--workload c2_fp64: the plain FP64 single chain as the headline."""
+    import torch
+    from pqmc_allinone_gb300.engine import kernel_launches
+    torch.cuda.set_device(local)
+    m = workload_model("c2_fp64")
     n0 = kernel_launches()
     clk = ClockSampler(local)
     barrier(world)
     clk.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    ev0.record()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        ch.sweep(loop, 1)
-        loop += 1
-    torch.cuda.synchronize()
-    ev1.record()
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    p = run_plain(m, args.steps, rank)
     clocks = clk.stop()
-    barrier(world)
     launches = kernel_launches() - n0
-    s1 = ch.state()
-    # the library runs on its own stream; host wall time bracketed by device
-    # synchronisation is the step time (the torch events only bracket it)
-    t_step = max_over_ranks(world, wall) / args.steps
-    value = world * 1.0 / t_step
-    n_acc = s1["positive_accept"] - s0["positive_accept"]
-    n_rej = s1["negative_accept"] - s0["negative_accept"]
-
-    # dominant kernel: update_phonon_field, timed alone per family launch
-    upd = time_update_kernel(ch, m)
-    flops_per_launch = algorithmic_update_flops(m, upd["acc"], upd["prop"]) / upd["launches"]
-    achieved = flops_per_launch / (upd["ms_per_launch"] * 1e-3) / 1e9
-
-    # end to end through the C-ABI with host buffers: set_field (H2D) +
-    # sweep with the measurement record + read back field and record (D2H)
-    e2e = run_e2e(ch, m, field, loop + 10, args.steps)
-
-    cb = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(m, field, words, args.cpu_slices or (2 if m.ntime >= 1000 else 20))
+    t_step = max_over_ranks(world, p["ms_per_step"] / 1000.0)
     if rank != 0:
         return
-    out = {"metric": "sweeps/s @14x14 Lt=1000", "value": value, "unit": "sweeps/s", "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1000.0,
+    out = {"metric": "sweeps/s @14x14 Lt=1000 (plain FP64)", "value": world * (m.ngroup / m.ntime) / t_step,
+           "unit": "sweeps/s", "n_gpus": world, "steps": args.steps, "warmup": 1, "ms_per_step": t_step * 1000,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-           "data": "synthetic", "config": config_of(args.workload, m, world, 1),
-           "e2e": e2e, "gpu_launches": int(launches),
-           "roofline": {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
-                        "frac": achieved / FP64_PEAK_GFLOPS, "traffic": None,
-                        "kernel": "k_update (update_phonon_field, one family)",
-                        "peak_source": "measured DFMA throughput of this GB300 (not in MEASURED_PEAKS.json)"},
-           "clocks": clocks, "cpu_baseline": cb,
-           "accept_ratio": n_acc / max(1, n_acc + n_rej),
-           "event_ms_per_step": ev0.elapsed_time(ev1) / args.steps}
+           "data": "synthetic", "config": config_of("c2_fp64", m, world, 1), "clocks": clocks,
+           "gpu_launches": int(launches), "plain_fp64": p, "roofline": None, "cpu_baseline": None,
+           "e2e": None}
     print(json.dumps(out))
-
-
-def time_update_kernel(ch, m) -> dict:
-    """CUDA-event timing of update_phonon_field launches on the library's
-    stream (per-family calls through the C-ABI)."""
-    import torch
-    lib = ch.lib
-    st0 = ch.state()
-    t = m.ntime // 2
-    reps = 0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for pf in range(1, len(m.pf) + 1):
-        for tt in range(t, t + 5):
-            ch.update_phonon_field(pf, tt)
-            reps += 1
-    torch.cuda.synchronize()
-    el = time.perf_counter() - t0
-    st1 = ch.state()
-    acc = st1["positive_accept"] - st0["positive_accept"]
-    rej = st1["negative_accept"] - st0["negative_accept"]
-    return {"launches": reps, "ms_per_launch": el * 1000.0 / reps, "acc": acc, "prop": acc + rej}
-
-
-def run_e2e(ch, m, field, loop, steps) -> dict:
-    import torch
-    from pqmc_allinone_gb300.model import record_width
-    hf = np.asfortranarray(field)
-    w = record_width(m)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(steps):
-        ch.set_field(hf)
-        rec = ch.sweep(loop + 2 * k, 1, warmup=0, meas_number=0, cap=1)
-        hf = ch.field()
-        _ = rec.sum()
-    torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / steps
-    return {"value": 1.0 / dt, "unit": "sweeps/s", "h2d_bytes_per_step": int(hf.nbytes),
-            "d2h_bytes_per_step": int(hf.nbytes + 16 * w)}
 
 
 def main():
     args = parse()
-    world, rank, local = dist_setup() if args.impl == "gb300" else (
-        int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0)
     if args.impl == "reference":
+        world, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
         run_reference(args, world, rank)
         return
-    run_gpu(args, world, rank, local)
+    world, rank, local = dist_setup()
+    if args.workload == "c2_fp64":
+        run_plain_headline(args, world, rank, local)
+    else:
+        run_mixed(args, world, rank, local)
 
 
 if __name__ == "__main__":

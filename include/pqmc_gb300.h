@@ -164,6 +164,10 @@ typedef struct pqmc_state {
   int64_t negative_accept;  /* local moves rejected                          */
   int32_t rng[5];           /* iran0,jran0,kran0,mran0,nran0 of ran2_s       */
   int32_t reserved;
+  double err_g;             /* max |G_fast - G_scratch| at the last recompute */
+  double err_g_rel_max;     /* largest ||G_fast - G_scratch||_F/||G_scratch||_F
+                               over all recomputes so far (no reference
+                               counterpart: the drift of the fast path)     */
 } pqmc_state;
 
 typedef struct pqmc_chain pqmc_chain; /* opaque, one Markov chain on the GPU */
@@ -182,6 +186,13 @@ int pqmc_set_meas_layout(pqmc_chain* chain, const pqmc_meas_layout* layout);
  * init_boson_field (Main_PQMC.f90:355-369) with exact doubles. */
 int pqmc_set_field(pqmc_chain* chain, const double* boson_field);
 int pqmc_get_field(pqmc_chain* chain, double* boson_field);
+/* boson_field(:, first_time .. first_time+n_times-1) from / to host memory
+ * (columns of the column-major array are contiguous).  Setting a block
+ * recomputes expKV/expKV_inv of those slices (set_pf_expKV_mat); it leaves
+ * G alone, so the values must be those G was built with (a host copy kept
+ * in step with the device) or a recompute must follow. */
+int pqmc_set_field_slices(pqmc_chain* chain, int first_time, int n_times, const double* boson_field_block);
+int pqmc_get_field_slices(pqmc_chain* chain, int first_time, int n_times, double* boson_field_block);
 /* slater_Q(Ns,nelec), slater_D(nelec) complex, from set_nelec_occupied
  * (Main_PQMC.f90:279-305). */
 int pqmc_set_slater(pqmc_chain* chain, const double* slater_q,
@@ -238,6 +249,10 @@ int pqmc_begin_measure(pqmc_chain* chain, int forward, int time,
 int pqmc_sweep(pqmc_chain* chain, int first_loop, int n_sweeps, int warmup,
                int meas_interval, int meas_number, double* records,
                int n_records_cap, int* n_records);
+/* Slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of that loop
+ * body (no measurement); n_slices = ntime from first_tc = 1 is one whole
+ * sweep.  Lets a driver advance a sweep in stabilisation blocks. */
+int pqmc_sweep_slices(pqmc_chain* chain, int loop, int first_tc, int n_slices);
 
 /* ---- differentiable log-weight ---------------------------------------- */
 /* boson_field from a DEVICE pointer (n_bf, ntime), e.g. a torch tensor. */
@@ -270,6 +285,24 @@ int pqmc_batch_chain(pqmc_batch* batch, int i, pqmc_chain** chain);
 int pqmc_batch_set_delay(pqmc_batch* batch, int depth);
 /* one sweep of every chain (Main_PQMC.f90:99-154), no measurement */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
+/* slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain */
+int pqmc_batch_sweep_slices(pqmc_batch* batch, int loop, int first_tc, int n_slices);
+/* init_expKV and init_g_T0(1) (mod_evolution.f90:46-111) of every chain
+ * (the fields set per chain first).  Mixed batches build the Q/D strings of
+ * all chains together (double-float propagation + CholeskyQR2). */
+int pqmc_batch_init(pqmc_batch* batch);
+/* the CUDA stream every batched kernel runs on (cudaStream_t) */
+int pqmc_batch_stream(pqmc_batch* batch, void** stream);
+/* CUDA-event timers per phase of the mixed family step; set_timing clears
+ * the totals, get_timing returns PQMC_N_PHASES totals (ms) and counts. */
+#define PQMC_PHASE_PREP      0   /* ran2 draws + proposal data           */
+#define PQMC_PHASE_SCAN      1   /* sequential ratios, delayed panels     */
+#define PQMC_PHASE_FLUSH     2   /* tensor-core rank-K flush G += A B     */
+#define PQMC_PHASE_WRAP      3   /* two-way wrap by a family             */
+#define PQMC_PHASE_RECOMPUTE 4   /* stabilised recompute (get_g_scratch)  */
+#define PQMC_N_PHASES        5
+int pqmc_batch_set_timing(pqmc_batch* batch, int enable);
+int pqmc_batch_get_timing(pqmc_batch* batch, double* ms, long long* launches);
 
 /* ---- recompute without device allocation ---------------------------- */
 /* No counterpart in the reference.  g_out = R (X^H R)^-1 X^H and

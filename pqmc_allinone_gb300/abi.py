@@ -57,13 +57,14 @@ class PqmcState(ctypes.Structure):
         ("ln_cw", ctypes.c_double * 2), ("err_fast_max", ctypes.c_double),
         ("err_fast", ctypes.c_double), ("positive_accept", ctypes.c_int64),
         ("negative_accept", ctypes.c_int64), ("rng", ctypes.c_int32 * 5),
-        ("reserved", ctypes.c_int32),
+        ("reserved", ctypes.c_int32), ("err_g", ctypes.c_double), ("err_g_rel_max", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:
         return dict(ln_cw=complex(self.ln_cw[0], self.ln_cw[1]), err_fast_max=self.err_fast_max,
                     err_fast=self.err_fast, positive_accept=self.positive_accept,
-                    negative_accept=self.negative_accept, rng=list(self.rng))
+                    negative_accept=self.negative_accept, rng=list(self.rng), err_g=self.err_g,
+                    err_g_rel_max=self.err_g_rel_max)
 
 
 def _ptr(a: np.ndarray, ty):
@@ -178,6 +179,14 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_chain": ([vp, ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
         "pqmc_batch_sweep": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_set_delay": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "pqmc_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "pqmc_set_field_slices": ([vp, ctypes.c_int, ctypes.c_int, _f64p], ctypes.c_int),
+        "pqmc_get_field_slices": ([vp, ctypes.c_int, ctypes.c_int, _f64p], ctypes.c_int),
+        "pqmc_batch_init": ([vp], ctypes.c_int),
+        "pqmc_batch_stream": ([vp, ctypes.POINTER(vp)], ctypes.c_int),
+        "pqmc_batch_set_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_get_timing": ([vp, _f64p, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "pqmc_version": ([], ctypes.c_char_p),
         "pqmc_last_error": ([], ctypes.c_char_p),
         "pqmc_kernel_launches": ([], ctypes.c_int64),

@@ -24,6 +24,7 @@
 #include "rng.cuh"
 #include "update_dev.cuh"
 #include "recompute_b.cuh"
+#include "df32.cuh"
 
 namespace pqmc {
 
@@ -34,10 +35,11 @@ struct BDesc {
   cplx* expkv_inv;
   cplx* g;       // parity 0 buffer
   cplx* g_alt;   // parity 1 buffer
-  float2* A;     // (kmax, ns): A[q*ns + r]
-  float2* B;     // (kmax, ns): B[q*ns + c]
+  float2* A;     // (kmax, ldp): A[q*ldp + r]
+  float2* B;     // (kmax, ldp): B[q*ldp + c]
   int kmax;
-  int pad;
+  int ldp;       // panel leading dimension: Ns rounded up to even (16-byte columns)
+  int* err;      // batch-wide error word (PQMC_ERR_* of a device-side failure)
   PlaqPre* pre;
   DevScalars* sc;
   int* kcount;
@@ -161,6 +163,15 @@ __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf, int t) {
 // (the delay depth); k_bflush then folds them into G and the next round
 // continues.  Ratios, R^-1 and T are FP32 (the panels are FP32); the weight
 // ln_cw is accumulated in FP64.
+//
+// Latency design: at the start of a round (panels empty) the kernel stages
+// the family's site table, the FP32 Delta and thresholds, and
+// Geff(S_p,S_p) = G(S_p,S_p) for every plaquette still to come in shared
+// memory.  Every warp evaluates each ratio redundantly from shared memory,
+// so a rejected proposal costs no block barrier and no global access.  An
+// accepted move builds its rank-dim panel block (one pass over the panels)
+// and adds its contribution to the cached Geff blocks of the later
+// plaquettes.
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_KSTAGE = 512;   // max delay depth (panel columns)
 
@@ -169,8 +180,8 @@ __device__ __forceinline__ float2 fdiv1(float2 a) {   // 1/a
   return make_float2(a.x / n, -a.y / n);
 }
 
-// 4x4 (or smaller) complex inverse in FP32 by Gauss-Jordan with partial
-// pivoting on one thread
+// small complex inverse in FP32 by Gauss-Jordan with partial pivoting on one
+// thread (sizes below 4)
 __device__ void finv_small(int n, float2* a) {
   float2 inv[16];
   for (int j = 0; j < n; ++j)
@@ -204,7 +215,6 @@ __device__ void finv_small(int n, float2* a) {
 __device__ float2 fdet_small(int n, const float2* a) {
   if (n == 1) return a[0];
   if (n == 2) return fsb(fm(a[0], a[3]), fm(a[2], a[1]));
-  // Gauss elimination with partial pivoting on a copy
   float2 b[16];
   for (int k = 0; k < n * n; ++k) b[k] = a[k];
   float2 det = make_float2(1.f, 0.f);
@@ -229,152 +239,377 @@ __device__ float2 fdet_small(int n, const float2* a) {
   return det;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int t, int parity, int kd, int* next_p) {
+// determinant of the dim x dim FP32 matrix R (shared, column-major) returned
+// to every lane: Laplace expansion along rows 0,1 over six lanes for dim 4,
+// lane 0 otherwise
+__device__ __forceinline__ float2 wf_det(int dim, const float2* R, int lane) {
+  float2 v = make_float2(0.f, 0.f);
+  if (dim == 4) {
+    if (lane < 6) {
+      const int J[6] = {0, 0, 0, 1, 1, 2}, K[6] = {1, 2, 3, 2, 3, 3};
+      const int L[6] = {2, 1, 1, 0, 0, 0}, Mm[6] = {3, 3, 2, 3, 2, 1};
+      const float sg[6] = {1.f, -1.f, 1.f, 1.f, -1.f, 1.f};
+      int j = J[lane], k = K[lane], l = L[lane], m = Mm[lane];
+      float2 mi = fsb(fm(R[0 + 4 * j], R[1 + 4 * k]), fm(R[0 + 4 * k], R[1 + 4 * j]));
+      float2 co = fsb(fm(R[2 + 4 * l], R[3 + 4 * m]), fm(R[2 + 4 * m], R[3 + 4 * l]));
+      float2 t = fm(mi, co);
+      v = make_float2(sg[lane] * t.x, sg[lane] * t.y);
+    }
+    for (int o = 4; o > 0; o >>= 1) {
+      float vx = __shfl_down_sync(0xffffffffu, v.x, o), vy = __shfl_down_sync(0xffffffffu, v.y, o);
+      if (lane + o < 8) { v.x += vx; v.y += vy; }
+    }
+  } else if (lane == 0) {
+    v = fdet_small(dim, R);
+  }
+  return make_float2(__shfl_sync(0xffffffffu, v.x, 0), __shfl_sync(0xffffffffu, v.y, 0));
+}
+
+// R <- R^-1 in place (shared, column-major): adjugate over 16 lanes for dim 4,
+// lane-0 Gauss-Jordan otherwise
+__device__ __forceinline__ void wf_inverse(int dim, float2* R, float2 det, int lane) {
+  if (dim == 4) {
+    float2 cof = make_float2(0.f, 0.f);
+    const int i = lane & 3, j = lane >> 2;
+    if (lane < 16) {
+      int r[3], c[3], n = 0;
+      for (int k = 0; k < 4; ++k)
+        if (k != i) r[n++] = k;
+      n = 0;
+      for (int k = 0; k < 4; ++k)
+        if (k != j) c[n++] = k;
+#define S(a, b) R[r[a] + 4 * c[b]]
+      cof = fa(fsb(fm(S(0, 0), fsb(fm(S(1, 1), S(2, 2)), fm(S(1, 2), S(2, 1)))),
+                   fm(S(0, 1), fsb(fm(S(1, 0), S(2, 2)), fm(S(1, 2), S(2, 0))))),
+               fm(S(0, 2), fsb(fm(S(1, 0), S(2, 1)), fm(S(1, 1), S(2, 0)))));
+#undef S
+      if ((i + j) & 1) cof = make_float2(-cof.x, -cof.y);
+      cof = fm(cof, fdiv1(det));
+    }
+    __syncwarp();
+    if (lane < 16) R[j + 4 * i] = cof;
+    __syncwarp();
+    return;
+  }
+  if (lane == 0) finv_small(dim, R);
+  __syncwarp();
+}
+
+// ---- 1-D bulk copies (TMA) global -> shared with mbarrier completion ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return ok;
+}
+// wait for the phase of parity `parity` to complete; false after ~2 s
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity))
+    if (clock64() - t0 > (4LL << 30)) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(b))
+               : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+constexpr int SCAN_NSTAGE = 3;   // panel chunks in flight
+constexpr int SCAN_RPT = 4;      // rows per thread: Ns <= SCAN_RPT * SCAN_THREADS
+
+__host__ __device__ __forceinline__ size_t al16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// dynamic shared memory of k_bscan (byte offsets, 16-byte aligned pieces)
+struct ScanLayout {
+  size_t stage, delta, geff, newA, newB, thr, site, accp, accd, total;
+};
+__host__ __device__ __forceinline__ ScanLayout scan_layout(int npla, int ns, int ldp, int qc, int kd) {
+  ScanLayout L;
+  size_t o = 0;
+  L.stage = o; o += al16(sizeof(float2) * (size_t)SCAN_NSTAGE * 2 * qc * ldp);
+  L.delta = o; o += al16(sizeof(float2) * 16 * (size_t)npla);
+  L.geff = o;  o += al16(sizeof(float2) * 16 * (size_t)npla);
+  L.newA = o;  o += al16(sizeof(float2) * 4 * (size_t)ns);
+  L.newB = o;  o += al16(sizeof(float2) * 4 * (size_t)ns);
+  L.thr = o;   o += al16(sizeof(double) * (size_t)npla);
+  L.site = o;  o += al16(sizeof(int) * 4 * (size_t)npla);
+  L.accp = o;  o += al16(sizeof(int) * (size_t)kd);
+  L.accd = o;  o += al16(sizeof(float2) * (size_t)kd);
+  L.total = o;
+  return L;
+}
+
+// thread 0: stream panel columns [c*qc, c*qc+nq) of A and B into stage c % NSTAGE
+__device__ __forceinline__ void scan_issue(float2* s_stage, uint64_t* s_full, const float2* A, const float2* B,
+                                           int ldp, int qc, int K, int c) {
+  const int st = c % SCAN_NSTAGE, q0 = c * qc, nq = min(qc, K - q0);
+  const uint32_t bytes = (uint32_t)(sizeof(float2) * (size_t)nq * ldp);
+  float2* dA = s_stage + (size_t)st * 2 * qc * ldp;
+  float2* dB = dA + (size_t)qc * ldp;
+  mbar_arrive_tx(&s_full[st], 2 * bytes);
+  bulk_g2s(dA, A + (size_t)q0 * ldp, bytes, &s_full[st]);
+  bulk_g2s(dB, B + (size_t)q0 * ldp, bytes, &s_full[st]);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int t, int parity, int kd, int qc,
+                                                         int* next_p) {
   __shared__ BDesc sd;
-  if (threadIdx.x == 0) sd = D[blockIdx.x];
+  __shared__ float2 s_R[SCAN_THREADS / 32][16];
+  __shared__ float2 s_T[SCAN_THREADS / 32][16];
+  __shared__ __align__(8) uint64_t s_full[SCAN_NSTAGE];
+  __shared__ int s_abort;
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  if (threadIdx.x == 0) {
+    sd = D[blockIdx.x];
+    s_abort = 0;
+    for (int k = 0; k < SCAN_NSTAGE; ++k) mbar_init(&s_full[k], 1);
+    fence_mbar_init();
+  }
   __syncthreads();
   const BDesc& d = sd;
   const DevModel& M = d.M;
-  const int ns = M.ns, npla = M.pf_npla[pf], dim = M.pf_dim[pf], pd = M.pdim;
+  constexpr int dim = DIM, dd = DIM * DIM;
+  const int ns = M.ns, npla = M.pf_npla[pf], pd = M.pdim, ldp = d.ldp;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int p0 = next_p[blockIdx.x];
+  const int p0 = next_p[blockIdx.x];
   if (p0 >= npla) {
     if (tid == 0) *d.kcount = 0;
     return;
   }
-  const cplx* G = parity ? d.g_alt : d.g;
+  const ScanLayout L = scan_layout(npla, ns, ldp, qc, kd);
+  float2* s_stage = reinterpret_cast<float2*>(s_dyn + L.stage);
+  float2* s_delta = reinterpret_cast<float2*>(s_dyn + L.delta);   // [npla][16]
+  float2* s_geff = reinterpret_cast<float2*>(s_dyn + L.geff);     // [npla][16]
+  float2* s_newA = reinterpret_cast<float2*>(s_dyn + L.newA);     // [4][ns]
+  float2* s_newB = reinterpret_cast<float2*>(s_dyn + L.newB);     // [4][ns]
+  double* s_thr = reinterpret_cast<double*>(s_dyn + L.thr);
+  int* s_site = reinterpret_cast<int*>(s_dyn + L.site);           // [npla][4]
+  int* s_accp = reinterpret_cast<int*>(s_dyn + L.accp);
+  float2* s_accd = reinterpret_cast<float2*>(s_dyn + L.accd);
+  const float4* G = reinterpret_cast<const float4*>(parity ? d.g_alt : d.g);   // double-float G
   float2* A = d.A;
   float2* B = d.B;
-  PlaqPre* pre = d.pre;
-  __shared__ int s_S[4];
-  __shared__ float2 s_g[16], s_r[16], s_T[16];
-  __shared__ int s_dec;
-  __shared__ float2 s_BS[4 * SCAN_KSTAGE];   // B(q, S_m)
-  __shared__ float2 s_AS[4 * SCAN_KSTAGE];   // A(S_l, q)
-  int K = 0;
-  double lprod = 1.0;
-  long long lexp = 0, pa = 0, na = 0;
+  const PlaqPre* pre = d.pre;
+  // ---- stage the rest of the family (panels are empty: Geff = G) ----------
+  for (int e = tid; e < (npla - p0) * 4; e += blockDim.x) {
+    const int p = p0 + e / 4, m = e % 4;
+    s_site[4 * p + m] = m < dim ? M.site[m + pd * (p + M.max_pla * pf)] : 0;
+  }
+  for (int p = p0 + tid; p < npla; p += blockDim.x) s_thr[p] = pre[p].thr;
+  for (int e = tid; e < (npla - p0) * 16; e += blockDim.x) {
+    const int p = p0 + e / 16, k = e % 16;
+    if (k < dd) s_delta[16 * p + k] = pre[p].deltaf[k];
+  }
+  __syncthreads();
+  for (int e = tid; e < (npla - p0) * 16; e += blockDim.x) {
+    const int p = p0 + e / 16, k = e % 16;
+    if (k < dd) s_geff[16 * p + k] = dg_f2(G[s_site[4 * p + k % dim] + (size_t)ns * s_site[4 * p + k / dim]]);
+  }
+  __syncthreads();
+  int K = 0, n_acc = 0;
+  long long na = 0;
+  uint32_t phase = 0;   // bit s: parity of the next completion of stage s
+  bool aborted = false;
   int p = p0;
+  const int i = lane % dim, j = lane / dim;
+  const bool act = lane < dd;
   for (; p < npla; ++p) {
     if (K + dim > kd) break;
-    if (tid < dim) s_S[tid] = M.site[tid + pd * (p + M.max_pla * pf)];
-    __syncthreads();
-    // stage A(S,:), B(:,S) for q < K (one round trip), and G(S,S)
-    for (int e = tid; e < K * dim; e += blockDim.x) {
-      int q = e / dim, m = e % dim;
-      s_BS[e] = B[(size_t)q * ns + s_S[m]];
-      s_AS[e] = A[(size_t)q * ns + s_S[m]];
+    // ---- ratio, evaluated by every warp from shared memory ----------------
+    const float2* ge = s_geff + 16 * p;
+    const float2* de = s_delta + 16 * p;
+    if (act) {
+      float2 a = make_float2(i == j ? 1.f : 0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < dim; ++k) a = fa(a, fm(ge[i + dim * k], de[k + dim * j]));
+      s_R[warp][lane] = a;
     }
-    if (tid < dim * dim) s_g[tid] = f2(G[s_S[tid % dim] + (size_t)ns * s_S[tid / dim]]);
-    __syncthreads();
-    const PlaqPre* pp = pre + p;
-    if (warp == 0) {
-      const int i = lane % dim, j = lane / dim;
-      const bool act = lane < dim * dim;
-      // G_eff(S,S) = G(S,S) + (A B)(S,S)
-      float2 gv = make_float2(0.f, 0.f);
-      if (act) {
-        gv = s_g[lane];
-        for (int q = 0; q < K; ++q) gv = fa(gv, fm(s_AS[q * dim + i], s_BS[q * dim + j]));
-      }
-      __syncwarp();
-      if (act) s_g[lane] = gv;
-      __syncwarp();
-      // R = I + G_eff(S,S) Delta
-      if (act) {
-        float2 a = make_float2(i == j ? 1.f : 0.f, 0.f);
-        for (int k = 0; k < dim; ++k) a = fa(a, fm(s_g[i + dim * k], pp->deltaf[k + dim * j]));
-        s_r[lane] = a;
-      }
-      __syncwarp();
-      int acc = 0;
-      if (lane == 0) {
-        float2 det = fdet_small(dim, s_r);
-        double d2 = (double)det.x * det.x + (double)det.y * det.y;
-        acc = d2 >= pp->thr;
-        if (acc) {
-          pa++;
-          double relr;
-          {
-            double dr = det.x, di = det.y;
-            double rr = dr, ri = di;
-            if (M.tr_weight) { rr = dr * dr + di * di; ri = 0.0; }
-            double ar = 1.0, ai = 0.0;
-            for (int k = 0; k < M.ncopy; ++k) {
-              double tr = ar * rr - ai * ri;
-              ai = ar * ri + ai * rr;
-              ar = tr;
-            }
-            relr = ar;
-          }
-          int ex;
-          lprod *= frexp(relr, &ex);
-          lexp += ex;
-          lprod = frexp(lprod, &ex);
-          lexp += ex;
-          d.field[M.bf[p + M.max_pla * pf] + (size_t)M.n_bf * t] = pp->xnew;
-          finv_small(dim, s_r);   // R^-1
-        } else {
-          na++;
-        }
-      }
-      acc = __shfl_sync(0xffffffffu, acc, 0);
-      __syncwarp();
-      if (acc) {
-        if (act) {
-          float2 a = make_float2(0.f, 0.f);
-          for (int k = 0; k < dim; ++k) a = fa(a, fm(pp->deltaf[i + dim * k], s_r[k + dim * j]));
-          s_T[lane] = a;
-        }
-        const size_t base2 = M.kv_base(p, pf, t);
-        if (lane < pd * pd) {
-          int ii = lane % pd, jj = lane / pd;
-          bool in = ii < dim && jj < dim;
-          d.expkv[base2 + lane] = in ? pp->enew[ii + dim * jj] : mk(0.0);
-          d.expkv_inv[base2 + lane] = in ? pp->einv[ii + dim * jj] : mk(0.0);
-        }
-      }
-      if (lane == 0) s_dec = acc;
+    __syncwarp();
+    const float2 det = wf_det(dim, s_R[warp], lane);
+    const float dm = det.x * det.x + det.y * det.y;
+    if (!((double)dm >= s_thr[p])) {
+      if (tid == 0) na++;
+      continue;
     }
-    __syncthreads();
-    if (!s_dec) continue;
-    // new panel block: a(r,l) = sum_m Geff(r,S_m) T(m,l),  b(l,c) = delta(S_l,c) - Geff(S_l,c)
-    for (int r = tid; r < ns; r += blockDim.x) {
-      float2 gm[4], bl[4];
+    // ---- accepted: T = Delta R^-1 on every warp, record the move ---------
+    wf_inverse(dim, s_R[warp], det, lane);
+    if (act) {
+      float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < dim; ++k) a = fa(a, fm(de[i + dim * k], s_R[warp][k + dim * j]));
+      s_T[warp][lane] = a;
+    }
+    __syncwarp();
+    if (tid == 0) {
+      s_accp[n_acc] = p;
+      s_accd[n_acc] = det;
+    }
+    ++n_acc;
+    const int* S = s_site + 4 * p;
+    // ---- panel block: a(r,l) = sum_m Geff(r,S_m) T(m,l), b(l,r) = delta(S_l,r) - Geff(S_l,r),
+    //      Geff = G + A B with the panel streamed through shared memory in chunks of qc columns
+    const int nch = (K + qc - 1) / qc;
+    if (tid == 0 && nch > 0) {
+      fence_proxy_async_global();   // this round's panel columns were written by generic stores
+      for (int c = 0; c < nch && c < SCAN_NSTAGE; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
+    }
+    float2 gm[SCAN_RPT][dim], bl[SCAN_RPT][dim];
+#pragma unroll
+    for (int k = 0; k < SCAN_RPT; ++k) {
+      const int r = tid + k * SCAN_THREADS;
+#pragma unroll
       for (int m = 0; m < dim; ++m) {
-        gm[m] = f2(G[r + (size_t)ns * s_S[m]]);
-        bl[m] = f2(G[s_S[m] + (size_t)ns * r]);
+        gm[k][m] = r < ns ? dg_f2(G[r + (size_t)ns * S[m]]) : make_float2(0.f, 0.f);
+        bl[k][m] = r < ns ? dg_f2(G[S[m] + (size_t)ns * r]) : make_float2(0.f, 0.f);
       }
-#pragma unroll 4
-      for (int q = 0; q < K; ++q) {
-        float2 ar = A[(size_t)q * ns + r];
-        float2 bc = B[(size_t)q * ns + r];
+    }
+    for (int c = 0; c < nch; ++c) {
+      const int st = c % SCAN_NSTAGE;
+      if (!mbar_wait_bounded(&s_full[st], (phase >> st) & 1u)) s_abort = 1;
+      phase ^= 1u << st;
+      const float2* cA = s_stage + (size_t)st * 2 * qc * ldp;
+      const float2* cB = cA + (size_t)qc * ldp;
+      const int nq = min(qc, K - c * qc);
+      for (int qq = 0; qq < nq; ++qq) {
+        float2 bs[dim], as[dim];
+#pragma unroll
         for (int m = 0; m < dim; ++m) {
-          gm[m] = fa(gm[m], fm(ar, s_BS[q * dim + m]));
-          bl[m] = fa(bl[m], fm(s_AS[q * dim + m], bc));
+          bs[m] = cB[(size_t)qq * ldp + S[m]];
+          as[m] = cA[(size_t)qq * ldp + S[m]];
+        }
+#pragma unroll
+        for (int k = 0; k < SCAN_RPT; ++k) {
+          const int r = tid + k * SCAN_THREADS;
+          if (r < ns) {
+            const float2 ar = cA[(size_t)qq * ldp + r], bc = cB[(size_t)qq * ldp + r];
+#pragma unroll
+            for (int m = 0; m < dim; ++m) {
+              gm[k][m] = fa(gm[k][m], fm(ar, bs[m]));
+              bl[k][m] = fa(bl[k][m], fm(as[m], bc));
+            }
+          }
         }
       }
+      __syncthreads();
+      if (s_abort) break;
+      if (tid == 0 && c + SCAN_NSTAGE < nch) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c + SCAN_NSTAGE);
+    }
+    if (s_abort) {
+      aborted = true;
+      break;
+    }
+    const float2* Tw = s_T[warp];
+#pragma unroll
+    for (int k = 0; k < SCAN_RPT; ++k) {
+      const int r = tid + k * SCAN_THREADS;
+      if (r >= ns) continue;
+#pragma unroll
       for (int l = 0; l < dim; ++l) {
         float2 a = make_float2(0.f, 0.f);
-        for (int m = 0; m < dim; ++m) a = fa(a, fm(gm[m], s_T[m + dim * l]));
-        A[(size_t)(K + l) * ns + r] = a;
-        float2 bv = make_float2(-bl[l].x, -bl[l].y);
-        if (r == s_S[l]) bv.x += 1.f;
-        B[(size_t)(K + l) * ns + r] = bv;
+#pragma unroll
+        for (int m = 0; m < dim; ++m) a = fa(a, fm(gm[k][m], Tw[m + dim * l]));
+        float2 bv = make_float2(-bl[k][l].x, -bl[k][l].y);
+        if (r == S[l]) bv.x += 1.f;
+        A[(size_t)(K + l) * ldp + r] = a;
+        B[(size_t)(K + l) * ldp + r] = bv;
+        s_newA[(size_t)l * ns + r] = a;
+        s_newB[(size_t)l * ns + r] = bv;
       }
+    }
+    __syncthreads();
+    // ---- the new block's contribution to the cached Geff of later plaquettes
+    for (int e = tid; e < (npla - p - 1) * dd; e += blockDim.x) {
+      const int pq = p + 1 + e / dd, k = e % dd;
+      const int si = s_site[4 * pq + k % dim], sj = s_site[4 * pq + k / dim];
+      float2 a = s_geff[16 * pq + k];
+#pragma unroll
+      for (int l = 0; l < dim; ++l) a = fa(a, fm(s_newA[(size_t)l * ns + si], s_newB[(size_t)l * ns + sj]));
+      s_geff[16 * pq + k] = a;
     }
     K += dim;
     __syncthreads();
   }
-  if (tid == 0) {
-    *d.kcount = K;
-    next_p[blockIdx.x] = p;
-    if (pa > 0) {
-      double l = (lprod > 0.0) ? log(lprod) + (double)lexp * 0.69314718055994530942 : log(lprod);
-      d.sc->ln_cw = cadd(d.sc->ln_cw, mk(l));
+  if (aborted) {
+    // a panel chunk never arrived: give the copies still in flight a bounded
+    // wait, flag the chain and stop (the host reports PQMC_ERR_TIMEOUT)
+    if (tid == 0) {
+      for (int st = 0; st < SCAN_NSTAGE; ++st) mbar_wait_bounded(&s_full[st], (phase >> st) & 1u);
+      d.sc->status = PQMC_ERR_TIMEOUT;
+      atomicExch(d.err, PQMC_ERR_TIMEOUT);
+      *d.kcount = 0;
+      next_p[blockIdx.x] = npla;
     }
-    d.sc->pos_acc += pa;
-    d.sc->neg_acc += na;
+    return;
+  }
+  __syncthreads();
+  // ---- bookkeeping of the round's accepted moves (field, expKV, ln_cw) -----
+  for (int e = tid; e < n_acc * pd * pd; e += blockDim.x) {
+    const int ja = e / (pd * pd), k = e % (pd * pd);
+    const int pa_ = s_accp[ja], ii = k % pd, jj = k / pd;
+    const bool in = ii < dim && jj < dim;
+    const size_t base2 = M.kv_base(pa_, pf, t);
+    d.expkv[base2 + k] = in ? pre[pa_].enew[ii + dim * jj] : mk(0.0);
+    d.expkv_inv[base2 + k] = in ? pre[pa_].einv[ii + dim * jj] : mk(0.0);
+  }
+  for (int ja = tid; ja < n_acc; ja += blockDim.x) {
+    const int pa_ = s_accp[ja];
+    d.field[M.bf[pa_ + M.max_pla * pf] + (size_t)M.n_bf * t] = pre[pa_].xnew;
+  }
+  if (warp == 0) {
+    // ln_cw += log prod_j Re(R_j^ncopy) (|R_j|^2 under TR_weight), as a
+    // mantissa/exponent product so long rounds cannot overflow
+    double mant = 1.0;
+    long long ex = 0;
+    for (int ja = lane; ja < n_acc; ja += 32) {
+      const double dr = s_accd[ja].x, di = s_accd[ja].y;
+      double rr = dr, ri = di;
+      if (M.tr_weight) { rr = dr * dr + di * di; ri = 0.0; }
+      double ar = 1.0, ai = 0.0;
+      for (int k = 0; k < M.ncopy; ++k) {
+        const double tr = ar * rr - ai * ri;
+        ai = ar * ri + ai * rr;
+        ar = tr;
+      }
+      int e2;
+      mant *= frexp(ar, &e2);
+      ex += e2;
+      mant = frexp(mant, &e2);
+      ex += e2;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double om = __shfl_down_sync(0xffffffffu, mant, o);
+      const long long oe = __shfl_down_sync(0xffffffffu, ex, o);
+      if (lane + o < 32) {
+        int e2;
+        mant = frexp(mant * om, &e2);
+        ex += oe + e2;
+      }
+    }
+    if (lane == 0) {
+      *d.kcount = K;
+      next_p[blockIdx.x] = p;
+      if (n_acc > 0) {
+        const double l = (mant > 0.0) ? log(mant) + (double)ex * 0.69314718055994530942 : log(mant);
+        d.sc->ln_cw = cadd(d.sc->ln_cw, mk(l));
+      }
+      d.sc->pos_acc += n_acc;
+      d.sc->neg_acc += na;
+    }
   }
 }
 
@@ -412,7 +647,7 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
   const int tiles_m = (ns + FB_M - 1) / FB_M, tiles_n = (ns + FB_N - 1) / FB_N;
   const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
   if (tn >= tiles_n) return;
-  cplx* G = parity ? d.g_alt : d.g;
+  float4* G = reinterpret_cast<float4*>(parity ? d.g_alt : d.g);   // double-float G
   // As[split][comp re,im][m][k], Bs[split][comp re,im,-im][n][k]
   __shared__ __align__(16) __nv_bfloat16 As[3][2][FB_M][FB_LD];
   __shared__ __align__(16) __nv_bfloat16 Bs[3][3][FB_N][FB_LD];
@@ -428,7 +663,7 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
     for (int e = tid; e < FB_M * FB_K; e += 256) {
       int r = e % FB_M, q = e / FB_M;
       float2 v = make_float2(0.f, 0.f);
-      if (row0 + r < ns && k0 + q < K) v = d.A[(size_t)(k0 + q) * ns + row0 + r];
+      if (row0 + r < ns && k0 + q < K) v = d.A[(size_t)(k0 + q) * d.ldp + row0 + r];
       __nv_bfloat16 sp[3];
       split3(v.x, sp);
       As[0][0][r][q] = sp[0]; As[1][0][r][q] = sp[1]; As[2][0][r][q] = sp[2];
@@ -438,7 +673,7 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
     for (int e = tid; e < FB_N * FB_K; e += 256) {
       int cix = e % FB_N, q = e / FB_N;
       float2 v = make_float2(0.f, 0.f);
-      if (col0 + cix < ns && k0 + q < K) v = d.B[(size_t)(k0 + q) * ns + col0 + cix];
+      if (col0 + cix < ns && k0 + q < K) v = d.B[(size_t)(k0 + q) * d.ldp + col0 + cix];
       __nv_bfloat16 sp[3];
       split3(v.x, sp);
       Bs[0][0][cix][q] = sp[0]; Bs[1][0][cix][q] = sp[1]; Bs[2][0][cix][q] = sp[2];
@@ -481,15 +716,19 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
       const int r = row0 + wm * 16 + g + ((e >> 1) ? 8 : 0);
       const int cc = col0 + wn * 32 + nt * 8 + 2 * tq + (e & 1);
       if (r < ns && cc < ns) {
-        cplx* p = G + r + (size_t)ns * cc;
-        *p = cadd(*p, mk((double)acc[nt][0][e], (double)acc[nt][1][e]));
+        float4* p = G + r + (size_t)ns * cc;
+        *p = dg_addf(*p, make_float2(acc[nt][0][e], acc[nt][1][e]));
       }
     }
 }
 
 // ---------------------------------------------------------------------------
 // Two-way wrap with an FP32 correction on the FP64 G (left: A=expKV, B=expKV_inv).
-__global__ void k_bwrap(const BDesc* D, int pf, int t, int left, int n_items, int parity) {
+// One thread per (row item, column item) block of the family's cover; items
+// are the family's plaquettes (DIM sites) and uncovered singletons, so every
+// block is at most DIM x DIM and lives in registers.
+template <int DIM>
+__global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, int left, int n_items, int parity) {
   __shared__ BDesc sd;
   if (threadIdx.x == 0) sd = D[blockIdx.y];
   __syncthreads();
@@ -500,56 +739,89 @@ __global__ void k_bwrap(const BDesc* D, int pf, int t, int left, int n_items, in
   const int ir = (int)(pair % n_items), ic = (int)(pair / n_items);
   const int ns = M.ns, pd = M.pdim;
   const int dr = d.wdim[ir], dc = d.wdim[ic];
-  const cplx* gin = parity ? d.g_alt : d.g;
-  cplx* gout = parity ? d.g : d.g_alt;
-  int Sr[4], Sc[4];
-  for (int k = 0; k < dr; ++k) Sr[k] = d.wsites[4 * ir + k];
-  for (int k = 0; k < dc; ++k) Sc[k] = d.wsites[4 * ic + k];
-  cplx gd[16];
-  float2 gf[16], gb[16];
-  for (int b = 0; b < dc; ++b)
-    for (int a = 0; a < dr; ++a) {
-      gd[a + 4 * b] = gin[Sr[a] + (size_t)ns * Sc[b]];
-      gf[a + 4 * b] = f2(gd[a + 4 * b]);
+  const float4* gin = reinterpret_cast<const float4*>(parity ? d.g_alt : d.g);   // double-float G
+  float4* gout = reinterpret_cast<float4*>(parity ? d.g : d.g_alt);
+  int Sr[DIM], Sc[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    Sr[k] = k < dr ? d.wsites[4 * ir + k] : 0;
+    Sc[k] = k < dc ? d.wsites[4 * ic + k] : 0;
+  }
+  float4 gd[DIM][DIM];
+  float2 gf[DIM][DIM], am[DIM][DIM], bm[DIM][DIM];
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      gd[a][b] = (a < dr && b < dc) ? gin[Sr[a] + (size_t)ns * Sc[b]] : make_float4(0.f, 0.f, 0.f, 0.f);
+      gf[a][b] = dg_f2(gd[a][b]);
     }
   const int pr = d.wpla[ir], pc = d.wpla[ic];
   const cplx* Am = (pr >= 0) ? (left ? d.expkv : d.expkv_inv) + M.kv_base(pr, pf, t) : nullptr;
   const cplx* Bm = (pc >= 0) ? (left ? d.expkv_inv : d.expkv) + M.kv_base(pc, pf, t) : nullptr;
-  // gb = G B
-  for (int b = 0; b < dc; ++b)
-    for (int a = 0; a < dr; ++a) {
+  // (A - I) and (B - I) in FP32; identity blocks for singletons
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      // A - I and B - I formed in FP64 and rounded once
+      const double one = a == b ? 1.0 : 0.0;
+      am[a][b] = (Am && a < dr && b < dr) ? f2(csub(Am[a + pd * b], mk(one))) : make_float2(0.f, 0.f);
+      bm[a][b] = (Bm && a < dc && b < dc) ? f2(csub(Bm[a + pd * b], mk(one))) : make_float2(0.f, 0.f);
+    }
+  // corr = (A - I) (G B) + G (B - I) = (A - I) G + (A - I) G (B - I) + G (B - I)
+  float2 gb[DIM][DIM];   // G (B - I)
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
       float2 s = make_float2(0.f, 0.f);
-      if (Bm) {
-        for (int k = 0; k < dc; ++k) s = fa(s, fm(gf[a + 4 * k], f2(Bm[k + pd * b])));
-      } else {
-        s = gf[a + 4 * b];
-      }
-      gb[a + 4 * b] = s;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) s = fa(s, fm(gf[a][k], bm[k][b]));
+      gb[a][b] = s;
     }
-  for (int b = 0; b < dc; ++b)
-    for (int a = 0; a < dr; ++a) {
-      float2 corr = make_float2(0.f, 0.f);
-      if (Am)
-        for (int k = 0; k < dr; ++k) {
-          float2 am = f2(Am[a + pd * k]);
-          if (k == a) am.x -= 1.f;
-          corr = fa(corr, fm(am, gb[k + 4 * b]));
-        }
-      if (Bm)
-        for (int k = 0; k < dc; ++k) {
-          float2 bm = f2(Bm[k + pd * b]);
-          if (k == b) bm.x -= 1.f;
-          corr = fa(corr, fm(gf[a + 4 * k], bm));
-        }
-      gout[Sr[a] + (size_t)ns * Sc[b]] = cadd(gd[a + 4 * b], mk((double)corr.x, (double)corr.y));
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      float2 corr = gb[a][b];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) corr = fa(corr, fm(am[a][k], fa(gf[k][b], gb[k][b])));
+      if (a < dr && b < dc) gout[Sr[a] + (size_t)ns * Sc[b]] = dg_addf(gd[a][b], corr);
     }
+}
+
+// G of every chain converted in place between FP64 complex (at rest) and the
+// double-float float4 form the mixed sweep works on
+__global__ void k_gconv(const BDesc* D, int to_df, long n) {
+  cplx* G = D[blockIdx.y].g;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    if (to_df) {
+      const cplx v = G[e];
+      reinterpret_cast<float4*>(G)[e] = dg_make(v);
+    } else {
+      const float4 v = reinterpret_cast<const float4*>(G)[e];
+      G[e] = dg_to_d(v);
+    }
+  }
 }
 
 }  // namespace pqmc
 
 // ===========================================================================
+struct PhaseMark {
+  int phase;
+  cudaEvent_t a, b;
+};
+
 struct pqmc_batch {
   std::vector<pqmc_chain*> chains;
+  // CUDA-event timers per phase of the family step (PQMC_PHASE_*)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<PhaseMark> marks;
+  double phase_ms[PQMC_N_PHASES] = {};
+  long long phase_n[PQMC_N_PHASES] = {};
   int precision = PQMC_PREC_FP64;
   pqmc::BDesc* d_desc = nullptr;
   std::vector<pqmc::BDesc> h_desc;
@@ -557,6 +829,8 @@ struct pqmc_batch {
   std::vector<int*> kcounts;
   int parity = 0;
   int kd = 64;            // delay depth (panel columns per flush)
+  int qc = 8;             // panel columns per streamed chunk of the scan
+  int* d_err = nullptr;   // device error word shared by all chains
   int* d_next = nullptr;  // per chain: next plaquette of the current family step
   cudaStream_t stream = nullptr;
   pqmc::BatchRecompute rec;
@@ -568,6 +842,49 @@ extern "C" int pqmc_create(const pqmc_model* model, pqmc_chain** out);
 extern "C" int pqmc_destroy(pqmc_chain* c);
 extern "C" int pqmc_sweep(pqmc_chain* c, int first_loop, int n_sweeps, int warmup, int meas_interval,
                           int meas_number, double* records, int n_records_cap, int* n_records);
+extern "C" int pqmc_sweep_slices(pqmc_chain* c, int loop, int first_tc, int n_slices);
+extern "C" int pqmc_init_g(pqmc_chain* c, int start_time);
+
+static cudaEvent_t ev_take(pqmc_batch* b) {
+  if (!b->ev_pool.empty()) {
+    cudaEvent_t e = b->ev_pool.back();
+    b->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+// open a timed phase on the batch stream (no-op unless timing is on)
+static cudaEvent_t phase_begin(pqmc_batch* b) {
+  if (!b->timing) return nullptr;
+  cudaEvent_t e = ev_take(b);
+  if (e) cudaEventRecord(e, b->stream);
+  return e;
+}
+
+static void phase_end(pqmc_batch* b, int phase, cudaEvent_t a) {
+  if (!b->timing || !a) return;
+  cudaEvent_t e = ev_take(b);
+  if (!e) return;
+  cudaEventRecord(e, b->stream);
+  b->marks.push_back(PhaseMark{phase, a, e});
+}
+
+// after a stream synchronisation: fold the recorded pairs into the totals
+static int phase_resolve(pqmc_batch* b) {
+  for (auto& m : b->marks) {
+    float ms = 0.f;
+    PQMC_CUDA(cudaEventElapsedTime(&ms, m.a, m.b));
+    b->phase_ms[m.phase] += ms;
+    b->phase_n[m.phase] += 1;
+    b->ev_pool.push_back(m.a);
+    b->ev_pool.push_back(m.b);
+  }
+  b->marks.clear();
+  return PQMC_OK;
+}
 
 static int batch_refresh(pqmc_batch* b) {
   // current G of every chain is c->g; rebuild descriptors, parity 0
@@ -605,9 +922,17 @@ static int bwrap(pqmc_batch* b, int pf, int time, bool left) {
   PQMC_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), sizeof(BDesc) * b->h_desc.size(), cudaMemcpyHostToDevice,
                             b->stream));
   long pairs = (long)w.n_items * w.n_items;
-  dim3 grid((unsigned)((pairs + 63) / 64), (unsigned)b->chains.size());
-  k_bwrap<<<grid, 64, 0, b->stream>>>(b->d_desc, pf, time - 1, left ? 1 : 0, w.n_items, b->parity);
+  dim3 grid((unsigned)((pairs + 127) / 128), (unsigned)b->chains.size());
+  const int l = left ? 1 : 0;
+  cudaEvent_t tw = phase_begin(b);
+  switch (c0->h_pf_dim[pf]) {
+    case 1: k_bwrap<1><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
+    case 2: k_bwrap<2><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
+    case 3: k_bwrap<3><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
+    default: k_bwrap<4><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
+  }
   PQMC_LAUNCHED();
+  phase_end(b, PQMC_PHASE_WRAP, tw);
   b->parity ^= 1;
   return PQMC_OK;
 }
@@ -616,20 +941,32 @@ static int bupdate(pqmc_batch* b, int pf, int time) {
   const int C = (int)b->chains.size();
   pqmc_chain* c0 = b->chains[0];
   const int npla = c0->h_pf_npla[pf], dim = c0->h_pf_dim[pf];
+  cudaEvent_t tp = phase_begin(b);
   k_bdraw<<<(C + 63) / 64, 64, 0, b->stream>>>(b->d_desc, C, pf);
   PQMC_LAUNCHED();
   k_bprep<<<dim3((npla + 7) / 8, C), 256, 0, b->stream>>>(b->d_desc, pf, time - 1);
   PQMC_LAUNCHED();
+  phase_end(b, PQMC_PHASE_PREP, tp);
   PQMC_CUDA(cudaMemsetAsync(b->d_next, 0, sizeof(int) * C, b->stream));
   const int kd = std::max(dim, std::min(b->kd, b->h_desc[0].kmax));
   // enough rounds for the worst case (every proposal accepted)
   const int rounds = (npla * dim + (kd / dim) * dim - 1) / ((kd / dim) * dim);
   const int tiles = ((c0->ns + FB_M - 1) / FB_M) * ((c0->ns + FB_N - 1) / FB_N);
   for (int r = 0; r < rounds; ++r) {
-    k_bscan<<<C, SCAN_THREADS, 0, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->d_next);
+    const size_t smem = scan_layout(npla, c0->ns, b->h_desc[0].ldp, b->qc, kd).total;
+    cudaEvent_t ts = phase_begin(b);
+    switch (dim) {
+      case 1: k_bscan<1><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
+      case 2: k_bscan<2><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
+      case 3: k_bscan<3><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
+      default: k_bscan<4><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
+    }
     PQMC_LAUNCHED();
+    phase_end(b, PQMC_PHASE_SCAN, ts);
+    cudaEvent_t tf = phase_begin(b);
     k_bflush<<<dim3(tiles, C), 256, 0, b->stream>>>(b->d_desc, b->parity);
     PQMC_LAUNCHED();
+    phase_end(b, PQMC_PHASE_FLUSH, tf);
   }
   return PQMC_OK;
 }
@@ -637,7 +974,9 @@ static int bupdate(pqmc_batch* b, int pf, int time) {
 static int bscratch(pqmc_batch* b, int time, bool forward, int loop) {
   (void)loop;
   PQMC_TRY(batch_sync_parity(b));
+  cudaEvent_t tr = phase_begin(b);
   PQMC_TRY(b->rec.scratch(time, forward));
+  phase_end(b, PQMC_PHASE_RECOMPUTE, tr);
   return batch_refresh(b);
 }
 
@@ -674,7 +1013,40 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   PQMC_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   int kmax = 0;
   for (int f = 0; f < c0->n_pf; ++f) kmax = std::max(kmax, c0->h_pf_npla[f] * c0->h_pf_dim[f]);
-  if (kmax > SCAN_KSTAGE) { set_error("batch_create: family too large for the staged panels"); return PQMC_ERR_ARG; }
+  if (kmax > SCAN_KSTAGE) {
+    set_error("batch_create: family too large for the staged panels");
+    pqmc_batch_destroy(b);
+    return PQMC_ERR_ARG;
+  }
+  const int ldp = (c0->ns + 1) & ~1;
+  if (precision == PQMC_PREC_MIXED) {
+    if (c0->ns > SCAN_RPT * SCAN_THREADS) {
+      set_error("batch_create: mixed precision supports Ns <= %d", SCAN_RPT * SCAN_THREADS);
+      pqmc_batch_destroy(b);
+      return PQMC_ERR_ARG;
+    }
+    int max_pla = 0, dev = 0, optin = 0;
+    for (int f = 0; f < c0->n_pf; ++f) max_pla = std::max(max_pla, c0->h_pf_npla[f]);
+    PQMC_CUDA(cudaGetDevice(&dev));
+    PQMC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t stat = 4096;   // static shared memory of k_bscan (descriptor, per-warp R and T, barriers)
+    int qc = 8;
+    while (qc > 1 && scan_layout(max_pla, c0->ns, ldp, qc, SCAN_KSTAGE).total + stat > (size_t)optin) qc /= 2;
+    const size_t need = scan_layout(max_pla, c0->ns, ldp, qc, SCAN_KSTAGE).total;
+    if (need + stat > (size_t)optin) {
+      set_error("batch_create: scan staging needs %zu bytes of shared memory, the device offers %d", need + stat,
+                optin);
+      pqmc_batch_destroy(b);
+      return PQMC_ERR_ARG;
+    }
+    b->qc = qc;
+    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+  }
+  PQMC_CUDA(cudaMalloc((void**)&b->d_err, sizeof(int)));
+  PQMC_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
   b->h_desc.resize(n_chains);
   for (int i = 0; i < n_chains; ++i) {
     pqmc_chain* c = b->chains[i];
@@ -687,15 +1059,17 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     h.g = c->g;
     h.g_alt = c->g_alt;
     h.kmax = kmax;
+    h.ldp = ldp;
+    h.err = b->d_err;
     h.pre = c->pre;
     h.sc = c->sc;
     float2* pan = nullptr;
     int* kc = nullptr;
     if (precision == PQMC_PREC_MIXED) {
-      PQMC_CUDA(cudaMalloc((void**)&pan, sizeof(float2) * (size_t)2 * kmax * c->ns));
+      PQMC_CUDA(cudaMalloc((void**)&pan, sizeof(float2) * (size_t)2 * kmax * ldp));
       PQMC_CUDA(cudaMalloc((void**)&kc, sizeof(int)));
       h.A = pan;
-      h.B = pan + (size_t)kmax * c->ns;
+      h.B = pan + (size_t)kmax * ldp;
       h.kcount = kc;
     }
     b->panels.push_back(pan);
@@ -713,6 +1087,11 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
 int pqmc_batch_destroy(pqmc_batch* b) {
   if (!b) return PQMC_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& m : b->marks) {
+    cudaEventDestroy(m.a);
+    cudaEventDestroy(m.b);
+  }
+  for (auto e : b->ev_pool) cudaEventDestroy(e);
   for (auto* c : b->chains) pqmc_destroy(c);
   for (auto* p : b->panels)
     if (p) cudaFree(p);
@@ -720,6 +1099,7 @@ int pqmc_batch_destroy(pqmc_batch* b) {
     if (k) cudaFree(k);
   if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_next) cudaFree(b->d_next);
+  if (b->d_err) cudaFree(b->d_err);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return PQMC_OK;
@@ -731,26 +1111,81 @@ int pqmc_batch_set_delay(pqmc_batch* b, int kd) {
   return PQMC_OK;
 }
 
+int pqmc_batch_init(pqmc_batch* b) {
+  if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  for (auto* c : b->chains) PQMC_TRY(launch_init_expkv(c, 0, c->ntime));
+  for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  pqmc_chain* c0 = b->chains[0];
+  if (b->precision == PQMC_PREC_FP64 || c0->ntime % c0->ngroup != 0) {
+    for (auto* c : b->chains) PQMC_TRY(pqmc_init_g(c, 1));
+    return PQMC_OK;
+  }
+  PQMC_TRY(b->rec.init_g());
+  for (auto* c : b->chains) c->have_g = true;
+  return batch_refresh(b);
+}
+
+int pqmc_batch_set_timing(pqmc_batch* b, int enable) {
+  if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  PQMC_TRY(phase_resolve(b));
+  b->timing = enable != 0;
+  for (int k = 0; k < PQMC_N_PHASES; ++k) {
+    b->phase_ms[k] = 0.0;
+    b->phase_n[k] = 0;
+  }
+  return PQMC_OK;
+}
+
+int pqmc_batch_get_timing(pqmc_batch* b, double* ms, long long* launches) {
+  if (!b || !ms || !launches) { set_error("batch_get_timing: null argument"); return PQMC_ERR_ARG; }
+  PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  PQMC_TRY(phase_resolve(b));
+  for (int k = 0; k < PQMC_N_PHASES; ++k) {
+    ms[k] = b->phase_ms[k];
+    launches[k] = b->phase_n[k];
+  }
+  return PQMC_OK;
+}
+
+int pqmc_batch_stream(pqmc_batch* b, void** stream) {
+  if (!b || !stream) { set_error("batch_stream: null argument"); return PQMC_ERR_ARG; }
+  *stream = (void*)b->stream;
+  return PQMC_OK;
+}
+
 int pqmc_batch_chain(pqmc_batch* b, int i, pqmc_chain** chain) {
   if (!b || !chain || i < 0 || i >= (int)b->chains.size()) { set_error("batch_chain: bad index"); return PQMC_ERR_ARG; }
   *chain = b->chains[i];
   return PQMC_OK;
 }
 
-int pqmc_batch_sweep(pqmc_batch* b, int loop) {
+int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices) {
   if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
   for (auto* c : b->chains)
     if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
+  pqmc_chain* c0 = b->chains[0];
+  if (first_tc < 1 || n_slices < 0) { set_error("batch_sweep_slices: bad slice range"); return PQMC_ERR_ARG; }
   if (b->precision == PQMC_PREC_FP64) {
-    for (auto* c : b->chains) PQMC_TRY(pqmc_sweep(c, loop, 1, 1 << 30, 1, 0, nullptr, 0, nullptr));
+    for (auto* c : b->chains) {
+      const int n = std::min(n_slices, c->ntime - first_tc + 1);
+      if (n > 0) PQMC_TRY(pqmc_sweep_slices(c, loop, first_tc, n));
+    }
     return PQMC_OK;
+  }
+  if (first_tc + n_slices - 1 > c0->ntime) {
+    set_error("batch_sweep_slices: slices %d..%d outside 1..%d", first_tc, first_tc + n_slices - 1, c0->ntime);
+    return PQMC_ERR_ARG;
   }
   // every chain finished its own previous work on its stream
   for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
   PQMC_TRY(batch_refresh(b));
-  pqmc_chain* c0 = b->chains[0];
+  const long ng2 = (long)c0->ns * c0->ns;
+  const dim3 cgrid((unsigned)std::min<long>((ng2 + 255) / 256, 64), (unsigned)b->chains.size());
+  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 1, ng2);
+  PQMC_LAUNCHED();
   const bool forward = (loop % 2) == 0;
-  for (int tc = 1; tc <= c0->ntime; ++tc) {
+  for (int tc = first_tc; tc < first_tc + n_slices; ++tc) {
     int time;
     if (!forward) {
       time = c0->ntime - tc + 1;
@@ -768,8 +1203,28 @@ int pqmc_batch_sweep(pqmc_batch* b, int loop) {
     if (tc % c0->ngroup == 0) PQMC_TRY(bscratch(b, forward ? time + 1 : time, forward, loop));
   }
   PQMC_TRY(batch_sync_parity(b));
+  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2);
+  PQMC_LAUNCHED();
+  int err = 0;
+  PQMC_CUDA(cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  PQMC_TRY(phase_resolve(b));
+  if (err != 0) {
+    set_error("batch sweep: a device-side wait gave up (panel stream of the scan)");
+    return err;
+  }
   return PQMC_OK;
+}
+
+int pqmc_batch_sweep(pqmc_batch* b, int loop) {
+  if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  if (b->precision == PQMC_PREC_FP64) {
+    for (auto* c : b->chains)
+      if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
+    for (auto* c : b->chains) PQMC_TRY(pqmc_sweep(c, loop, 1, 1 << 30, 1, 0, nullptr, 0, nullptr));
+    return PQMC_OK;
+  }
+  return pqmc_batch_sweep_slices(b, loop, 1, b->chains[0]->ntime);
 }
 
 }  // extern "C"

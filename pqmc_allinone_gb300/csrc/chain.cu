@@ -31,12 +31,14 @@ static __device__ __forceinline__ cplx ldg_c(const cplx* p) { return __ldcg(p); 
 
 // ---------------------------------------------------------------------------
 // init_expKV for every (family, plaquette, slice) (mod_phonon_field.f90:423-450)
-__global__ void k_init_expkv(DevModel M, const double* __restrict__ field, cplx* expkv, cplx* expkv_inv) {
-  const long total = (long)M.n_pf * M.max_pla * M.ntime;
+// expKV / expKV_inv of slices t0 .. t0+nt-1 (0-based) from the field
+__global__ void k_init_expkv(DevModel M, const double* __restrict__ field, cplx* expkv, cplx* expkv_inv, int t0,
+                             int nt) {
+  const long total = (long)M.n_pf * M.max_pla * nt;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
     int p = (int)(e % M.max_pla);
     int pf = (int)((e / M.max_pla) % M.n_pf);
-    int t = (int)(e / ((long)M.max_pla * M.n_pf));
+    int t = t0 + (int)(e / ((long)M.max_pla * M.n_pf));
     if (p >= M.pf_npla[pf]) continue;
     double bf = M.pf_v_exist[pf] ? field[M.bf[p + M.max_pla * pf] + (size_t)M.n_bf * t] : 0.0;
     const int dim = M.pf_dim[pf];
@@ -53,11 +55,12 @@ __global__ void k_init_expkv(DevModel M, const double* __restrict__ field, cplx*
   }
 }
 
-int launch_init_expkv(pqmc_chain* c) {
-  long total = (long)c->n_pf * c->max_pla * c->ntime;
+int launch_init_expkv(pqmc_chain* c, int t0, int nt) {
+  if (nt <= 0) nt = c->ntime - t0;
+  long total = (long)c->n_pf * c->max_pla * nt;
   int blocks = (int)((total + 127) / 128);
   if (blocks > 4096) blocks = 4096;
-  k_init_expkv<<<blocks, 128, 0, c->stream>>>(c->M, c->field, c->expkv, c->expkv_inv);
+  k_init_expkv<<<blocks, 128, 0, c->stream>>>(c->M, c->field, c->expkv, c->expkv_inv, t0, nt);
   PQMC_LAUNCHED();
   return PQMC_OK;
 }
@@ -254,25 +257,44 @@ __global__ void k_finish_weight(DevScalars* sc, int tr_weight, int ncopy, int co
   sc->ln_cw = nw;
 }
 
+// out[0] = max |a - b| (atomicMax on the bit pattern of a non-negative
+// double), out[1] += sum |a - b|^2, out[2] += sum |b|^2
 __global__ void k_maxdiff(long n, const cplx* __restrict__ a, const cplx* __restrict__ b, double* out) {
-  __shared__ double red[256];
-  double m = 0.0;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    m = fmax(m, cabsd(csub(a[i], b[i])));
+  __shared__ double red[256], rd[256], rb[256];
+  double m = 0.0, sd = 0.0, sb = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const cplx bi = b[i], di = csub(a[i], bi);
+    m = fmax(m, cabsd(di));
+    sd += cabs2(di);
+    sb += cabs2(bi);
+  }
   red[threadIdx.x] = m;
+  rd[threadIdx.x] = sd;
+  rb[threadIdx.x] = sb;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    if (threadIdx.x < s) {
+      red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+      rd[threadIdx.x] += rd[threadIdx.x + s];
+      rb[threadIdx.x] += rb[threadIdx.x + s];
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicMax((unsigned long long*)out, __double_as_longlong(red[0]));
+  if (threadIdx.x == 0) {
+    atomicMax((unsigned long long*)out, __double_as_longlong(red[0]));
+    atomicAdd(out + 1, rd[0]);
+    atomicAdd(out + 2, rb[0]);
+  }
 }
 
 __global__ void k_set_errg(DevScalars* sc, const double* e) {
-  double v = *e;
+  double v = e[0];
   sc->err_g = v;
   sc->err_fast = v;
   if (v > sc->err_fast_max) sc->err_fast_max = v;
+  const double rel = e[2] > 0.0 ? sqrt(e[1] / e[2]) : 0.0;
+  sc->err_g_rel = rel;
+  if (rel > sc->err_g_rel_max) sc->err_g_rel_max = rel;
 }
 
 __global__ void k_scalars_zero(DevScalars* sc) {
@@ -295,7 +317,7 @@ static int cal_g_and_det(pqmc_chain* c, const cplx* X, const cplx* R, bool compa
   PQMC_TRY(zgemm(s, 'N', 'N', ns, ns, ne, mk(1.0), R, ns, c->lmat, ne, mk(0.0), c->g_alt, ns));
   if (compare) {
     double* e = reinterpret_cast<double*>(c->lcol);   // scratch scalar
-    PQMC_CUDA(cudaMemsetAsync(e, 0, sizeof(double), s));
+    PQMC_CUDA(cudaMemsetAsync(e, 0, 3 * sizeof(double), s));
     k_maxdiff<<<152, 256, 0, s>>>((long)ns * ns, c->g, c->g_alt, e);
     PQMC_LAUNCHED();
     k_set_errg<<<1, 1, 0, s>>>(c->sc, e);
@@ -669,6 +691,31 @@ int pqmc_set_field(pqmc_chain* c, const double* f) {
   return PQMC_OK;
 }
 
+int pqmc_set_field_slices(pqmc_chain* c, int first_time, int n_times, const double* f) {
+  CHK_CHAIN(c);
+  if (!f || first_time < 1 || n_times < 1 || first_time + n_times - 1 > c->ntime) {
+    set_error("set_field_slices: slices %d..%d outside 1..%d", first_time, first_time + n_times - 1, c->ntime);
+    return PQMC_ERR_ARG;
+  }
+  PQMC_CUDA(cudaMemcpyAsync(c->field + (size_t)c->n_bf * (first_time - 1), f, sizeof(double) * (size_t)c->n_bf * n_times,
+                            cudaMemcpyHostToDevice, c->stream));
+  PQMC_TRY(launch_init_expkv(c, first_time - 1, n_times));
+  PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  return PQMC_OK;
+}
+
+int pqmc_get_field_slices(pqmc_chain* c, int first_time, int n_times, double* f) {
+  CHK_CHAIN(c);
+  if (!f || first_time < 1 || n_times < 1 || first_time + n_times - 1 > c->ntime) {
+    set_error("get_field_slices: slices %d..%d outside 1..%d", first_time, first_time + n_times - 1, c->ntime);
+    return PQMC_ERR_ARG;
+  }
+  PQMC_CUDA(cudaMemcpyAsync(f, c->field + (size_t)c->n_bf * (first_time - 1), sizeof(double) * (size_t)c->n_bf * n_times,
+                            cudaMemcpyDeviceToHost, c->stream));
+  PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  return PQMC_OK;
+}
+
 int pqmc_get_field(pqmc_chain* c, double* f) {
   CHK_CHAIN(c);
   PQMC_CUDA(cudaMemcpyAsync(f, c->field, sizeof(double) * (size_t)c->n_bf * c->ntime, cudaMemcpyDeviceToHost,
@@ -710,6 +757,8 @@ int pqmc_get_state(pqmc_chain* c, pqmc_state* out) {
   out->ln_cw[1] = h.ln_cw.y;
   out->err_fast_max = h.err_fast_max;
   out->err_fast = h.err_fast;
+  out->err_g = h.err_g;
+  out->err_g_rel_max = h.err_g_rel_max;
   out->positive_accept = h.pos_acc;
   out->negative_accept = h.neg_acc;
   for (int k = 0; k < 5; ++k) out->rng[k] = h.rng[k];
@@ -739,7 +788,7 @@ int pqmc_get_qd(pqmc_chain* c, int block, double* q, double* d) {
 
 int pqmc_init_expkv(pqmc_chain* c) {
   CHK_CHAIN(c);
-  PQMC_TRY(launch_init_expkv(c));
+  PQMC_TRY(launch_init_expkv(c, 0, c->ntime));
   PQMC_CUDA(cudaStreamSynchronize(c->stream));
   return PQMC_OK;
 }

@@ -17,6 +17,8 @@ struct DevScalars {
   double err_fast_max;
   double err_g;
   double err_w;
+  double err_g_rel;       // ||G_fast - G_scratch||_F / ||G_scratch||_F at the last recompute
+  double err_g_rel_max;   // largest err_g_rel so far
   long long pos_acc;
   long long neg_acc;
   int rng[5];
@@ -109,7 +111,7 @@ struct pqmc_chain {
 namespace pqmc {
 int chain_alloc(pqmc_chain* c, const pqmc_model* m, cudaStream_t s);
 int chain_free(pqmc_chain* c);
-int launch_init_expkv(pqmc_chain* c);
+int launch_init_expkv(pqmc_chain* c, int t0, int nt);
 int launch_update(pqmc_chain* c, int pf, int time);
 int update_setup(pqmc_chain* c);
 int launch_wrap(pqmc_chain* c, int pf, int time, bool left);

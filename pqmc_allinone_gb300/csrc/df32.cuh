@@ -86,3 +86,31 @@ __device__ __forceinline__ dfc dfc_mulc(dfc a, dfc b) {
   return dfc{df_add(df_mul(a.re, b.re), df_mul(a.im, b.im)), df_sub(df_mul(a.re, b.im), df_mul(a.im, b.re))};
 }
 __device__ __forceinline__ dfc dfc_zero() { return dfc{{0.0f, 0.0f}, {0.0f, 0.0f}}; }
+
+// A complex double-float held in 16 bytes as float4 {re_hi, im_hi, re_lo,
+// im_lo}: the storage of G inside a mixed-precision batched sweep (the same
+// footprint as an FP64 complex, converted in place at the sweep boundary).
+__device__ __forceinline__ float4 dg_make(double2 v) {
+  const df r = df_make(v.x), i = df_make(v.y);
+  return make_float4(r.hi, i.hi, r.lo, i.lo);
+}
+__device__ __forceinline__ double2 dg_to_d(float4 g) {
+  return make_double2((double)g.x + (double)g.z, (double)g.y + (double)g.w);
+}
+// rounded to a single FP32 complex
+__device__ __forceinline__ float2 dg_f2(float4 g) { return make_float2(__fadd_rn(g.x, g.z), __fadd_rn(g.y, g.w)); }
+// (hi, lo) += a, a an FP32 value (two-sum, then renormalise)
+__device__ __forceinline__ void df_accf(float& hi, float& lo, float a) {
+  df s = two_sum(hi, a);
+  s.lo = __fadd_rn(s.lo, lo);
+  s = quick_two_sum(s.hi, s.lo);
+  hi = s.hi;
+  lo = s.lo;
+}
+__device__ __forceinline__ float4 dg_addf(float4 g, float2 a) {
+  df_accf(g.x, g.z, a.x);
+  df_accf(g.y, g.w, a.y);
+  return g;
+}
+__device__ __forceinline__ float4 dg_from_dfc(dfc a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
+__device__ __forceinline__ dfc dfc_from_dg(float4 g) { return dfc{df{g.x, g.z}, df{g.y, g.w}}; }

@@ -283,11 +283,12 @@ static int record_width(const pqmc_chain* c) { return PQMC_N_SCALAR + 2 * PQMC_N
 
 // the slice loop of Main_PQMC.f90:99-154 for one value of `loop`
 static int sweep_one(pqmc_chain* c, int loop, int warmup, int meas_interval, int meas_number, double* records,
-                     int cap, int* nrec) {
+                     int cap, int* nrec, int tc_first = 1, int tc_last = 0) {
   const bool forward = (loop % 2) == 0;   // the first loop (loop=1) runs backward (:85)
   const int half = c->ntime / 2;
   const int W = record_width(c);
-  for (int tc = 1; tc <= c->ntime; ++tc) {
+  if (tc_last <= 0) tc_last = c->ntime;
+  for (int tc = tc_first; tc <= tc_last; ++tc) {
     int time;
     if (!forward) {
       time = c->ntime - tc + 1;
@@ -414,6 +415,20 @@ int pqmc_sweep(pqmc_chain* c, int first_loop, int n_sweeps, int warmup, int meas
     PQMC_TRY(sweep_one(c, loop, warmup, meas_interval, meas_number, records, n_records_cap, &nrec));
   PQMC_CUDA(cudaStreamSynchronize(c->stream));
   if (n_records) *n_records = nrec;
+  return PQMC_OK;
+}
+
+int pqmc_sweep_slices(pqmc_chain* c, int loop, int first_tc, int n_slices) {
+  if (!c) { set_error("null chain"); return PQMC_ERR_ARG; }
+  if (!c->have_g) { set_error("sweep before init_g"); return PQMC_ERR_STATE; }
+  if (first_tc < 1 || n_slices < 0 || first_tc + n_slices - 1 > c->ntime) {
+    set_error("sweep_slices: slices %d..%d outside 1..%d", first_tc, first_tc + n_slices - 1, c->ntime);
+    return PQMC_ERR_ARG;
+  }
+  if (n_slices == 0) return PQMC_OK;
+  int nrec = 0;
+  PQMC_TRY(sweep_one(c, loop, 1 << 30, 1, 0, nullptr, 0, &nrec, first_tc, first_tc + n_slices - 1));
+  PQMC_CUDA(cudaStreamSynchronize(c->stream));
   return PQMC_OK;
 }
 

@@ -9,6 +9,7 @@
 // -> G = R (P^H B P)^-1 L.  All products are batched complex GEMMs over the
 // chains.  CholeskyQR gives the Householder Q up to column phases and
 // |diag R| for D; G and Re ln_cw do not depend on those phases.
+#include <cooperative_groups.h>
 #include <string.h>
 #include <vector>
 #include "chain.cuh"
@@ -25,6 +26,7 @@ struct GemmArgs {
   const cplx* B;
   cplx* C;
   int lda, ldb, ldc;
+  int out_df;   // C is written in the double-float float4 form (not accumulated)
 };
 
 template <bool TA, bool TB>
@@ -69,7 +71,9 @@ __global__ void __launch_bounds__(256) k_dfgemm(const GemmArgs* args, int m, int
       int r = row0 + tx + 16 * i, c = col0 + ty + 16 * j;
       if (r < m && c < n) {
         cplx* p = g.C + r + (size_t)g.ldc * c;
-        if (accumulate) {
+        if (g.out_df) {
+          *reinterpret_cast<float4*>(p) = dg_from_dfc(acc[i][j]);
+        } else if (accumulate) {
           dfc v = dfc_add(acc[i][j], dfc_make(*p));
           *p = dfc_to_d(v);
         } else {
@@ -149,17 +153,14 @@ __global__ void __launch_bounds__(512) k_chol_inv(const CholArgs* args, int n, i
       L[i + (size_t)n * j] = dfc{df_mul(v.re, inv), df_mul(v.im, inv)};
     }
     __syncthreads();
-    // trailing update: L(i,k) -= L(i,j) conj(L(k,j)) for j < k <= i
+    // trailing update: L(i,k) -= L(i,j) conj(L(k,j)) for j < k <= i; threads run
+    // down the columns (consecutive rows i) so the accesses coalesce
     const int m = n - j - 1;
-    const long tri = (long)m * (m + 1) / 2;
-    for (long e = threadIdx.x; e < tri; e += blockDim.x) {
-      // map e -> (ii, kk) with kk <= ii, both in [0, m)
-      int ii = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
-      while ((long)(ii + 1) * (ii + 2) / 2 <= e) ++ii;
-      while ((long)ii * (ii + 1) / 2 > e) --ii;
-      int kk = (int)(e - (long)ii * (ii + 1) / 2);
-      int i = j + 1 + ii, k = j + 1 + kk;
-      dfc lij = L[i + (size_t)n * j], lkj = L[k + (size_t)n * j];
+    for (long e = threadIdx.x; e < (long)m * m; e += blockDim.x) {
+      const int ii = (int)(e % m), kk = (int)(e / m);
+      if (ii < kk) continue;
+      const int i = j + 1 + ii, k = j + 1 + kk;
+      const dfc lij = L[i + (size_t)n * j], lkj = L[k + (size_t)n * j];
       L[i + (size_t)n * k] = dfc_sub(L[i + (size_t)n * k], dfc_mul(lij, dfc{lkj.re, df_neg(lkj.im)}));
     }
     __syncthreads();
@@ -170,17 +171,47 @@ __global__ void __launch_bounds__(512) k_chol_inv(const CholArgs* args, int n, i
     if (accumulate_d) a.d[j] = mk(a.d[j].x * v, 0.0);
     else a.d[j] = mk(v, 0.0);
   }
-  // R = L^H (upper) to `rinv`; it is inverted in place by k_gj_inverse
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    int i = e % n, j = e / n;
-    if (i <= j) {
-      dfc v = L[j + (size_t)n * i];
-      a.rinv[i + (size_t)n * j] = mk(df_to_d(v.re), -df_to_d(v.im));
-    } else {
-      a.rinv[i + (size_t)n * j] = mk(0.0);
-    }
-  }
+  // the factor stays in `work`; k_tri_inv forms (L^H)^-1
   if (threadIdx.x == 0 && s_bad) *a.status = 1;
+}
+
+// R^-1 for R = L^H (upper triangular) from the double-float Cholesky factor L
+// (lower, column-major) left in `work`: one warp per column j solves
+// R x = e_j by back substitution, x_i = -(sum_{k=i+1..j} conj(L_ki) x_k) / L_ii,
+// reading column i of L (contiguous).  Written to `rinv` in FP64.
+constexpr int TRI_WARPS = 8;
+__global__ void __launch_bounds__(TRI_WARPS * 32) k_tri_inv(const CholArgs* args, int n) {
+  extern __shared__ __align__(16) unsigned char tri_dyn[];
+  const CholArgs a = args[blockIdx.y];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * TRI_WARPS + warp;
+  if (j >= n) return;
+  dfc* x = reinterpret_cast<dfc*>(tri_dyn) + (size_t)warp * n;
+  const dfc* L = a.work;
+  if (lane == 0) {
+    const df d = L[j + (size_t)n * j].re;
+    x[j] = dfc{df_div(df{1.f, 0.f}, d), {0.f, 0.f}};
+  }
+  __syncwarp();
+  for (int i = j - 1; i >= 0; --i) {
+    const dfc* Li = L + (size_t)n * i;
+    dfc acc = dfc_zero();
+    for (int k = i + 1 + lane; k <= j; k += 32) acc = dfc_add(acc, dfc_mulc(Li[k], x[k]));
+    for (int o = 16; o > 0; o >>= 1) {
+      dfc t;
+      t.re.hi = __shfl_xor_sync(0xffffffffu, acc.re.hi, o);
+      t.re.lo = __shfl_xor_sync(0xffffffffu, acc.re.lo, o);
+      t.im.hi = __shfl_xor_sync(0xffffffffu, acc.im.hi, o);
+      t.im.lo = __shfl_xor_sync(0xffffffffu, acc.im.lo, o);
+      acc = dfc_add(acc, t);
+    }
+    if (lane == 0) {
+      const df d = Li[i].re;   // L_ii, real and positive
+      x[i] = dfc{df_neg(df_div(acc.re, d)), df_neg(df_div(acc.im, d))};
+    }
+    __syncwarp();
+  }
+  for (int i = lane; i < n; i += 32) a.rinv[i + (size_t)n * j] = i <= j ? dfc_to_d(x[i]) : mk(0.0);
 }
 
 // ---------------------------------------------------------------------------
@@ -313,41 +344,306 @@ struct PropArgs {
   const cplx* expkv;
 };
 
-__global__ void k_bprop_df(const PropArgs* args, int t_from, int t_to, int forward) {
-  const PropArgs a = args[blockIdx.y];
-  const DevModel& M = a.M;
-  extern __shared__ dfc colv[];
-  const int ns = M.ns, pd = M.pdim;
-  cplx* x = a.X + (size_t)ns * blockIdx.x;
-  for (int r = threadIdx.x; r < ns; r += blockDim.x) colv[r] = dfc_make(x[r]);
+// expKV of the nt slices of one propagation converted once to double-float,
+// in application order and already transposed-conjugated for the backward
+// direction: ekv[((it * n_pf + f) * max_pla + p) * 16 + r + 4 k] = M(r, k)
+// with M = expKV (forward) or expKV^H (backward).
+__global__ void k_ekv_df(const PropArgs* args, dfc* ekv_all, size_t stride, int t_from, int nt, int forward) {
+  __shared__ PropArgs sa;
+  if (threadIdx.x == 0) sa = args[blockIdx.y];
   __syncthreads();
-  const int nt = forward ? (t_to - t_from + 1) : (t_from - t_to + 1);
-  for (int it = 0; it < nt; ++it) {
+  const DevModel& M = sa.M;
+  dfc* out = ekv_all + stride * blockIdx.y;
+  const long total = (long)nt * M.n_pf * M.max_pla * 16;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int k16 = (int)(e % 16);
+    long rest = e / 16;
+    const int p = (int)(rest % M.max_pla);
+    rest /= M.max_pla;
+    const int f = (int)(rest % M.n_pf);
+    const int it = (int)(rest / M.n_pf);
+    const int pf = forward ? f : M.n_pf - 1 - f;
     const int t = (forward ? t_from + it : t_from - it) - 1;
-    for (int f = 0; f < M.n_pf; ++f) {
-      const int pf = forward ? f : M.n_pf - 1 - f;
-      const int dim = M.pf_dim[pf], npla = M.pf_npla[pf];
-      for (int p = threadIdx.x; p < npla; p += blockDim.x) {
-        int S[4];
-        dfc v[4];
-        for (int k = 0; k < dim; ++k) {
-          S[k] = M.site[k + pd * (p + M.max_pla * pf)];
-          v[k] = colv[S[k]];
+    const int dim = M.pf_dim[pf], r = k16 % 4, k = k16 / 4;
+    dfc v = dfc_zero();
+    if (p < M.pf_npla[pf] && r < dim && k < dim) {
+      const cplx* E = sa.expkv + M.kv_base(p, pf, t);
+      v = dfc_make(forward ? E[r + M.pdim * k] : cconj(E[k + M.pdim * r]));
+    }
+    out[e] = v;
+  }
+}
+
+// One-way propagation of PROP_NC columns of X through nt slices (all
+// families, application order) in double-float, the columns held in shared
+// memory.  Work items are (plaquette, column group): the plaquette's matrix
+// stays in registers across the group's columns.
+constexpr int PROP_NC = 8, PROP_NCG = 2;
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bprop_df(const PropArgs* args, const dfc* ekv_all, size_t stride, int n,
+                                                  int nt, int forward) {
+  __shared__ PropArgs sa;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  if (threadIdx.x == 0) sa = args[blockIdx.y];
+  __syncthreads();
+  const DevModel& M = sa.M;
+  const int ns = M.ns, pd = M.pdim, npf = M.n_pf, mp = M.max_pla;
+  dfc* col = reinterpret_cast<dfc*>(dyn);                               // [PROP_NC][ns]
+  int* s_site = reinterpret_cast<int*>(col + (size_t)PROP_NC * ns);     // [n_pf][max_pla][4]
+  const int c0 = blockIdx.x * PROP_NC, ncol = min(PROP_NC, n - c0);
+  cplx* X = sa.X + (size_t)ns * c0;
+  for (int e = threadIdx.x; e < ncol * ns; e += blockDim.x) col[e] = dfc_make(X[e]);
+  for (int e = threadIdx.x; e < npf * mp * 4; e += blockDim.x) {
+    const int k = e % 4, p = (e / 4) % mp, pf = e / (4 * mp);
+    s_site[e] = (p < M.pf_npla[pf] && k < M.pf_dim[pf]) ? M.site[k + pd * (p + mp * pf)] : 0;
+  }
+  __syncthreads();
+  const dfc* ekv = ekv_all + stride * blockIdx.y;
+  constexpr int CPG = PROP_NC / PROP_NCG;
+  for (int it = 0; it < nt; ++it) {
+    for (int f = 0; f < npf; ++f) {
+      const int pf = forward ? f : npf - 1 - f;
+      const int npla = M.pf_npla[pf], dim = M.pf_dim[pf];
+      const dfc* Ef = ekv + ((size_t)it * npf + f) * mp * 16;
+      for (int item = threadIdx.x; item < npla * PROP_NCG; item += blockDim.x) {
+        const int p = item % npla, cg = item / npla;
+        dfc e[DIM][DIM];
+        int S[DIM];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) {
+          S[r] = s_site[(pf * mp + p) * 4 + r];
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) e[r][k] = Ef[(size_t)p * 16 + r + 4 * k];
         }
-        const cplx* E = a.expkv + M.kv_base(p, pf, t);
-        for (int r = 0; r < dim; ++r) {
-          dfc s = dfc_zero();
-          for (int k = 0; k < dim; ++k) {
-            cplx e = forward ? E[r + pd * k] : cconj(E[k + pd * r]);
-            s = dfc_add(s, dfc_mul(dfc_make(e), v[k]));
+#pragma unroll
+        for (int j = 0; j < CPG; ++j) {
+          const int c = cg * CPG + j;
+          if (c >= ncol) break;
+          dfc* x = col + (size_t)c * ns;
+          dfc v[DIM];
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) v[k] = k < dim ? x[S[k]] : dfc_zero();
+#pragma unroll
+          for (int r = 0; r < DIM; ++r) {
+            if (r >= dim) break;
+            dfc acc = dfc_mul(e[r][0], v[0]);
+#pragma unroll
+            for (int k = 1; k < DIM; ++k) acc = dfc_add(acc, dfc_mul(e[r][k], v[k]));
+            x[S[r]] = acc;
           }
-          colv[S[r]] = s;
         }
       }
       __syncthreads();
     }
   }
-  for (int r = threadIdx.x; r < ns; r += blockDim.x) x[r] = dfc_to_d(colv[r]);
+  for (int e = threadIdx.x; e < ncol * ns; e += blockDim.x) X[e] = dfc_to_d(col[e]);
+}
+
+__host__ __forceinline__ size_t prop_smem(int ns, int n_pf, int max_pla) {
+  return sizeof(dfc) * (size_t)PROP_NC * ns + sizeof(int) * 4 * (size_t)n_pf * max_pla;
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Jordan inverse with partial pivoting in double-float on a cluster of
+// GJ_CL thread blocks per matrix: each block keeps a slab of columns in its
+// shared memory; at pivot step k the block owning column k picks the pivot,
+// and writes the pivot row index, 1/pivot and the multiplier column into
+// every block of the cluster through distributed shared memory.  Same
+// result layout as k_gj_inverse (inverse in place in M, log det, pivots).
+constexpr int GJ_CL = 4;
+constexpr int GJ_MAXN = 512;
+namespace cgx = cooperative_groups;
+
+__global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_gj_cluster(const GJArgs* args, int n) {
+  cgx::cluster_group cl = cgx::this_cluster();
+  extern __shared__ __align__(16) unsigned char gj_dyn[];
+  __shared__ dfc s_f[GJ_MAXN];   // multipliers of the current step (written by the owner block)
+  __shared__ int s_perm[GJ_MAXN];
+  __shared__ int s_p;
+  __shared__ dfc s_rec;
+  __shared__ float s_bv[256];
+  __shared__ int s_bi[256];
+  const int rank = (int)cl.block_rank();
+  const GJArgs a = args[blockIdx.x / GJ_CL];
+  const int w = (n + GJ_CL - 1) / GJ_CL, c_lo = rank * w, c_hi = min(n, c_lo + w), nc = max(0, c_hi - c_lo);
+  dfc* A = reinterpret_cast<dfc*>(gj_dyn);   // [nc][n] local slab, A[i + n*(j - c_lo)]
+  const int tid = threadIdx.x;
+  for (int e = tid; e < nc * n; e += blockDim.x) A[e] = dfc_make(a.M[(size_t)c_lo * n + e]);
+  cl.sync();
+  int nswap = 0;
+  for (int k = 0; k < n; ++k) {
+    const int owner = k / w;
+    if (rank == owner) {
+      const dfc* col = A + (size_t)n * (k - c_lo);
+      float best = -1.f;
+      int bi = k;
+      for (int i = k + tid; i < n; i += blockDim.x) {
+        const float m = fabsf(col[i].re.hi) + fabsf(col[i].im.hi);
+        if (m > best) { best = m; bi = i; }
+      }
+      s_bv[tid] = best;
+      s_bi[tid] = bi;
+      __syncthreads();
+      for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (tid < st) {
+          const float ov = s_bv[tid + st];
+          const int oi = s_bi[tid + st];
+          if (ov > s_bv[tid] || (ov == s_bv[tid] && oi < s_bi[tid])) { s_bv[tid] = ov; s_bi[tid] = oi; }
+        }
+        __syncthreads();
+      }
+      const int p = s_bi[0];
+      const dfc pv = col[p];
+      df nrm = df_add(df_mul(pv.re, pv.re), df_mul(pv.im, pv.im));
+      if (tid == 0) {
+        if (nrm.hi == 0.0f) *a.status = 1;
+        a.piv[k] = dfc_to_d(pv);
+      }
+      const df inv = df_div(df{1.f, 0.f}, nrm.hi == 0.0f ? df{1.f, 0.f} : nrm);
+      const dfc rec = dfc{df_mul(pv.re, inv), df_neg(df_mul(pv.im, inv))};
+      // multipliers f_i = A(sigma(i), k) with rows k and p exchanged
+      for (int r = 0; r < GJ_CL; ++r) {
+        dfc* rf = cl.map_shared_rank(s_f, r);
+        for (int i = tid; i < n; i += blockDim.x) {
+          const int src = (i == k) ? p : ((i == p) ? k : i);
+          rf[i] = col[src];
+        }
+        if (tid == 0) {
+          *cl.map_shared_rank(&s_p, r) = p;
+          *cl.map_shared_rank(&s_rec, r) = rec;
+        }
+      }
+    }
+    cl.sync();
+    const int p = s_p;
+    const dfc rec = s_rec;
+    if (tid == 0) s_perm[k] = p;
+    if (p != k) ++nswap;
+    // exchange rows k and p, scale row k, eliminate, in this block's columns
+    for (int jl = tid; jl < nc; jl += blockDim.x) {
+      dfc* cj = A + (size_t)n * jl;
+      if (p != k) {
+        const dfc t = cj[k];
+        cj[k] = cj[p];
+        cj[p] = t;
+      }
+      cj[k] = (c_lo + jl == k) ? rec : dfc_mul(cj[k], rec);
+    }
+    __syncthreads();
+    for (long e = tid; e < (long)nc * n; e += blockDim.x) {
+      const int i = (int)(e % n), jl = (int)(e / n);
+      if (i == k) continue;
+      dfc* cj = A + (size_t)n * jl;
+      const dfc f = s_f[i];
+      if (c_lo + jl == k) cj[i] = dfc_sub(dfc_zero(), dfc_mul(f, rec));
+      else cj[i] = dfc_sub(cj[i], dfc_mul(f, cj[k]));
+    }
+    cl.sync();   // s_f, s_p, s_rec are rewritten by the next step's owner
+  }
+  // undo the row exchanges as column exchanges: computed column c ends at pos(c)
+  __shared__ int s_at[GJ_MAXN];
+  if (tid == 0) {
+    for (int q = 0; q < n; ++q) s_at[q] = q;
+    for (int k = n - 1; k >= 0; --k) {
+      const int p = s_perm[k];
+      const int t = s_at[k];
+      s_at[k] = s_at[p];
+      s_at[p] = t;
+    }
+  }
+  __syncthreads();
+  // s_at[q] = computed column found at final position q; write this block's columns there
+  for (int q = 0; q < n; ++q) {
+    const int c = s_at[q];
+    if (c < c_lo || c >= c_hi) continue;
+    const dfc* cj = A + (size_t)n * (c - c_lo);
+    for (int i = tid; i < n; i += blockDim.x) a.M[(size_t)q * n + i] = dfc_to_d(cj[i]);
+  }
+  if (rank == 0) {
+    // log det = sum log(piv) + i pi (odd number of exchanges)
+    __shared__ double rre[256], rim[256];
+    double sr = 0.0, sim = 0.0;
+    for (int i = tid; i < n; i += blockDim.x) {
+      const cplx l = clog_(a.piv[i]);
+      sr += l.x;
+      sim += l.y;
+    }
+    rre[tid] = sr;
+    rim[tid] = sim;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if (tid < st) {
+        rre[tid] += rre[tid + st];
+        rim[tid] += rim[tid + st];
+      }
+      __syncthreads();
+    }
+    if (tid == 0) *a.logdet = mk(rre[0], rim[0] + ((nswap & 1) ? 3.14159265358979323846 : 0.0));
+  }
+}
+
+// Cholesky W = L L^H in double-float on a cluster of GJ_CL blocks, a slab
+// of columns of W per block in shared memory (right-looking: the block
+// owning column j forms it and writes it to every block of the cluster, each
+// block updates its own trailing columns).  The factor goes to `work` for
+// k_tri_inv and d_j = L_jj to `d` (multiplied in when accumulate_d).
+__global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_chol_cluster(const CholArgs* args, int n,
+                                                                                      int accumulate_d) {
+  cgx::cluster_group cl = cgx::this_cluster();
+  extern __shared__ __align__(16) unsigned char ch_dyn[];
+  __shared__ dfc s_f[GJ_MAXN];   // column j of L (written by the owner block)
+  __shared__ int s_bad;
+  __shared__ df s_l;
+  const int rank = (int)cl.block_rank();
+  const CholArgs a = args[blockIdx.x / GJ_CL];
+  const int w = (n + GJ_CL - 1) / GJ_CL, c_lo = rank * w, c_hi = min(n, c_lo + w), nc = max(0, c_hi - c_lo);
+  dfc* A = reinterpret_cast<dfc*>(ch_dyn);   // [nc][n]
+  const int tid = threadIdx.x;
+  for (int e = tid; e < nc * n; e += blockDim.x) A[e] = dfc_make(a.W[(size_t)c_lo * n + e]);
+  if (tid == 0) s_bad = 0;
+  cl.sync();
+  for (int j = 0; j < n; ++j) {
+    const int owner = j / w;
+    if (rank == owner) {
+      dfc* col = A + (size_t)n * (j - c_lo);
+      if (tid == 0) {
+        df ajj = col[j].re;
+        if (!(ajj.hi > 0.0f)) {
+          s_bad = 1;
+          ajj = df{1.0f, 0.0f};
+        }
+        s_l = df_sqrt(ajj);
+        col[j] = dfc{s_l, {0.f, 0.f}};
+      }
+      __syncthreads();
+      const df inv = df_div(df{1.0f, 0.0f}, s_l);
+      for (int i = j + 1 + tid; i < n; i += blockDim.x) col[i] = dfc{df_mul(col[i].re, inv), df_mul(col[i].im, inv)};
+      __syncthreads();
+      for (int r = 0; r < GJ_CL; ++r) {
+        dfc* rf = cl.map_shared_rank(s_f, r);
+        for (int i = j + 1 + tid; i < n; i += blockDim.x) rf[i] = col[i];
+      }
+    }
+    cl.sync();
+    // L(i,k) -= L(i,j) conj(L(k,j)) for j < k <= i, k in this block's columns
+    const int k0 = max(c_lo, j + 1);
+    for (long e = tid; e < (long)(c_hi - k0) * n; e += blockDim.x) {
+      const int i = (int)(e % n), k = k0 + (int)(e / n);
+      if (i < k) continue;
+      const dfc lkj = s_f[k];
+      dfc* cell = A + (size_t)n * (k - c_lo) + i;
+      *cell = dfc_sub(*cell, dfc_mul(s_f[i], dfc{lkj.re, df_neg(lkj.im)}));
+    }
+    cl.sync();
+  }
+  for (int jl = tid; jl < nc; jl += blockDim.x) {
+    const int j = c_lo + jl;
+    const double v = df_to_d(A[(size_t)n * jl + j].re);
+    a.d[j] = accumulate_d ? mk(a.d[j].x * v, 0.0) : mk(v, 0.0);
+  }
+  for (int e = tid; e < nc * n; e += blockDim.x) a.work[(size_t)c_lo * n + e] = A[e];
+  if (tid == 0 && s_bad) *a.status = 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -362,28 +658,56 @@ struct WeightArgs {
   const cplx* gold;
   const cplx* gnew;
   int tr_weight, ncopy;
+  int gdf;   // gold and gnew are in the double-float float4 form
 };
 
 __global__ void k_bweight(const WeightArgs* args, int ndcount, long ng, int compare) {
   const WeightArgs a = args[blockIdx.x];
-  __shared__ double rre[256], rim[256], rmx[256];
-  double sr = 0.0, sim = 0.0, mx = 0.0;
+  __shared__ double rre[256], rim[256], rmx[256], rdf[256], rgn[256];
+  double sr = 0.0, sim = 0.0, mx = 0.0, df = 0.0, gn = 0.0;
   for (int i = threadIdx.x; i < ndcount; i += blockDim.x) {
     cplx l = clog_(a.d_block[i]);
     sr += l.x;
     sim += l.y;
   }
-  if (compare)
-    for (long e = threadIdx.x; e < ng; e += blockDim.x) mx = fmax(mx, cabsd(csub(a.gold[e], a.gnew[e])));
+  if (compare && a.gdf) {
+    // differences of double-float values in FP32: hi and lo parts separately
+    const float4* go = reinterpret_cast<const float4*>(a.gold);
+    const float4* gw = reinterpret_cast<const float4*>(a.gnew);
+    float mxf = 0.f, dff = 0.f, gnf = 0.f;
+    for (long e = threadIdx.x; e < ng; e += blockDim.x) {
+      const float4 o = go[e], w = gw[e];
+      const float dr = (o.x - w.x) + (o.z - w.z), di = (o.y - w.y) + (o.w - w.w);
+      const float nr = w.x + w.z, ni = w.y + w.w;
+      const float d2 = dr * dr + di * di;
+      mxf = fmaxf(mxf, d2);
+      dff += d2;
+      gnf += nr * nr + ni * ni;
+    }
+    mx = sqrt((double)mxf);
+    df = dff;
+    gn = gnf;
+  } else if (compare) {
+    for (long e = threadIdx.x; e < ng; e += blockDim.x) {
+      const cplx gnew = a.gnew[e], dg = csub(a.gold[e], gnew);
+      mx = fmax(mx, cabsd(dg));
+      df += cabs2(dg);
+      gn += cabs2(gnew);
+    }
+  }
   rre[threadIdx.x] = sr;
   rim[threadIdx.x] = sim;
   rmx[threadIdx.x] = mx;
+  rdf[threadIdx.x] = df;
+  rgn[threadIdx.x] = gn;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
       rre[threadIdx.x] += rre[threadIdx.x + s];
       rim[threadIdx.x] += rim[threadIdx.x + s];
       rmx[threadIdx.x] = fmax(rmx[threadIdx.x], rmx[threadIdx.x + s]);
+      rdf[threadIdx.x] += rdf[threadIdx.x + s];
+      rgn[threadIdx.x] += rgn[threadIdx.x + s];
     }
     __syncthreads();
   }
@@ -399,6 +723,9 @@ __global__ void k_bweight(const WeightArgs* args, int ndcount, long ng, int comp
     if (compare) {
       double ew = fabs(nw.x - a.sc->ln_cw.x);
       a.sc->err_g = rmx[0];
+      const double rel = rgn[0] > 0.0 ? sqrt(rdf[0] / rgn[0]) : 0.0;
+      a.sc->err_g_rel = rel;
+      if (rel > a.sc->err_g_rel_max) a.sc->err_g_rel_max = rel;
       a.sc->err_w = ew;
       a.sc->err_fast = ew;
       double m = fmax(rmx[0], ew);
@@ -411,7 +738,7 @@ __global__ void k_bweight(const WeightArgs* args, int ndcount, long ng, int comp
 // ---------------------------------------------------------------------------
 BatchRecompute::~BatchRecompute() {
   void* ps[] = {d_gemm, d_chol, d_gj, d_prop, d_weight, work_df, tmpX, gram, rinv, pbp, wmat, logdet, piv, perm,
-                status};
+                status, ekv_df};
   for (void* p : ps)
     if (p) cudaFree(p);
 }
@@ -443,6 +770,36 @@ int BatchRecompute::setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s
   PQMC_TRY(al((void**)&perm, sizeof(int) * (size_t)C * ne));
   PQMC_TRY(al((void**)&status, sizeof(int) * C));
   PQMC_CUDA(cudaMemset(status, 0, sizeof(int) * C));
+  ekv_slices = c0->ngroup;
+  ekv_stride = (size_t)ekv_slices * c0->n_pf * c0->max_pla * 16;
+  PQMC_TRY(al((void**)&ekv_df, sizeof(dfc) * ekv_stride * C));
+  {
+    const size_t smem = prop_smem(ns, c0->n_pf, c0->max_pla);
+    int dev = 0, optin = 0;
+    PQMC_CUDA(cudaGetDevice(&dev));
+    PQMC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (smem + 1024 > (size_t)optin) {
+      set_error("batch recompute: %zu bytes of shared memory needed for the propagation", smem);
+      return PQMC_ERR_ARG;
+    }
+    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t tsm = sizeof(dfc) * TRI_WARPS * (size_t)ne;
+    if (tsm + 1024 > (size_t)optin) {
+      set_error("batch recompute: nelec %d too large for the triangular inverse", ne);
+      return PQMC_ERR_ARG;
+    }
+    PQMC_CUDA(cudaFuncSetAttribute(k_tri_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    // the cluster Gauss-Jordan needs a quarter of the matrix per block in shared memory
+    const size_t gsm = sizeof(dfc) * (size_t)((ne + GJ_CL - 1) / GJ_CL) * ne;
+    gj_cluster = ne <= GJ_MAXN && gsm + 20480 <= (size_t)optin;
+    if (gj_cluster) {
+      PQMC_CUDA(cudaFuncSetAttribute(k_gj_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
+      PQMC_CUDA(cudaFuncSetAttribute(k_chol_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
+    }
+  }
   return PQMC_OK;
 }
 
@@ -466,17 +823,16 @@ int BatchRecompute::cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*
       ca[i] = CholArgs{gram + (size_t)i * ne * ne, work_df + (size_t)i * ne * ne, rinv + (size_t)i * ne * ne, D[i],
                        status + i};
     PQMC_CUDA(cudaMemcpyAsync(d_chol, ca.data(), sizeof(CholArgs) * C, cudaMemcpyHostToDevice, stream));
-    k_chol_inv<<<C, 512, 0, stream>>>(d_chol, ne, pass);
-    PQMC_LAUNCHED();
-    {
-      std::vector<GJArgs> gj(C);
-      for (int i = 0; i < C; ++i)
-        gj[i] = GJArgs{rinv + (size_t)i * ne * ne, work_df + (size_t)i * ne * ne, logdet + i, piv + (size_t)i * ne,
-                       perm + (size_t)i * ne, status + i};
-      PQMC_CUDA(cudaMemcpyAsync(d_gj + C, gj.data(), sizeof(GJArgs) * C, cudaMemcpyHostToDevice, stream));
-      k_gj_inverse<<<C, 512, 0, stream>>>(d_gj + C, ne);
-      PQMC_LAUNCHED();
+    if (gj_cluster) {
+      const int w = (ne + GJ_CL - 1) / GJ_CL;
+      k_chol_cluster<<<C * GJ_CL, 256, sizeof(dfc) * (size_t)w * ne, stream>>>(d_chol, ne, pass);
+    } else {
+      k_chol_inv<<<C, 512, 0, stream>>>(d_chol, ne, pass);
     }
+    PQMC_LAUNCHED();
+    k_tri_inv<<<dim3((ne + TRI_WARPS - 1) / TRI_WARPS, C), TRI_WARPS * 32, sizeof(dfc) * TRI_WARPS * ne, stream>>>(
+        d_chol, ne);
+    PQMC_LAUNCHED();
     for (int i = 0; i < C; ++i) ga[i] = GemmArgs{X[i], rinv + (size_t)i * ne * ne, tmpX + (size_t)i * ns * ne, ns, ne, ns};
     PQMC_TRY(gemm('N', 'N', ns, ne, ne, ga, 1, 0));
     for (int i = 0; i < C; ++i)
@@ -488,7 +844,8 @@ int BatchRecompute::cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*
 
 // G = R (L R)^-1 L with L = XL^H; ln_cw; errors (cal_g_and_det_T0)
 int BatchRecompute::g_and_det(const std::vector<cplx*>& XL, const std::vector<cplx*>& R,
-                              const std::vector<cplx*>& Gcur, const std::vector<cplx*>& Gnew, bool compare, int blk1) {
+                              const std::vector<cplx*>& Gcur, const std::vector<cplx*>& Gnew, bool compare, int blk1,
+                              bool g_df) {
   std::vector<GemmArgs> ga(C);
   for (int i = 0; i < C; ++i) ga[i] = GemmArgs{XL[i], R[i], pbp + (size_t)i * ne * ne, ns, ns, ne};
   PQMC_TRY(gemm('C', 'N', ne, ne, ns, ga, 2, 0));
@@ -497,16 +854,21 @@ int BatchRecompute::g_and_det(const std::vector<cplx*>& XL, const std::vector<cp
     gj[i] = GJArgs{pbp + (size_t)i * ne * ne, work_df + (size_t)i * ne * ne, logdet + i, piv + (size_t)i * ne,
                    perm + (size_t)i * ne, status + i};
   PQMC_CUDA(cudaMemcpyAsync(d_gj, gj.data(), sizeof(GJArgs) * C, cudaMemcpyHostToDevice, stream));
-  k_gj_inverse<<<C, 512, 0, stream>>>(d_gj, ne);
+  if (gj_cluster) {
+    const int w = (ne + GJ_CL - 1) / GJ_CL;
+    k_gj_cluster<<<C * GJ_CL, 256, sizeof(dfc) * (size_t)w * ne, stream>>>(d_gj, ne);
+  } else {
+    k_gj_inverse<<<C, 512, 0, stream>>>(d_gj, ne);
+  }
   PQMC_LAUNCHED();
   for (int i = 0; i < C; ++i) ga[i] = GemmArgs{R[i], pbp + (size_t)i * ne * ne, wmat + (size_t)i * ns * ne, ns, ne, ns};
   PQMC_TRY(gemm('N', 'N', ns, ne, ne, ga, 3, 0));
-  for (int i = 0; i < C; ++i) ga[i] = GemmArgs{wmat + (size_t)i * ns * ne, XL[i], Gnew[i], ns, ns, ns};
+  for (int i = 0; i < C; ++i) ga[i] = GemmArgs{wmat + (size_t)i * ns * ne, XL[i], Gnew[i], ns, ns, ns, g_df ? 1 : 0};
   PQMC_TRY(gemm('N', 'C', ns, ns, ne, ga, 4, 0));
   std::vector<WeightArgs> wa(C);
   for (int i = 0; i < C; ++i)
     wa[i] = WeightArgs{cs[i]->sc, dblk(cs[i], blk1), cs[i]->d_logsum, blk1 - 1, cs[i]->nblock, logdet + i, Gcur[i],
-                       Gnew[i], cs[i]->M.tr_weight, cs[i]->M.ncopy};
+                       Gnew[i], cs[i]->M.tr_weight, cs[i]->M.ncopy, g_df ? 1 : 0};
   PQMC_CUDA(cudaMemcpyAsync(d_weight, wa.data(), sizeof(WeightArgs) * C, cudaMemcpyHostToDevice, stream));
   k_bweight<<<C, 256, 0, stream>>>(d_weight, ne, (long)ns * ns, compare ? 1 : 0);
   PQMC_LAUNCHED();
@@ -514,12 +876,75 @@ int BatchRecompute::g_and_det(const std::vector<cplx*>& XL, const std::vector<cp
 }
 
 int BatchRecompute::propagate(const std::vector<cplx*>& X, int t_from, int t_to, bool forward) {
+  const int nt = forward ? (t_to - t_from + 1) : (t_from - t_to + 1);
+  if (nt < 1 || nt > ekv_slices) { set_error("batch propagate: %d slices (at most %d)", nt, ekv_slices); return PQMC_ERR_ARG; }
   std::vector<PropArgs> pa(C);
   for (int i = 0; i < C; ++i) pa[i] = PropArgs{cs[i]->M, X[i], cs[i]->expkv};
   PQMC_CUDA(cudaMemcpyAsync(d_prop, pa.data(), sizeof(PropArgs) * C, cudaMemcpyHostToDevice, stream));
-  dim3 grid(ne, C);
-  k_bprop_df<<<grid, 128, sizeof(dfc) * ns, stream>>>(d_prop, t_from, t_to, forward ? 1 : 0);
+  pqmc_chain* c0 = cs[0];
+  const long total = (long)nt * c0->n_pf * c0->max_pla * 16;
+  k_ekv_df<<<dim3((unsigned)std::min<long>((total + 255) / 256, 1024), C), 256, 0, stream>>>(d_prop, ekv_df, ekv_stride,
+                                                                                         t_from, nt, forward ? 1 : 0);
   PQMC_LAUNCHED();
+  int maxdim = 1;
+  for (int f = 0; f < c0->n_pf; ++f) maxdim = std::max(maxdim, c0->h_pf_dim[f]);
+  const dim3 grid((ne + PROP_NC - 1) / PROP_NC, C);
+  const size_t smem = prop_smem(ns, c0->n_pf, c0->max_pla);
+  const int fw = forward ? 1 : 0;
+  switch (maxdim) {
+    case 1: k_bprop_df<1><<<grid, 256, smem, stream>>>(d_prop, ekv_df, ekv_stride, ne, nt, fw); break;
+    case 2: k_bprop_df<2><<<grid, 256, smem, stream>>>(d_prop, ekv_df, ekv_stride, ne, nt, fw); break;
+    case 3: k_bprop_df<3><<<grid, 256, smem, stream>>>(d_prop, ekv_df, ekv_stride, ne, nt, fw); break;
+    default: k_bprop_df<4><<<grid, 256, smem, stream>>>(d_prop, ekv_df, ekv_stride, ne, nt, fw); break;
+  }
+  PQMC_LAUNCHED();
+  return PQMC_OK;
+}
+
+// init_g_T0(1) (src/mod_evolution.f90:46-111) for every chain: the right
+// string Q(2..nblock-1) from the Slater matrix upward, one block of ngroup
+// slices and one CholeskyQR2 at a time for all chains together, then G at
+// the top slice from L = P^H and R = Q(nblock-1).
+int BatchRecompute::init_g() {
+  pqmc_chain* c0 = cs[0];
+  const int ng = c0->ngroup, nb = c0->nblock;
+  if (c0->ntime % ng != 0) { set_error("batch init_g: ntime %% ngroup != 0"); return PQMC_ERR_ARG; }
+  const size_t qb = sizeof(cplx) * (size_t)ns * ne;
+  std::vector<cplx*> X(C), D(C), XL(C), Gc(C), Gn(C);
+  for (int i = 0; i < C; ++i) {
+    pqmc_chain* c = cs[i];
+    PQMC_CUDA(cudaMemcpyAsync(qblk(c, 1), c->slater_q, qb, cudaMemcpyDeviceToDevice, stream));
+    PQMC_CUDA(cudaMemcpyAsync(qblk(c, nb), c->slater_q, qb, cudaMemcpyDeviceToDevice, stream));
+    PQMC_CUDA(cudaMemcpyAsync(dblk(c, 1), c->slater_d, sizeof(cplx) * ne, cudaMemcpyDeviceToDevice, stream));
+    PQMC_CUDA(cudaMemcpyAsync(dblk(c, nb), c->slater_d, sizeof(cplx) * ne, cudaMemcpyDeviceToDevice, stream));
+    X[i] = c->rmat;
+    PQMC_CUDA(cudaMemcpyAsync(X[i], c->slater_q, qb, cudaMemcpyDeviceToDevice, stream));
+  }
+  for (int blk = 2; blk <= nb - 1; ++blk) {
+    PQMC_TRY(propagate(X, (blk - 2) * ng + 1, (blk - 1) * ng, true));
+    for (int i = 0; i < C; ++i) D[i] = dblk(cs[i], blk);
+    PQMC_TRY(cholqr2(X, D));
+    for (int i = 0; i < C; ++i)
+      PQMC_CUDA(cudaMemcpyAsync(qblk(cs[i], blk), X[i], qb, cudaMemcpyDeviceToDevice, stream));
+  }
+  // per-block sums of log D on each chain's own stream, after the strings
+  PQMC_CUDA(cudaStreamSynchronize(stream));
+  for (auto* c : cs) {
+    for (int b = 1; b <= nb; ++b) PQMC_TRY(block_log(c, b));
+    PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  for (int i = 0; i < C; ++i) {
+    XL[i] = qblk(cs[i], nb);
+    Gc[i] = cs[i]->g;
+    Gn[i] = cs[i]->g_alt;
+  }
+  PQMC_TRY(g_and_det(XL, X, Gc, Gn, false, nb, false));
+  for (auto* c : cs) {
+    cplx* t = c->g;
+    c->g = c->g_alt;
+    c->g_alt = t;
+  }
+  PQMC_CUDA(cudaStreamSynchronize(stream));
   return PQMC_OK;
 }
 
@@ -570,7 +995,7 @@ int BatchRecompute::scratch(int time, bool forward) {
     Gc[i] = cs[i]->g;
     Gn[i] = cs[i]->g_alt;
   }
-  PQMC_TRY(g_and_det(XL, R, Gc, Gn, true, blk));
+  PQMC_TRY(g_and_det(XL, R, Gc, Gn, true, blk, true));   // the mixed sweep keeps G in double-float form
   for (auto* c : cs) {
     cplx* t = c->g;
     c->g = c->g_alt;

@@ -31,14 +31,19 @@ struct BatchRecompute {
   cplx* piv = nullptr;
   int* perm = nullptr;
   int* status = nullptr;
+  ::dfc* ekv_df = nullptr;   // expKV of one block of slices in double-float, per chain
+  size_t ekv_stride = 0;
+  int ekv_slices = 0;
+  bool gj_cluster = false;   // (L R)^-1 on a cluster of blocks with the matrix in shared memory
 
   ~BatchRecompute();
   int setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s);
   int gemm(char ta, char tb, int m, int n, int k, const std::vector<GemmArgs>& a, int slot, int accumulate);
   int cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*>& D);
   int g_and_det(const std::vector<cplx*>& XL, const std::vector<cplx*>& R, const std::vector<cplx*>& Gcur,
-                const std::vector<cplx*>& Gnew, bool compare, int blk1);
+                const std::vector<cplx*>& Gnew, bool compare, int blk1, bool g_df);
   int propagate(const std::vector<cplx*>& X, int t_from, int t_to, bool forward);
   int scratch(int time, bool forward);
+  int init_g();   // init_g_T0(1) of every chain (needs ntime % ngroup == 0)
 };
 }  // namespace pqmc

@@ -96,6 +96,20 @@ class PqmcChain:
         self._chk(self.lib.pqmc_get_field(self.h, f.ctypes.data_as(_f64p)), "pqmc_get_field")
         return f
 
+    def set_field_slices(self, first_time: int, block):
+        """boson_field(:, first_time..) from a host (n_bf, n) block; refreshes expKV there."""
+        blk = np.asfortranarray(block, dtype=np.float64)
+        assert blk.shape[0] == self.m.n_bf
+        self._chk(self.lib.pqmc_set_field_slices(self.h, first_time, blk.shape[1], blk.ctypes.data_as(_f64p)),
+                  "pqmc_set_field_slices")
+
+    def get_field_slices(self, first_time: int, n: int, out=None) -> np.ndarray:
+        if out is None:
+            out = np.zeros((self.m.n_bf, n), order="F")
+        self._chk(self.lib.pqmc_get_field_slices(self.h, first_time, n, out.ctypes.data_as(_f64p)),
+                  "pqmc_get_field_slices")
+        return out
+
     def set_rng(self, words):
         w = (ctypes.c_int32 * 5)(*[int(x) for x in words])
         self._chk(self.lib.pqmc_set_rng(self.h, w), "pqmc_set_rng")
@@ -172,6 +186,10 @@ class PqmcChain:
                   "pqmc_logweight_grad")
         return complex(o[0], o[1])
 
+    def sweep_slices(self, loop: int, first_tc: int, n_slices: int):
+        """Slices first_tc .. first_tc+n_slices-1 of sweep `loop` (no measurement)."""
+        self._chk(self.lib.pqmc_sweep_slices(self.h, loop, first_tc, n_slices), "pqmc_sweep_slices")
+
     def take_measurement(self, time: int):
         self._chk(self.lib.pqmc_take_measurement(self.h, time), "take_measurement")
 
@@ -224,12 +242,35 @@ class PqmcBatch:
             self.chains.append(PqmcChain(m, field=f, rng_words=w, meas=meas, handle=ch))
 
     def init(self):
-        for c in self.chains:
-            c.init_expkv()
-            c.init_g(1)
+        """init_expKV + init_g_T0(1) of every chain (batched for mixed batches)."""
+        check(self.lib, self.lib.pqmc_batch_init(self.h), "pqmc_batch_init")
 
     def sweep(self, loop: int):
         check(self.lib, self.lib.pqmc_batch_sweep(self.h, loop), "pqmc_batch_sweep")
+
+    def sweep_slices(self, loop: int, first_tc: int, n_slices: int):
+        """Slices first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain."""
+        check(self.lib, self.lib.pqmc_batch_sweep_slices(self.h, loop, first_tc, n_slices),
+              "pqmc_batch_sweep_slices")
+
+    def stream(self) -> int:
+        """The cudaStream_t (as an integer) the batched kernels run on."""
+        s = ctypes.c_void_p()
+        check(self.lib, self.lib.pqmc_batch_stream(self.h, ctypes.byref(s)), "pqmc_batch_stream")
+        return int(s.value or 0)
+
+    PHASES = ("prep", "scan", "flush", "wrap", "recompute")
+
+    def set_timing(self, enable: bool):
+        check(self.lib, self.lib.pqmc_batch_set_timing(self.h, 1 if enable else 0), "pqmc_batch_set_timing")
+
+    def timing(self) -> dict:
+        """{phase: (total ms, timed launches)} since set_timing(True)."""
+        ms = np.zeros(len(self.PHASES))
+        n = (ctypes.c_longlong * len(self.PHASES))()
+        check(self.lib, self.lib.pqmc_batch_get_timing(self.h, ms.ctypes.data_as(_f64p), n),
+              "pqmc_batch_get_timing")
+        return {p: (float(ms[i]), int(n[i])) for i, p in enumerate(self.PHASES)}
 
     def set_delay(self, depth: int):
         check(self.lib, self.lib.pqmc_batch_set_delay(self.h, depth), "pqmc_batch_set_delay")

@@ -49,5 +49,5 @@ def test_no_cpu_fallback():
 def test_struct_layout_matches_header():
     # pqmc_model: 16 int32 + 5 double + 12 pointers
     assert ctypes.sizeof(abi.PqmcModel) == 16 * 4 + 5 * 8 + 12 * 8
-    assert ctypes.sizeof(abi.PqmcState) == 16 + 8 + 8 + 8 + 8 + 20 + 4
+    assert ctypes.sizeof(abi.PqmcState) == 16 + 8 + 8 + 8 + 8 + 20 + 4 + 8 + 8
     assert abi.N_FIELD == 25 and abi.N_SCALAR == 3

@@ -283,6 +283,10 @@ int pqmc_batch_chain(pqmc_batch* batch, int i, pqmc_chain** chain);
 /* delay depth of the mixed-precision update: panel columns folded into G
  * per tensor-core flush (default 64, at most 512) */
 int pqmc_batch_set_delay(pqmc_batch* batch, int depth);
+/* rank-K flush engine of the mixed batch: 1 (default) = tcgen05 tensor
+ * cores with the accumulator in tensor memory (delay depth <= 64; deeper
+ * delays use 0), 0 = mma.sync split-BF16 tiles */
+int pqmc_batch_set_flush(pqmc_batch* batch, int mode);
 /* one sweep of every chain (Main_PQMC.f90:99-154), no measurement */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
 /* slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain */

@@ -711,15 +711,254 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
     }
     __syncthreads();
   }
+  float4 gv[4][4];
+#pragma unroll
   for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int r = row0 + wm * 16 + g + ((e >> 1) ? 8 : 0);
       const int cc = col0 + wn * 32 + nt * 8 + 2 * tq + (e & 1);
-      if (r < ns && cc < ns) {
-        float4* p = G + r + (size_t)ns * cc;
-        *p = dg_addf(*p, make_float2(acc[nt][0][e], acc[nt][1][e]));
+      if (r < ns && cc < ns) gv[nt][e] = G[r + (size_t)ns * cc];
+    }
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int r = row0 + wm * 16 + g + ((e >> 1) ? 8 : 0);
+      const int cc = col0 + wn * 32 + nt * 8 + 2 * tq + (e & 1);
+      if (r < ns && cc < ns) G[r + (size_t)ns * cc] = dg_addf(gv[nt][e], make_float2(acc[nt][0][e], acc[nt][1][e]));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Rank-K flush on the 5th-generation tensor cores (tcgen05).
+//
+// The complex update G += A B is one real GEMM  D = A' B'^T  with
+//   A' = [Ar | Ai]               (rows of G  x  2K),
+//   B' = [[Br | -Bi]; [Bi | Br]] (64 re columns then 64 im columns x 2K),
+// every FP32 operand split into three BF16 terms (hi, mid, lo) and the six
+// products hi.hi, hi.mid, mid.hi, hi.lo, mid.mid, lo.hi accumulated into one
+// FP32 accumulator in tensor memory (128 lanes x 128 columns per tile).
+//
+// k_bsplit writes the split operands as shared-memory tile images in the
+// no-swizzle K-major core-matrix layout: a core matrix is 8 rows x 16 bytes
+// (8 BF16 along K); core (row group i8, K group j8) sits at
+// j8 * UM_LBO + i8 * 128 bytes (UM_LBO = 16 row groups * 128 B), so the
+// first k columns of a tile image are one contiguous prefix.  Per chain:
+// UM_RT row tiles of A' and UM_CT column tiles of B', three splits each,
+// each image 128 rows x 2*UM_KP BF16 (Ar/Br-part at k < UM_KP, Ai-part at
+// UM_KP + k).
+constexpr int UM_KP = 64;                    // panel columns per flush on this path (delay depth <= 64)
+constexpr int UM_IMG = 128 * 2 * UM_KP * 2;  // bytes per tile image (32 KB)
+constexpr int UM_LBO = 16 * 128;             // bytes between adjacent K core matrices
+
+__host__ __device__ __forceinline__ int um_rtiles(int ns) { return (ns + 127) / 128; }
+__host__ __device__ __forceinline__ int um_ctiles(int ns) { return (ns + 63) / 64; }
+__host__ __device__ __forceinline__ size_t um_chain_bytes(int ns) {
+  return (size_t)3 * (um_rtiles(ns) + um_ctiles(ns)) * UM_IMG;
+}
+__device__ __forceinline__ int um_off(int row, int k) {   // byte offset of (row, k) in a tile image
+  return (k >> 3) * UM_LBO + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+// three-way BF16 split of an FP32 value
+__device__ __forceinline__ void split3b(float x, __nv_bfloat16* o) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(h);
+  const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+  o[0] = h;
+  o[1] = m;
+  o[2] = __float2bfloat16_rn(r1 - __bfloat162float(m));
+}
+
+__global__ void __launch_bounds__(256) k_bsplit(const BDesc* D, unsigned char* img_all) {
+  const BDesc& d = D[blockIdx.y];
+  const int K = *d.kcount;
+  if (K == 0) return;
+  const int ns = d.M.ns, ldp = d.ldp, K16 = (K + 15) & ~15;
+  const int RT = um_rtiles(ns), CT = um_ctiles(ns);
+  unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
+  // work item: (tile t, row in tile, k < K16); A tiles first, then B tiles
+  const long total = (long)(RT + CT) * 128 * K16;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % K16);
+    const int row = (int)((e / K16) % 128);
+    const int t = (int)(e / ((long)K16 * 128));
+    float2 lo_part, hi_part;   // values at k (first half) and UM_KP + k (second half)
+    if (t < RT) {
+      const int r = t * 128 + row;
+      const float2 v = (r < ns && k < K) ? d.A[(size_t)k * ldp + r] : make_float2(0.f, 0.f);
+      lo_part = make_float2(v.x, 0.f);   // Ar
+      hi_part = make_float2(v.y, 0.f);   // Ai
+    } else {
+      const int ct = t - RT, n = row & 63, c = ct * 64 + n;
+      const float2 v = (c < ns && k < K) ? d.B[(size_t)k * ldp + c] : make_float2(0.f, 0.f);
+      if (row < 64) {   // re column: [Br | -Bi]
+        lo_part = make_float2(v.x, 0.f);
+        hi_part = make_float2(-v.y, 0.f);
+      } else {          // im column: [Bi | Br]
+        lo_part = make_float2(v.y, 0.f);
+        hi_part = make_float2(v.x, 0.f);
       }
     }
+    __nv_bfloat16 a3[3], b3[3];
+    split3b(lo_part.x, a3);
+    split3b(hi_part.x, b3);
+    unsigned char* base = img + (size_t)t * 3 * UM_IMG;
+    const int o1 = um_off(row, k), o2 = um_off(row, UM_KP + k);
+#pragma unroll
+    for (int s3 = 0; s3 < 3; ++s3) {
+      *reinterpret_cast<__nv_bfloat16*>(base + (size_t)s3 * UM_IMG + o1) = a3[s3];
+      *reinterpret_cast<__nv_bfloat16*>(base + (size_t)s3 * UM_IMG + o2) = b3[s3];
+    }
+  }
+}
+
+// shared-memory operand descriptor (no swizzle, K-major), Blackwell format
+__device__ __forceinline__ uint64_t um_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t dsc = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  dsc |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  dsc |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  dsc |= (uint64_t)1 << 46;   // descriptor version 1 (tcgen05)
+  return dsc;                 // base offset 0, layout type 0 = no swizzle
+}
+// instruction descriptor: kind::f16, D = F32, A = B = BF16, both K-major, M = N = 128
+constexpr uint32_t UM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void um_mma(uint32_t dtm, uint64_t ad, uint64_t bd, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtm),
+      "l"(ad), "l"(bd), "r"(UM_IDESC), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void um_commit(uint64_t* mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar))
+               : "memory");
+}
+__device__ __forceinline__ void um_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void um_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+// 32 lanes x 32 consecutive FP32 columns of tensor memory into registers
+__device__ __forceinline__ void um_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// one CTA per (128-row tile, 64-column tile, chain); 8 warps: warps w and w+4
+// read accumulator lanes 32(w%4).. and take column halves 0 and 1
+__global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigned char* img_all, int parity) {
+  __shared__ BDesc sd;
+  __shared__ __align__(8) uint64_t s_load, s_mma;
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_fail;
+  extern __shared__ __align__(1024) unsigned char um_dyn[];   // 3 A images, then 3 B images
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    sd = D[blockIdx.y];
+    s_fail = 0;
+    mbar_init(&s_load, 1);
+    mbar_init(&s_mma, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_addr(&s_taddr))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  um_fence_before();
+  __syncthreads();
+  um_fence_after();
+  const BDesc& d = sd;
+  const uint32_t taddr = s_taddr;
+  const int K = *d.kcount;
+  const int ns = d.M.ns, RT = um_rtiles(ns);
+  const int ti = blockIdx.x % RT, tj = blockIdx.x / RT;
+  if (K > 0) {
+    const int K16 = (K + 15) & ~15;
+    const unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
+    const uint32_t part = (uint32_t)(K16 / 8) * UM_LBO;   // bytes of k < K16 in one half
+    if (tid == 0) {
+      mbar_arrive_tx(&s_load, 6u * 2u * part);
+      for (int s3 = 0; s3 < 3; ++s3) {
+        const unsigned char* ga = img + ((size_t)ti * 3 + s3) * UM_IMG;
+        const unsigned char* gb = img + ((size_t)(RT + tj) * 3 + s3) * UM_IMG;
+        unsigned char* sa = um_dyn + (size_t)s3 * UM_IMG;
+        unsigned char* sb = um_dyn + (size_t)(3 + s3) * UM_IMG;
+        const size_t h2 = (size_t)(UM_KP / 8) * UM_LBO;
+        bulk_g2s(sa, ga, part, &s_load);
+        bulk_g2s(sa + h2, ga + h2, part, &s_load);
+        bulk_g2s(sb, gb, part, &s_load);
+        bulk_g2s(sb + h2, gb + h2, part, &s_load);
+      }
+      if (!mbar_wait_bounded(&s_load, 0)) s_fail = 1;
+      um_fence_after();
+      if (!s_fail) {
+        // split pairs (A', B'): (0,0) (0,1) (1,0) (0,2) (1,1) (2,0), packed 2 bits each
+        constexpr uint32_t PA = 0u | (0u << 2) | (1u << 4) | (0u << 6) | (1u << 8) | (2u << 10);
+        constexpr uint32_t PB = 0u | (1u << 2) | (0u << 4) | (2u << 6) | (1u << 8) | (0u << 10);
+        const uint32_t base = smem_addr(um_dyn);
+        uint32_t acc = 0;
+        for (int pr = 0; pr < 6; ++pr) {
+          const uint32_t sa = (PA >> (2 * pr)) & 3u, sb = (PB >> (2 * pr)) & 3u;
+          for (int half = 0; half < 2; ++half)
+            for (int kk = 0; kk < K16 / 16; ++kk) {
+              const uint32_t off = (uint32_t)half * (UM_KP / 8) * UM_LBO + (uint32_t)kk * 2 * UM_LBO;
+              const uint64_t ad = um_desc(base + sa * UM_IMG + off, UM_LBO, 128);
+              const uint64_t bd = um_desc(base + (3 + sb) * UM_IMG + off, UM_LBO, 128);
+              um_mma(taddr, ad, bd, acc);
+              acc = 1;
+            }
+        }
+        um_commit(&s_mma);
+      }
+    }
+    __syncthreads();
+    if (!s_fail) {
+      if (!mbar_wait_bounded(&s_mma, 0)) s_fail = 1;   // every thread observes the commit
+      um_fence_after();
+    }
+    __syncthreads();
+    if (!s_fail) {
+      // epilogue: accumulator lanes (rows) 32(w%4)..+31, columns of half w/4;
+      // the 32 G entries of the thread are loaded before any is written
+      float4* G = reinterpret_cast<float4*>(parity ? d.g_alt : d.g);
+      const int q = warp & 3, half = warp >> 2;
+      const int r = ti * 128 + q * 32 + lane;
+      const int col0 = tj * 64 + half * 32;
+      const int ncol = min(32, ns - col0);
+      float4 gv[32];
+      if (r < ns) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          if (c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c)];
+      }
+      float re[32], im[32];
+      const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+      um_ld32(taddr + lane_base + half * 32, re);
+      um_ld32(taddr + lane_base + 64 + half * 32, im);
+      if (r < ns) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          if (c < ncol) G[r + (size_t)ns * (col0 + c)] = dg_addf(gv[c], make_float2(re[c], im[c]));
+      }
+    } else if (tid == 0) {
+      atomicExch(d.err, PQMC_ERR_TIMEOUT);
+    }
+  }
+  um_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(taddr) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -830,6 +1069,8 @@ struct pqmc_batch {
   int parity = 0;
   int kd = 64;            // delay depth (panel columns per flush)
   int qc = 8;             // panel columns per streamed chunk of the scan
+  int flush_mode = 1;     // 1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush
+  unsigned char* d_img = nullptr;   // split operand tile images of the tcgen05 flush
   int* d_err = nullptr;   // device error word shared by all chains
   int* d_next = nullptr;  // per chain: next plaquette of the current family step
   cudaStream_t stream = nullptr;
@@ -964,8 +1205,18 @@ static int bupdate(pqmc_batch* b, int pf, int time) {
     PQMC_LAUNCHED();
     phase_end(b, PQMC_PHASE_SCAN, ts);
     cudaEvent_t tf = phase_begin(b);
-    k_bflush<<<dim3(tiles, C), 256, 0, b->stream>>>(b->d_desc, b->parity);
-    PQMC_LAUNCHED();
+    if (b->flush_mode == 1 && b->d_img && kd <= UM_KP) {
+      const int ns = c0->ns;
+      const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * ((kd + 15) & ~15);
+      k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, b->stream>>>(b->d_desc, b->d_img);
+      PQMC_LAUNCHED();
+      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, b->stream>>>(b->d_desc, b->d_img,
+                                                                                       b->parity);
+      PQMC_LAUNCHED();
+    } else {
+      k_bflush<<<dim3(tiles, C), 256, 0, b->stream>>>(b->d_desc, b->parity);
+      PQMC_LAUNCHED();
+    }
     phase_end(b, PQMC_PHASE_FLUSH, tf);
   }
   return PQMC_OK;
@@ -1047,6 +1298,13 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_err, sizeof(int)));
   PQMC_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
+  if (precision == PQMC_PREC_MIXED) {
+    // tcgen05 flush: split operand images (zero outside the rows and columns of G)
+    const size_t ib = um_chain_bytes(c0->ns) * (size_t)n_chains;
+    PQMC_CUDA(cudaMalloc((void**)&b->d_img, ib));
+    PQMC_CUDA(cudaMemset(b->d_img, 0, ib));
+    PQMC_CUDA(cudaFuncSetAttribute(k_bflush_um, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * UM_IMG));
+  }
   b->h_desc.resize(n_chains);
   for (int i = 0; i < n_chains; ++i) {
     pqmc_chain* c = b->chains[i];
@@ -1100,8 +1358,15 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
+  if (b->d_img) cudaFree(b->d_img);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
+  return PQMC_OK;
+}
+
+int pqmc_batch_set_flush(pqmc_batch* b, int mode) {
+  if (!b || (mode != 0 && mode != 1)) { set_error("batch_set_flush: mode 0 (mma.sync) or 1 (tcgen05)"); return PQMC_ERR_ARG; }
+  b->flush_mode = mode;
   return PQMC_OK;
 }
 

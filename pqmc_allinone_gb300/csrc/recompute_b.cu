@@ -29,68 +29,116 @@ struct GemmArgs {
   int out_df;   // C is written in the double-float float4 form (not accumulated)
 };
 
+// Batched complex GEMM with FP64-class accuracy on the FP32 pipe: the
+// operands are split into double-float (hi + lo), every real product is
+// formed error-free (hi*hi by FMA two-product plus the hi*lo cross terms),
+// its high part enters the running sum through a two-sum and all low-order
+// parts are summed in plain FP32 (the compensated dot product "Dot2" of
+// Ogita, Rump and Oishi, 2005).  About 12 FP32 instructions per real
+// multiply-add instead of ~27 for full double-float arithmetic.
+// CTA tile 64 x 64, 4 x 4 outputs per thread, k-tiles of 16.
+constexpr int DG_BM = 64, DG_BN = 64, DG_BK = 16;
+
+struct d2acc {
+  float h, l;
+};
+// acc += x*y, x = (xh, xl), y = (yh, yl)
+__device__ __forceinline__ void dot2_mac(d2acc& acc, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float e = __fmaf_rn(xh, yh, -p);
+  const float c = __fmaf_rn(xh, yl, __fmul_rn(xl, yh));
+  const float s = __fadd_rn(acc.h, p);
+  const float bb = __fsub_rn(s, acc.h);
+  const float err = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  acc.h = s;
+  acc.l = __fadd_rn(acc.l, __fadd_rn(err, __fadd_rn(e, c)));
+}
+
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) k_dfgemm(const GemmArgs* args, int m, int n, int k, int accumulate) {
+__global__ void __launch_bounds__(256) k_dfgemm2(const GemmArgs* args, int m, int n, int k, int accumulate) {
   const GemmArgs g = args[blockIdx.z];
-  __shared__ dfc sA[16][33];
-  __shared__ dfc sB[16][33];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int row0 = blockIdx.x * 32, col0 = blockIdx.y * 32;
-  dfc acc[2][2];
-  for (int i = 0; i < 2; ++i)
-    for (int j = 0; j < 2; ++j) acc[i][j] = dfc_zero();
-  for (int kk = 0; kk < k; kk += 16) {
-    for (int e = threadIdx.x; e < 16 * 32; e += 256) {
-      int r = e & 31, q = e >> 5;
-      int gr = row0 + r, gk = kk + q;
+  __shared__ float4 sA[DG_BK][DG_BM];   // (re.hi, re.lo, im.hi, im.lo)
+  __shared__ float4 sB[DG_BK][DG_BN];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int row0 = blockIdx.x * DG_BM, col0 = blockIdx.y * DG_BN;
+  d2acc cr[4][4], ci[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      cr[i][j] = d2acc{0.f, 0.f};
+      ci[i][j] = d2acc{0.f, 0.f};
+    }
+  for (int kk = 0; kk < k; kk += DG_BK) {
+    // stage A(row0:+64, kk:+16) and B(kk:+16, col0:+64) as double-float, reading
+    // memory in its contiguous direction
+    for (int e = tid; e < DG_BM * DG_BK; e += 256) {
+      int r, q;
+      if (TA) { q = e % DG_BK; r = e / DG_BK; } else { r = e % DG_BM; q = e / DG_BM; }
+      const int gr = row0 + r, gk = kk + q;
       cplx v = mk(0.0);
       if (gr < m && gk < k) v = TA ? cconj(g.A[gk + (size_t)g.lda * gr]) : g.A[gr + (size_t)g.lda * gk];
-      sA[q][r] = dfc_make(v);
+      const df vr = df_make(v.x), vi = df_make(v.y);
+      sA[q][r] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);
     }
-    for (int e = threadIdx.x; e < 16 * 32; e += 256) {
-      int q = e & 15, cc = e >> 4;
-      int gc = col0 + cc, gk = kk + q;
+    for (int e = tid; e < DG_BK * DG_BN; e += 256) {
+      int q, c;
+      if (TB) { c = e % DG_BN; q = e / DG_BN; } else { q = e % DG_BK; c = e / DG_BK; }
+      const int gc = col0 + c, gk = kk + q;
       cplx v = mk(0.0);
       if (gc < n && gk < k) v = TB ? cconj(g.B[gc + (size_t)g.ldb * gk]) : g.B[gk + (size_t)g.ldb * gc];
-      sB[q][cc] = dfc_make(v);
+      const df vr = df_make(v.x), vi = df_make(v.y);
+      sB[q][c] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);
     }
     __syncthreads();
-#pragma unroll 4
-    for (int q = 0; q < 16; ++q) {
-      dfc a0 = sA[q][tx], a1 = sA[q][tx + 16];
-      dfc b0 = sB[q][ty], b1 = sB[q][ty + 16];
-      acc[0][0] = dfc_add(acc[0][0], dfc_mul(a0, b0));
-      acc[1][0] = dfc_add(acc[1][0], dfc_mul(a1, b0));
-      acc[0][1] = dfc_add(acc[0][1], dfc_mul(a0, b1));
-      acc[1][1] = dfc_add(acc[1][1], dfc_mul(a1, b1));
+#pragma unroll 2
+    for (int q = 0; q < DG_BK; ++q) {
+      float4 av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = sA[q][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = sB[q][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float4 x = av[i], y = bv[j];
+          // re += xr yr - xi yi ; im += xr yi + xi yr
+          dot2_mac(cr[i][j], x.x, x.y, y.x, y.y);
+          dot2_mac(cr[i][j], -x.z, -x.w, y.z, y.w);
+          dot2_mac(ci[i][j], x.x, x.y, y.z, y.w);
+          dot2_mac(ci[i][j], x.z, x.w, y.x, y.y);
+        }
     }
     __syncthreads();
   }
-  for (int i = 0; i < 2; ++i)
-    for (int j = 0; j < 2; ++j) {
-      int r = row0 + tx + 16 * i, c = col0 + ty + 16 * j;
-      if (r < m && c < n) {
-        cplx* p = g.C + r + (size_t)g.ldc * c;
-        if (g.out_df) {
-          *reinterpret_cast<float4*>(p) = dg_from_dfc(acc[i][j]);
-        } else if (accumulate) {
-          dfc v = dfc_add(acc[i][j], dfc_make(*p));
-          *p = dfc_to_d(v);
-        } else {
-          *p = dfc_to_d(acc[i][j]);
-        }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = row0 + tx + 16 * i, c = col0 + ty + 16 * j;
+      if (r >= m || c >= n) continue;
+      df re = quick_two_sum(cr[i][j].h, cr[i][j].l), im = quick_two_sum(ci[i][j].h, ci[i][j].l);
+      cplx* p = g.C + r + (size_t)g.ldc * c;
+      if (g.out_df) {
+        *reinterpret_cast<float4*>(p) = make_float4(re.hi, im.hi, re.lo, im.lo);
+      } else if (accumulate) {
+        const dfc v = dfc_add(dfc{re, im}, dfc_make(*p));
+        *p = dfc_to_d(v);
+      } else {
+        *p = make_double2(df_to_d(re), df_to_d(im));
       }
     }
 }
 
 int dfgemm_batched(cudaStream_t s, char ta, char tb, int m, int n, int k, const GemmArgs* d_args, int count,
                    int accumulate) {
-  dim3 grid((m + 31) / 32, (n + 31) / 32, count);
+  dim3 grid((m + DG_BM - 1) / DG_BM, (n + DG_BN - 1) / DG_BN, count);
   bool TA = ta == 'C', TB = tb == 'C';
-  if (!TA && !TB) k_dfgemm<false, false><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
-  else if (TA && !TB) k_dfgemm<true, false><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
-  else if (!TA && TB) k_dfgemm<false, true><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
-  else k_dfgemm<true, true><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
+  if (!TA && !TB) k_dfgemm2<false, false><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
+  else if (TA && !TB) k_dfgemm2<true, false><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
+  else if (!TA && TB) k_dfgemm2<false, true><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
+  else k_dfgemm2<true, true><<<grid, 256, 0, s>>>(d_args, m, n, k, accumulate);
   PQMC_LAUNCHED();
   return PQMC_OK;
 }

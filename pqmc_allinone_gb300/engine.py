@@ -275,6 +275,10 @@ class PqmcBatch:
     def set_delay(self, depth: int):
         check(self.lib, self.lib.pqmc_batch_set_delay(self.h, depth), "pqmc_batch_set_delay")
 
+    def set_flush(self, mode: int):
+        """1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush."""
+        check(self.lib, self.lib.pqmc_batch_set_flush(self.h, mode), "pqmc_batch_set_flush")
+
     def close(self):
         if getattr(self, "h", None) is not None:
             for c in self.chains:

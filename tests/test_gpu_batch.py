@@ -91,3 +91,28 @@ def test_mixed_batch_drift_and_recompute_8x8():
         o.init_expkv()
         o.init_g(1)
         assert rel_fro(ch.g(), o.g()) < MIXED_RECOMPUTE_TOL
+
+
+@pytest.mark.parametrize("L", [8, 14])
+def test_tcgen05_flush_matches_mma_sync(L):
+    """The two rank-K flush engines (tcgen05 with the accumulator in tensor
+    memory, and mma.sync split-BF16 tiles) on identical chains: the same
+    accept/reject decisions and G equal to FP32 accumulation rounding, over
+    slices that end before the stabilised recompute (which would replace G)."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(2):
+        m, f = epsocz_small(L=L, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=60 + i)
+        ms.append((m, f, seed_words(600 + i)))
+    out = []
+    for mode in (0, 1):
+        b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+        b.set_flush(mode)
+        b.init()
+        b.sweep_slices(1, 1, 5)
+        out.append([(c.field(), c.g(), c.state()) for c in b.chains])
+        b.close()
+    for (f0, g0, s0), (f1, g1, s1) in zip(*out):
+        assert np.array_equal(f0, f1)
+        assert s0["positive_accept"] == s1["positive_accept"] and s0["positive_accept"] > 0
+        assert rel_fro(g1, g0) < 2e-6

@@ -47,7 +47,8 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="c4_mixed", choices=["c4_mixed", "c2_fp64", "small"])
     p.add_argument("--chains", type=int, default=0, help="chains per GPU of the mixed batch (default 64)")
-    p.add_argument("--delay", type=int, default=64, help="delay depth of the mixed batch")
+    p.add_argument("--delay", type=int, default=0,
+                   help="delay depth of the mixed batch (0: chosen by the autotuner during warm-up)")
     p.add_argument("--flush", type=int, default=1, choices=[0, 1],
                    help="rank-K flush engine: 1 tcgen05 (tensor memory accumulator), 0 mma.sync")
     p.add_argument("--plain-steps", type=int, default=3, help="timed blocks of the plain FP64 chain")
@@ -287,12 +288,22 @@ def run_mixed(args, world, rank, local):
     seeds = [3000 + i + 1000 * rank for i in range(C)]
     fields = [M.field_gaussian(m, s) for s in seeds]
     b = PqmcBatch([m] * C, fields, [seed_words(s) for s in seeds], precision=1)
-    b.set_delay(args.delay)
-    b.set_flush(args.flush)
     t0 = time.perf_counter()
     b.init()
     t_init = time.perf_counter() - t0
     cur = Cursor(m)
+    tune = None
+    if args.delay > 0:
+        b.set_delay(args.delay)
+        b.set_flush(args.flush)
+        depth = args.delay
+    else:
+        # the autotuner runs one block per candidate depth (part of the warm-up)
+        cands = (32, 48, 64, 96, 128)
+        depth, table = b.autotune(cur.loop, cur.tc, m.ngroup, cands)
+        for _ in cands:
+            cur.next()
+        tune = {"candidates_ms_per_slice": table, "chosen": depth}
     for _ in range(args.warmup):
         b.sweep_slices(*cur.next(), m.ngroup)
     torch.cuda.synchronize()
@@ -370,8 +381,9 @@ def run_mixed(args, world, rank, local):
            "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp32/bf16 fast path on an FP64 G",
            "data": "synthetic (x ~ N(0,0.5^2), seeds 3000+i)",
-           "config": config_of(args.workload, m, world, C, {"delay_depth": args.delay,
-                                                             "flush": "tcgen05" if args.flush else "mma.sync"}),
+           "config": config_of(args.workload, m, world, C, {"delay_depth": depth, "autotune": tune,
+                                                             "flush": "tcgen05" if (depth <= 64 and (args.flush or tune))
+                                                             else "mma.sync"}),
            "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "clocks": clocks,
            "cpu_baseline": cb, "plain_fp64": plain,
            "speedup_vs_plain_fp64": (per_gpu / plain["value"]) if plain else None,

@@ -289,6 +289,15 @@ int pqmc_batch_set_delay(pqmc_batch* batch, int depth);
 int pqmc_batch_set_flush(pqmc_batch* batch, int mode);
 /* one sweep of every chain (Main_PQMC.f90:99-154), no measurement */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
+/* Delay-depth autotuner (no reference counterpart): runs n_slices slices
+ * of the sweep order per candidate depth, starting at (loop, first_tc) and
+ * continuing block after block (these are genuine Monte Carlo steps of every
+ * chain, so tune during warm-up), times each with CUDA events and keeps the
+ * fastest depth (and the tcgen05 flush when it allows).  ms_out (optional,
+ * n_candidates) receives the measured ms per slice. */
+int pqmc_batch_autotune(pqmc_batch* batch, int loop, int first_tc, int n_slices,
+                        const int* candidates, int n_candidates, int* best,
+                        double* ms_out);
 /* slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain */
 int pqmc_batch_sweep_slices(pqmc_batch* batch, int loop, int first_tc, int n_slices);
 /* init_expKV and init_g_T0(1) (mod_evolution.f90:46-111) of every chain

@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf, int t) {
 // accepted move builds its rank-dim panel block (one pass over the panels)
 // and adds its contribution to the cached Geff blocks of the later
 // plaquettes.
-constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_KSTAGE = 512;   // max delay depth (panel columns)
 
 __device__ __forceinline__ float2 fdiv1(float2 a) {   // 1/a
@@ -329,7 +329,7 @@ __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 constexpr int SCAN_NSTAGE = 3;   // panel chunks in flight
-constexpr int SCAN_RPT = 4;      // rows per thread: Ns <= SCAN_RPT * SCAN_THREADS
+constexpr int SCAN_RPT = 2;      // rows per thread: Ns <= SCAN_RPT * SCAN_THREADS
 
 __host__ __device__ __forceinline__ size_t al16(size_t b) { return (b + 15) & ~(size_t)15; }
 
@@ -368,9 +368,12 @@ __device__ __forceinline__ void scan_issue(float2* s_stage, uint64_t* s_full, co
 template <int DIM>
 __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int t, int parity, int kd, int qc,
                                                          int* next_p) {
+  constexpr int NW = SCAN_THREADS / 32;
   __shared__ BDesc sd;
-  __shared__ float2 s_R[SCAN_THREADS / 32][16];
-  __shared__ float2 s_T[SCAN_THREADS / 32][16];
+  __shared__ float2 s_R[NW][16];
+  __shared__ float2 s_T[16];
+  __shared__ float2 s_det[NW];
+  __shared__ int s_dec[NW];
   __shared__ __align__(8) uint64_t s_full[SCAN_NSTAGE];
   __shared__ int s_abort;
   extern __shared__ __align__(16) unsigned char s_dyn[];
@@ -428,46 +431,69 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   int p = p0;
   const int i = lane % dim, j = lane / dim;
   const bool act = lane < dd;
-  for (; p < npla; ++p) {
-    if (K + dim > kd) break;
-    // ---- ratio, evaluated by every warp from shared memory ----------------
-    const float2* ge = s_geff + 16 * p;
-    const float2* de = s_delta + 16 * p;
-    if (act) {
-      float2 a = make_float2(i == j ? 1.f : 0.f, 0.f);
+  while (p < npla && K + dim <= kd) {
+    // ---- ratios of the next NW proposals, one warp each, from the cached
+    //      Geff (valid for every proposal up to the first accepted one) ------
+    {
+      const int pw = p + warp;
+      int dec = 0;
+      float2 det = make_float2(0.f, 0.f);
+      if (pw < npla) {
+        const float2* ge = s_geff + 16 * pw;
+        const float2* de = s_delta + 16 * pw;
+        if (act) {
+          float2 a = make_float2(i == j ? 1.f : 0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < dim; ++k) a = fa(a, fm(ge[i + dim * k], de[k + dim * j]));
-      s_R[warp][lane] = a;
+          for (int k = 0; k < dim; ++k) a = fa(a, fm(ge[i + dim * k], de[k + dim * j]));
+          s_R[warp][lane] = a;
+        }
+        __syncwarp();
+        det = wf_det(dim, s_R[warp], lane);
+        const float dm = det.x * det.x + det.y * det.y;
+        dec = ((double)dm >= s_thr[pw]) ? 1 : 0;
+      }
+      if (lane == 0) {
+        s_dec[warp] = dec;
+        s_det[warp] = det;
+      }
     }
-    __syncwarp();
-    const float2 det = wf_det(dim, s_R[warp], lane);
-    const float dm = det.x * det.x + det.y * det.y;
-    if (!((double)dm >= s_thr[p])) {
-      if (tid == 0) na++;
+    __syncthreads();
+    int wa = -1;
+    for (int w = 0; w < NW && p + w < npla; ++w)
+      if (s_dec[w]) { wa = w; break; }
+    if (wa < 0) {   // all evaluated proposals rejected
+      const int nrej = min(NW, npla - p);
+      if (tid == 0) na += nrej;
+      p += nrej;
+      __syncthreads();   // s_dec / s_R are rewritten by the next pass
       continue;
     }
-    // ---- accepted: T = Delta R^-1 on every warp, record the move ---------
-    wf_inverse(dim, s_R[warp], det, lane);
-    if (act) {
-      float2 a = make_float2(0.f, 0.f);
+    if (tid == 0) na += wa;
+    p += wa;
+    // ---- accepted move p: T = Delta R^-1 by the warp that evaluated it ------
+    const float2 det = s_det[wa];
+    if (warp == wa) {
+      wf_inverse(dim, s_R[warp], det, lane);
+      if (act) {
+        const float2* de = s_delta + 16 * p;
+        float2 a = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < dim; ++k) a = fa(a, fm(de[i + dim * k], s_R[warp][k + dim * j]));
-      s_T[warp][lane] = a;
-    }
-    __syncwarp();
-    if (tid == 0) {
-      s_accp[n_acc] = p;
-      s_accd[n_acc] = det;
+        for (int k = 0; k < dim; ++k) a = fa(a, fm(de[i + dim * k], s_R[warp][k + dim * j]));
+        s_T[lane] = a;
+      }
+      if (lane == 0) {
+        s_accp[n_acc] = p;
+        s_accd[n_acc] = det;
+      }
     }
     ++n_acc;
     const int* S = s_site + 4 * p;
-    // ---- panel block: a(r,l) = sum_m Geff(r,S_m) T(m,l), b(l,r) = delta(S_l,r) - Geff(S_l,r),
-    //      Geff = G + A B with the panel streamed through shared memory in chunks of qc columns
     const int nch = (K + qc - 1) / qc;
     if (tid == 0 && nch > 0) {
       fence_proxy_async_global();   // this round's panel columns were written by generic stores
       for (int c = 0; c < nch && c < SCAN_NSTAGE; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
     }
+    // rows of G at the accepted sites; then warm L2 with the next plaquette's
     float2 gm[SCAN_RPT][dim], bl[SCAN_RPT][dim];
 #pragma unroll
     for (int k = 0; k < SCAN_RPT; ++k) {
@@ -478,6 +504,19 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
         bl[k][m] = r < ns ? dg_f2(G[S[m] + (size_t)ns * r]) : make_float2(0.f, 0.f);
       }
     }
+    if (p + 1 < npla) {
+      const int* Sn = s_site + 4 * (p + 1);
+#pragma unroll
+      for (int k = 0; k < SCAN_RPT; ++k) {
+        const int r = tid + k * SCAN_THREADS;
+        if (r < ns)
+#pragma unroll
+          for (int m = 0; m < dim; ++m) {
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(G + r + (size_t)ns * Sn[m]));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(G + Sn[m] + (size_t)ns * r));
+          }
+      }
+    }
     for (int c = 0; c < nch; ++c) {
       const int st = c % SCAN_NSTAGE;
       if (!mbar_wait_bounded(&s_full[st], (phase >> st) & 1u)) s_abort = 1;
@@ -485,6 +524,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       const float2* cA = s_stage + (size_t)st * 2 * qc * ldp;
       const float2* cB = cA + (size_t)qc * ldp;
       const int nq = min(qc, K - c * qc);
+#pragma unroll 2
       for (int qq = 0; qq < nq; ++qq) {
         float2 bs[dim], as[dim];
 #pragma unroll
@@ -513,7 +553,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       aborted = true;
       break;
     }
-    const float2* Tw = s_T[warp];
+    if (nch == 0) __syncthreads();   // s_T visible
 #pragma unroll
     for (int k = 0; k < SCAN_RPT; ++k) {
       const int r = tid + k * SCAN_THREADS;
@@ -522,7 +562,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       for (int l = 0; l < dim; ++l) {
         float2 a = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int m = 0; m < dim; ++m) a = fa(a, fm(gm[k][m], Tw[m + dim * l]));
+        for (int m = 0; m < dim; ++m) a = fa(a, fm(gm[k][m], s_T[m + dim * l]));
         float2 bv = make_float2(-bl[k][l].x, -bl[k][l].y);
         if (r == S[l]) bv.x += 1.f;
         A[(size_t)(K + l) * ldp + r] = a;
@@ -542,6 +582,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       s_geff[16 * pq + k] = a;
     }
     K += dim;
+    ++p;
     __syncthreads();
   }
   if (aborted) {
@@ -778,38 +819,49 @@ __global__ void __launch_bounds__(256) k_bsplit(const BDesc* D, unsigned char* i
   const int ns = d.M.ns, ldp = d.ldp, K16 = (K + 15) & ~15;
   const int RT = um_rtiles(ns), CT = um_ctiles(ns);
   unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
-  // work item: (tile t, row in tile, k < K16); A tiles first, then B tiles
-  const long total = (long)(RT + CT) * 128 * K16;
+  // work item: (tile t, group of 8 k, row in tile); consecutive threads take
+  // consecutive rows, so the panel reads coalesce and every thread writes one
+  // 16-byte core-matrix row per split and half
+  const int KG = K16 / 8;
+  const long total = (long)(RT + CT) * KG * 128;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-    const int k = (int)(e % K16);
-    const int row = (int)((e / K16) % 128);
-    const int t = (int)(e / ((long)K16 * 128));
-    float2 lo_part, hi_part;   // values at k (first half) and UM_KP + k (second half)
-    if (t < RT) {
-      const int r = t * 128 + row;
-      const float2 v = (r < ns && k < K) ? d.A[(size_t)k * ldp + r] : make_float2(0.f, 0.f);
-      lo_part = make_float2(v.x, 0.f);   // Ar
-      hi_part = make_float2(v.y, 0.f);   // Ai
-    } else {
-      const int ct = t - RT, n = row & 63, c = ct * 64 + n;
-      const float2 v = (c < ns && k < K) ? d.B[(size_t)k * ldp + c] : make_float2(0.f, 0.f);
-      if (row < 64) {   // re column: [Br | -Bi]
-        lo_part = make_float2(v.x, 0.f);
-        hi_part = make_float2(-v.y, 0.f);
-      } else {          // im column: [Bi | Br]
-        lo_part = make_float2(v.y, 0.f);
-        hi_part = make_float2(v.x, 0.f);
+    const int row = (int)(e % 128);
+    const int kg = (int)((e / 128) % KG);
+    const int t = (int)(e / (128L * KG));
+    float lo8[8], hi8[8];   // values at k (first half) and UM_KP + k (second half)
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      const int k = kg * 8 + jj;
+      if (t < RT) {
+        const int r = t * 128 + row;
+        const float2 v = (r < ns && k < K) ? d.A[(size_t)k * ldp + r] : make_float2(0.f, 0.f);
+        lo8[jj] = v.x;   // Ar
+        hi8[jj] = v.y;   // Ai
+      } else {
+        const int c = (t - RT) * 64 + (row & 63);
+        const float2 v = (c < ns && k < K) ? d.B[(size_t)k * ldp + c] : make_float2(0.f, 0.f);
+        if (row < 64) { lo8[jj] = v.x; hi8[jj] = -v.y; }   // re column: [Br | -Bi]
+        else { lo8[jj] = v.y; hi8[jj] = v.x; }             // im column: [Bi | Br]
       }
     }
-    __nv_bfloat16 a3[3], b3[3];
-    split3b(lo_part.x, a3);
-    split3b(hi_part.x, b3);
+    __align__(16) __nv_bfloat16 ls[3][8], hs[3][8];
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      __nv_bfloat16 a3[3], b3[3];
+      split3b(lo8[jj], a3);
+      split3b(hi8[jj], b3);
+#pragma unroll
+      for (int s3 = 0; s3 < 3; ++s3) {
+        ls[s3][jj] = a3[s3];
+        hs[s3][jj] = b3[s3];
+      }
+    }
     unsigned char* base = img + (size_t)t * 3 * UM_IMG;
-    const int o1 = um_off(row, k), o2 = um_off(row, UM_KP + k);
+    const int o1 = um_off(row, kg * 8), o2 = um_off(row, UM_KP + kg * 8);
 #pragma unroll
     for (int s3 = 0; s3 < 3; ++s3) {
-      *reinterpret_cast<__nv_bfloat16*>(base + (size_t)s3 * UM_IMG + o1) = a3[s3];
-      *reinterpret_cast<__nv_bfloat16*>(base + (size_t)s3 * UM_IMG + o2) = b3[s3];
+      *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o1) = *reinterpret_cast<const uint4*>(ls[s3]);
+      *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o2) = *reinterpret_cast<const uint4*>(hs[s3]);
     }
   }
 }
@@ -1207,7 +1259,7 @@ static int bupdate(pqmc_batch* b, int pf, int time) {
     cudaEvent_t tf = phase_begin(b);
     if (b->flush_mode == 1 && b->d_img && kd <= UM_KP) {
       const int ns = c0->ns;
-      const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * ((kd + 15) & ~15);
+      const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * (((kd + 15) & ~15) / 8);
       k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, b->stream>>>(b->d_desc, b->d_img);
       PQMC_LAUNCHED();
       k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, b->stream>>>(b->d_desc, b->d_img,
@@ -1416,6 +1468,48 @@ int pqmc_batch_get_timing(pqmc_batch* b, double* ms, long long* launches) {
 int pqmc_batch_stream(pqmc_batch* b, void** stream) {
   if (!b || !stream) { set_error("batch_stream: null argument"); return PQMC_ERR_ARG; }
   *stream = (void*)b->stream;
+  return PQMC_OK;
+}
+
+int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, const int* candidates, int n_candidates,
+                        int* best, double* ms_out) {
+  if (!b || !candidates || n_candidates < 1 || n_slices < 1 || !best) {
+    set_error("batch_autotune: bad arguments");
+    return PQMC_ERR_ARG;
+  }
+  if (b->precision != PQMC_PREC_MIXED) { set_error("batch_autotune: mixed batches only"); return PQMC_ERR_ARG; }
+  pqmc_chain* c0 = b->chains[0];
+  const int nt = c0->ntime;
+  cudaEvent_t e0, e1;
+  PQMC_CUDA(cudaEventCreate(&e0));
+  PQMC_CUDA(cudaEventCreate(&e1));
+  double best_ms = 1e300;
+  int best_kd = b->kd;
+  int lp = loop, tc = first_tc;
+  int st = PQMC_OK;
+  for (int i = 0; i < n_candidates && st == PQMC_OK; ++i) {
+    const int kd = candidates[i];
+    if (kd < 1 || kd > SCAN_KSTAGE) { st = PQMC_ERR_ARG; set_error("batch_autotune: depth %d out of range", kd); break; }
+    b->kd = kd;
+    const int n = std::min(n_slices, nt - tc + 1);
+    cudaEventRecord(e0, b->stream);
+    st = pqmc_batch_sweep_slices(b, lp, tc, n);
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per_slice = ms / n;
+    if (ms_out) ms_out[i] = per_slice;
+    if (per_slice < best_ms) { best_ms = per_slice; best_kd = kd; }
+    tc += n;
+    if (tc > nt) { tc = 1; ++lp; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != PQMC_OK) return st;
+  b->kd = best_kd;
+  b->flush_mode = best_kd <= UM_KP ? 1 : 0;
+  *best = best_kd;
   return PQMC_OK;
 }
 

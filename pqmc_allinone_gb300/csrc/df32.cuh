@@ -114,3 +114,25 @@ __device__ __forceinline__ float4 dg_addf(float4 g, float2 a) {
 }
 __device__ __forceinline__ float4 dg_from_dfc(dfc a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
 __device__ __forceinline__ dfc dfc_from_dg(float4 g) { return dfc{df{g.x, g.z}, df{g.y, g.w}}; }
+
+// (h, l) -= x*y for double-float reals: the product formed error-free
+// (FMA two-product plus the hi*lo cross terms), its high part subtracted by a
+// two-sum, the low-order parts gathered in l (not renormalised)
+__device__ __forceinline__ void df_msub_acc(float& h, float& l, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float e = __fmaf_rn(xh, yh, -p);
+  const float c = __fmaf_rn(xh, yl, __fmul_rn(xl, yh));
+  const df s = two_sum(h, -p);
+  h = s.hi;
+  l = __fsub_rn(__fadd_rn(l, s.lo), __fadd_rn(e, c));
+}
+// a - f*b for double-float complex values, one renormalisation per component
+// (about half the instructions of dfc_sub(a, dfc_mul(f, b)))
+__device__ __forceinline__ dfc dfc_fms(dfc a, dfc f, dfc b) {
+  float rh = a.re.hi, rl = a.re.lo, ih = a.im.hi, il = a.im.lo;
+  df_msub_acc(rh, rl, f.re.hi, f.re.lo, b.re.hi, b.re.lo);     // re -= fr br
+  df_msub_acc(rh, rl, -f.im.hi, -f.im.lo, b.im.hi, b.im.lo);   // re += fi bi
+  df_msub_acc(ih, il, f.re.hi, f.re.lo, b.im.hi, b.im.lo);     // im -= fr bi
+  df_msub_acc(ih, il, f.im.hi, f.im.lo, b.re.hi, b.re.lo);     // im -= fi br
+  return dfc{quick_two_sum(rh, rl), quick_two_sum(ih, il)};
+}

@@ -27,6 +27,8 @@ struct GemmArgs {
   cplx* C;
   int lda, ldb, ldc;
   int out_df;   // C is written in the double-float float4 form (not accumulated)
+  int shape;    // 0 general; 1 only the lower triangle of C is needed (Gram
+                // matrix for a Cholesky factor); 2 B is upper triangular
 };
 
 // Batched complex GEMM with FP64-class accuracy on the FP32 pipe: the
@@ -61,6 +63,8 @@ __global__ void __launch_bounds__(256) k_dfgemm2(const GemmArgs* args, int m, in
   __shared__ float4 sB[DG_BK][DG_BN];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int row0 = blockIdx.x * DG_BM, col0 = blockIdx.y * DG_BN;
+  if (g.shape == 1 && row0 + DG_BM <= col0) return;   // tile strictly above the diagonal
+  if (g.shape == 2) k = min(k, col0 + DG_BN);          // B(q, c) = 0 for q > c
   d2acc cr[4][4], ci[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -585,7 +589,7 @@ __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_gj_cluste
       dfc* cj = A + (size_t)n * jl;
       const dfc f = s_f[i];
       if (c_lo + jl == k) cj[i] = dfc_sub(dfc_zero(), dfc_mul(f, rec));
-      else cj[i] = dfc_sub(cj[i], dfc_mul(f, cj[k]));
+      else cj[i] = dfc_fms(cj[i], f, cj[k]);
     }
     cl.sync();   // s_f, s_p, s_rec are rewritten by the next step's owner
   }
@@ -681,7 +685,7 @@ __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_chol_clus
       if (i < k) continue;
       const dfc lkj = s_f[k];
       dfc* cell = A + (size_t)n * (k - c_lo) + i;
-      *cell = dfc_sub(*cell, dfc_mul(s_f[i], dfc{lkj.re, df_neg(lkj.im)}));
+      *cell = dfc_fms(*cell, s_f[i], dfc{lkj.re, df_neg(lkj.im)});
     }
     cl.sync();
   }
@@ -865,7 +869,7 @@ int BatchRecompute::cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*
   std::vector<GemmArgs> ga(C);
   std::vector<CholArgs> ca(C);
   for (int pass = 0; pass < 2; ++pass) {
-    for (int i = 0; i < C; ++i) ga[i] = GemmArgs{X[i], X[i], gram + (size_t)i * ne * ne, ns, ns, ne};
+    for (int i = 0; i < C; ++i) ga[i] = GemmArgs{X[i], X[i], gram + (size_t)i * ne * ne, ns, ns, ne, 0, 1};
     PQMC_TRY(gemm('C', 'N', ne, ne, ns, ga, 0, 0));
     for (int i = 0; i < C; ++i)
       ca[i] = CholArgs{gram + (size_t)i * ne * ne, work_df + (size_t)i * ne * ne, rinv + (size_t)i * ne * ne, D[i],
@@ -881,7 +885,8 @@ int BatchRecompute::cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*
     k_tri_inv<<<dim3((ne + TRI_WARPS - 1) / TRI_WARPS, C), TRI_WARPS * 32, sizeof(dfc) * TRI_WARPS * ne, stream>>>(
         d_chol, ne);
     PQMC_LAUNCHED();
-    for (int i = 0; i < C; ++i) ga[i] = GemmArgs{X[i], rinv + (size_t)i * ne * ne, tmpX + (size_t)i * ns * ne, ns, ne, ns};
+    for (int i = 0; i < C; ++i)
+      ga[i] = GemmArgs{X[i], rinv + (size_t)i * ne * ne, tmpX + (size_t)i * ns * ne, ns, ne, ns, 0, 2};
     PQMC_TRY(gemm('N', 'N', ns, ne, ne, ga, 1, 0));
     for (int i = 0; i < C; ++i)
       PQMC_CUDA(cudaMemcpyAsync(X[i], tmpX + (size_t)i * ns * ne, sizeof(cplx) * (size_t)ns * ne,

@@ -275,6 +275,18 @@ class PqmcBatch:
     def set_delay(self, depth: int):
         check(self.lib, self.lib.pqmc_batch_set_delay(self.h, depth), "pqmc_batch_set_delay")
 
+    def autotune(self, loop: int, first_tc: int, n_slices: int, candidates=(32, 48, 64, 96, 128)):
+        """Delay-depth autotuner: one block of n_slices per candidate from
+        (loop, first_tc) on (genuine Monte Carlo steps); keeps the fastest.
+        Returns (best depth, {depth: ms per slice})."""
+        cand = np.ascontiguousarray(candidates, dtype=np.int32)
+        ms = np.zeros(len(cand))
+        best = np.zeros(1, dtype=np.int32)
+        check(self.lib, self.lib.pqmc_batch_autotune(self.h, loop, first_tc, n_slices, cand.ctypes.data_as(_i32p),
+                                                      len(cand), best.ctypes.data_as(_i32p),
+                                                      ms.ctypes.data_as(_f64p)), "pqmc_batch_autotune")
+        return int(best[0]), {int(k): float(v) for k, v in zip(cand, ms)}
+
     def set_flush(self, mode: int):
         """1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush."""
         check(self.lib, self.lib.pqmc_batch_set_flush(self.h, mode), "pqmc_batch_set_flush")

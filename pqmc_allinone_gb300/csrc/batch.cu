@@ -43,9 +43,6 @@ struct BDesc {
   PlaqPre* pre;
   DevScalars* sc;
   int* kcount;
-  const int* wpla;   // wrap cover items of the family loop (per family, see host)
-  const int* wsites;
-  const int* wdim;
 };
 
 __device__ __forceinline__ float2 f2(cplx a) { return make_float2((float)a.x, (float)a.y); }
@@ -54,7 +51,7 @@ __device__ __forceinline__ float2 fa(float2 a, float2 b) { return make_float2(a.
 __device__ __forceinline__ float2 fsb(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 
 // ---------------------------------------------------------------------------
-__global__ void k_bdraw(BDesc* D, int C, int pf) {
+__global__ void k_bdraw(const BDesc* D, int C, int pf) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const BDesc d = D[c];
@@ -1019,7 +1016,9 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigne
 // are the family's plaquettes (DIM sites) and uncovered singletons, so every
 // block is at most DIM x DIM and lives in registers.
 template <int DIM>
-__global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, int left, int n_items, int parity) {
+__global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, int left, int n_items, int parity,
+                                               const int* __restrict__ wpla, const int* __restrict__ wsites,
+                                               const int* __restrict__ wdim) {
   __shared__ BDesc sd;
   if (threadIdx.x == 0) sd = D[blockIdx.y];
   __syncthreads();
@@ -1029,14 +1028,14 @@ __global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, in
   const DevModel& M = d.M;
   const int ir = (int)(pair % n_items), ic = (int)(pair / n_items);
   const int ns = M.ns, pd = M.pdim;
-  const int dr = d.wdim[ir], dc = d.wdim[ic];
+  const int dr = wdim[ir], dc = wdim[ic];
   const float4* gin = reinterpret_cast<const float4*>(parity ? d.g_alt : d.g);   // double-float G
   float4* gout = reinterpret_cast<float4*>(parity ? d.g : d.g_alt);
   int Sr[DIM], Sc[DIM];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
-    Sr[k] = k < dr ? d.wsites[4 * ir + k] : 0;
-    Sc[k] = k < dc ? d.wsites[4 * ic + k] : 0;
+    Sr[k] = k < dr ? wsites[4 * ir + k] : 0;
+    Sc[k] = k < dc ? wsites[4 * ic + k] : 0;
   }
   float4 gd[DIM][DIM];
   float2 gf[DIM][DIM], am[DIM][DIM], bm[DIM][DIM];
@@ -1047,7 +1046,7 @@ __global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, in
       gd[a][b] = (a < dr && b < dc) ? gin[Sr[a] + (size_t)ns * Sc[b]] : make_float4(0.f, 0.f, 0.f, 0.f);
       gf[a][b] = dg_f2(gd[a][b]);
     }
-  const int pr = d.wpla[ir], pc = d.wpla[ic];
+  const int pr = wpla[ir], pc = wpla[ic];
   const cplx* Am = (pr >= 0) ? (left ? d.expkv : d.expkv_inv) + M.kv_base(pr, pf, t) : nullptr;
   const cplx* Bm = (pc >= 0) ? (left ? d.expkv_inv : d.expkv) + M.kv_base(pc, pf, t) : nullptr;
   // (A - I) and (B - I) in FP32; identity blocks for singletons
@@ -1125,8 +1124,14 @@ struct pqmc_batch {
   unsigned char* d_img = nullptr;   // split operand tile images of the tcgen05 flush
   int* d_err = nullptr;   // device error word shared by all chains
   int* d_next = nullptr;  // per chain: next plaquette of the current family step
-  cudaStream_t stream = nullptr;
-  pqmc::BatchRecompute rec;
+  cudaStream_t stream = nullptr;   // the stream of group 0, the batch's public stream
+  // chain groups: each group has its own stream and recompute workspace, so
+  // one group's latency-bound scan overlaps the other's flush and recompute
+  int n_groups = 1;
+  int g_first[2] = {0, 0}, g_count[2] = {0, 0};
+  cudaStream_t g_stream[2] = {nullptr, nullptr};
+  pqmc::BatchRecompute rec[2];
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 using namespace pqmc;
@@ -1203,84 +1208,87 @@ static int batch_sync_parity(pqmc_batch* b) {
   return batch_refresh(b);
 }
 
-static int bwrap(pqmc_batch* b, int pf, int time, bool left) {
+// phase timers follow group 0 only (groups overlap on the device)
+static cudaEvent_t gphase_begin(pqmc_batch* b, int g) { return g == 0 ? phase_begin(b) : nullptr; }
+static void gphase_end(pqmc_batch* b, int g, int phase, cudaEvent_t a) {
+  if (g == 0) phase_end(b, phase, a);
+}
+
+// two-way wrap of group g's chains by family pf (the caller flips the parity)
+static int bwrap(pqmc_batch* b, int g, int pf, int time, bool left) {
   pqmc_chain* c0 = b->chains[0];
   const WrapItems& w = c0->wrap[pf];
-  // the descriptors carry family 0's cover; point them at this family's
-  for (auto& h : b->h_desc) {
-    h.wpla = w.d_pla;
-    h.wsites = w.d_sites;
-    h.wdim = w.d_dim;
-  }
-  PQMC_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), sizeof(BDesc) * b->h_desc.size(), cudaMemcpyHostToDevice,
-                            b->stream));
+  const int C = b->g_count[g];
+  const BDesc* D = b->d_desc + b->g_first[g];
+  cudaStream_t st = b->g_stream[g];
   long pairs = (long)w.n_items * w.n_items;
-  dim3 grid((unsigned)((pairs + 127) / 128), (unsigned)b->chains.size());
+  dim3 grid((unsigned)((pairs + 127) / 128), (unsigned)C);
   const int l = left ? 1 : 0;
-  cudaEvent_t tw = phase_begin(b);
+  cudaEvent_t tw = gphase_begin(b, g);
   switch (c0->h_pf_dim[pf]) {
-    case 1: k_bwrap<1><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
-    case 2: k_bwrap<2><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
-    case 3: k_bwrap<3><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
-    default: k_bwrap<4><<<grid, 128, 0, b->stream>>>(b->d_desc, pf, time - 1, l, w.n_items, b->parity); break;
+    case 1: k_bwrap<1><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
+    case 2: k_bwrap<2><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
+    case 3: k_bwrap<3><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
+    default: k_bwrap<4><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
   }
   PQMC_LAUNCHED();
-  phase_end(b, PQMC_PHASE_WRAP, tw);
-  b->parity ^= 1;
+  gphase_end(b, g, PQMC_PHASE_WRAP, tw);
   return PQMC_OK;
 }
 
-static int bupdate(pqmc_batch* b, int pf, int time) {
-  const int C = (int)b->chains.size();
+static int bupdate(pqmc_batch* b, int g, int pf, int time) {
+  const int C = b->g_count[g], c_first = b->g_first[g];
+  const BDesc* Dg = b->d_desc + c_first;
+  int* next = b->d_next + c_first;
+  cudaStream_t st = b->g_stream[g];
   pqmc_chain* c0 = b->chains[0];
   const int npla = c0->h_pf_npla[pf], dim = c0->h_pf_dim[pf];
-  cudaEvent_t tp = phase_begin(b);
-  k_bdraw<<<(C + 63) / 64, 64, 0, b->stream>>>(b->d_desc, C, pf);
+  cudaEvent_t tp = gphase_begin(b, g);
+  k_bdraw<<<(C + 63) / 64, 64, 0, st>>>(Dg, C, pf);
   PQMC_LAUNCHED();
-  k_bprep<<<dim3((npla + 7) / 8, C), 256, 0, b->stream>>>(b->d_desc, pf, time - 1);
+  k_bprep<<<dim3((npla + 7) / 8, C), 256, 0, st>>>(Dg, pf, time - 1);
   PQMC_LAUNCHED();
-  phase_end(b, PQMC_PHASE_PREP, tp);
-  PQMC_CUDA(cudaMemsetAsync(b->d_next, 0, sizeof(int) * C, b->stream));
+  gphase_end(b, g, PQMC_PHASE_PREP, tp);
+  PQMC_CUDA(cudaMemsetAsync(next, 0, sizeof(int) * C, st));
   const int kd = std::max(dim, std::min(b->kd, b->h_desc[0].kmax));
   // enough rounds for the worst case (every proposal accepted)
   const int rounds = (npla * dim + (kd / dim) * dim - 1) / ((kd / dim) * dim);
   const int tiles = ((c0->ns + FB_M - 1) / FB_M) * ((c0->ns + FB_N - 1) / FB_N);
+  const int ns = c0->ns;
+  unsigned char* img = b->d_img ? b->d_img + um_chain_bytes(ns) * c_first : nullptr;
   for (int r = 0; r < rounds; ++r) {
-    const size_t smem = scan_layout(npla, c0->ns, b->h_desc[0].ldp, b->qc, kd).total;
-    cudaEvent_t ts = phase_begin(b);
+    const size_t smem = scan_layout(npla, ns, b->h_desc[0].ldp, b->qc, kd).total;
+    cudaEvent_t ts = gphase_begin(b, g);
     switch (dim) {
-      case 1: k_bscan<1><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
-      case 2: k_bscan<2><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
-      case 3: k_bscan<3><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
-      default: k_bscan<4><<<C, SCAN_THREADS, smem, b->stream>>>(b->d_desc, pf, time - 1, b->parity, kd, b->qc, b->d_next); break;
+      case 1: k_bscan<1><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
+      case 2: k_bscan<2><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
+      case 3: k_bscan<3><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
+      default: k_bscan<4><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
     }
     PQMC_LAUNCHED();
-    phase_end(b, PQMC_PHASE_SCAN, ts);
-    cudaEvent_t tf = phase_begin(b);
-    if (b->flush_mode == 1 && b->d_img && kd <= UM_KP) {
-      const int ns = c0->ns;
+    gphase_end(b, g, PQMC_PHASE_SCAN, ts);
+    cudaEvent_t tf = gphase_begin(b, g);
+    if (b->flush_mode == 1 && img && kd <= UM_KP) {
       const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * (((kd + 15) & ~15) / 8);
-      k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, b->stream>>>(b->d_desc, b->d_img);
+      k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, st>>>(Dg, img);
       PQMC_LAUNCHED();
-      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, b->stream>>>(b->d_desc, b->d_img,
-                                                                                       b->parity);
+      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, st>>>(Dg, img, b->parity);
       PQMC_LAUNCHED();
     } else {
-      k_bflush<<<dim3(tiles, C), 256, 0, b->stream>>>(b->d_desc, b->parity);
+      k_bflush<<<dim3(tiles, C), 256, 0, st>>>(Dg, b->parity);
       PQMC_LAUNCHED();
     }
-    phase_end(b, PQMC_PHASE_FLUSH, tf);
+    gphase_end(b, g, PQMC_PHASE_FLUSH, tf);
   }
   return PQMC_OK;
 }
 
-static int bscratch(pqmc_batch* b, int time, bool forward, int loop) {
-  (void)loop;
-  PQMC_TRY(batch_sync_parity(b));
-  cudaEvent_t tr = phase_begin(b);
-  PQMC_TRY(b->rec.scratch(time, forward));
-  phase_end(b, PQMC_PHASE_RECOMPUTE, tr);
-  return batch_refresh(b);
+// stabilised recompute of group g (the caller flips the parity)
+static int bscratch(pqmc_batch* b, int g, int time, bool forward) {
+  cudaEvent_t tr = gphase_begin(b, g);
+  PQMC_TRY(b->rec[g].scratch(time, forward, b->parity));
+  gphase_end(b, g, PQMC_PHASE_RECOMPUTE, tr);
+  return PQMC_OK;
 }
 
 extern "C" {
@@ -1387,7 +1395,24 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
   PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
-  if (precision == PQMC_PREC_MIXED) PQMC_TRY(b->rec.setup(b->chains, b->stream));
+  // two chain groups on two streams for mixed batches of 16 chains or more
+  b->n_groups = (precision == PQMC_PREC_MIXED && n_chains >= 16) ? 2 : 1;
+  b->g_stream[0] = b->stream;
+  b->g_first[0] = 0;
+  b->g_count[0] = (n_chains + b->n_groups - 1) / b->n_groups;
+  if (b->n_groups == 2) {
+    b->g_first[1] = b->g_count[0];
+    b->g_count[1] = n_chains - b->g_count[0];
+    PQMC_CUDA(cudaStreamCreateWithFlags(&b->g_stream[1], cudaStreamNonBlocking));
+  }
+  PQMC_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  PQMC_CUDA(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+  if (precision == PQMC_PREC_MIXED)
+    for (int g = 0; g < b->n_groups; ++g) {
+      std::vector<pqmc_chain*> sub(b->chains.begin() + b->g_first[g],
+                                   b->chains.begin() + b->g_first[g] + b->g_count[g]);
+      PQMC_TRY(b->rec[g].setup(sub, b->g_stream[g]));
+    }
   PQMC_TRY(batch_refresh(b));
   PQMC_CUDA(cudaStreamSynchronize(b->stream));
   *out = b;
@@ -1411,6 +1436,12 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
   if (b->d_img) cudaFree(b->d_img);
+  if (b->g_stream[1]) {
+    cudaStreamSynchronize(b->g_stream[1]);
+    cudaStreamDestroy(b->g_stream[1]);
+  }
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return PQMC_OK;
@@ -1437,7 +1468,7 @@ int pqmc_batch_init(pqmc_batch* b) {
     for (auto* c : b->chains) PQMC_TRY(pqmc_init_g(c, 1));
     return PQMC_OK;
   }
-  PQMC_TRY(b->rec.init_g());
+  for (int g = 0; g < b->n_groups; ++g) PQMC_TRY(b->rec[g].init_g());
   for (auto* c : b->chains) c->have_g = true;
   return batch_refresh(b);
 }
@@ -1543,23 +1574,42 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
   const dim3 cgrid((unsigned)std::min<long>((ng2 + 255) / 256, 64), (unsigned)b->chains.size());
   k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 1, ng2);
   PQMC_LAUNCHED();
+  // fork: the other group's stream starts after the work queued so far
+  const int NG = b->n_groups;
+  if (NG > 1) {
+    PQMC_CUDA(cudaEventRecord(b->ev_fork, b->stream));
+    PQMC_CUDA(cudaStreamWaitEvent(b->g_stream[1], b->ev_fork, 0));
+  }
   const bool forward = (loop % 2) == 0;
+  const bool upd = c0->M.local_update != 0;
   for (int tc = first_tc; tc < first_tc + n_slices; ++tc) {
     int time;
     if (!forward) {
       time = c0->ntime - tc + 1;
       for (int pf = c0->n_pf - 1; pf >= 0; --pf) {
-        PQMC_TRY(bwrap(b, pf, time, false));
-        if (c0->M.local_update && c0->h_pf_v_exist[pf]) PQMC_TRY(bupdate(b, pf, time));
+        for (int g = 0; g < NG; ++g) PQMC_TRY(bwrap(b, g, pf, time, false));
+        b->parity ^= 1;
+        if (upd && c0->h_pf_v_exist[pf])
+          for (int g = 0; g < NG; ++g) PQMC_TRY(bupdate(b, g, pf, time));
       }
     } else {
       time = tc;
       for (int pf = 0; pf < c0->n_pf; ++pf) {
-        if (c0->M.local_update && c0->h_pf_v_exist[pf]) PQMC_TRY(bupdate(b, pf, time));
-        PQMC_TRY(bwrap(b, pf, time, true));
+        if (upd && c0->h_pf_v_exist[pf])
+          for (int g = 0; g < NG; ++g) PQMC_TRY(bupdate(b, g, pf, time));
+        for (int g = 0; g < NG; ++g) PQMC_TRY(bwrap(b, g, pf, time, true));
+        b->parity ^= 1;
       }
     }
-    if (tc % c0->ngroup == 0) PQMC_TRY(bscratch(b, forward ? time + 1 : time, forward, loop));
+    if (tc % c0->ngroup == 0) {
+      for (int g = 0; g < NG; ++g) PQMC_TRY(bscratch(b, g, forward ? time + 1 : time, forward));
+      b->parity ^= 1;
+    }
+  }
+  // join, then G back to FP64 in the current buffer of every chain
+  if (NG > 1) {
+    PQMC_CUDA(cudaEventRecord(b->ev_join, b->g_stream[1]));
+    PQMC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
   }
   PQMC_TRY(batch_sync_parity(b));
   k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2);

@@ -1003,7 +1003,7 @@ int BatchRecompute::init_g() {
 
 // get_g_scratch_T0 for every chain (each chain's current G is in c->g;
 // the new G is written to c->g_alt and the pointers are swapped)
-int BatchRecompute::scratch(int time, bool forward) {
+int BatchRecompute::scratch(int time, bool forward, int parity) {
   pqmc_chain* c0 = cs[0];
   const int ng = c0->ngroup;
   std::vector<cplx*> X(C), XL(C), D(C), R(C), Gc(C), Gn(C);
@@ -1044,17 +1044,13 @@ int BatchRecompute::scratch(int time, bool forward) {
       R[i] = qblk(cs[i], blk - 1);
     }
   }
+  // the current G is the parity buffer; the new one goes to the other (the
+  // caller flips the parity)
   for (int i = 0; i < C; ++i) {
-    Gc[i] = cs[i]->g;
-    Gn[i] = cs[i]->g_alt;
+    Gc[i] = parity ? cs[i]->g_alt : cs[i]->g;
+    Gn[i] = parity ? cs[i]->g : cs[i]->g_alt;
   }
-  PQMC_TRY(g_and_det(XL, R, Gc, Gn, true, blk, true));   // the mixed sweep keeps G in double-float form
-  for (auto* c : cs) {
-    cplx* t = c->g;
-    c->g = c->g_alt;
-    c->g_alt = t;
-  }
-  return PQMC_OK;
+  return g_and_det(XL, R, Gc, Gn, true, blk, true);   // the mixed sweep keeps G in double-float form
 }
 
 }  // namespace pqmc

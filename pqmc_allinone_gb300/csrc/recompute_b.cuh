@@ -43,7 +43,7 @@ struct BatchRecompute {
   int g_and_det(const std::vector<cplx*>& XL, const std::vector<cplx*>& R, const std::vector<cplx*>& Gcur,
                 const std::vector<cplx*>& Gnew, bool compare, int blk1, bool g_df);
   int propagate(const std::vector<cplx*>& X, int t_from, int t_to, bool forward);
-  int scratch(int time, bool forward);
+  int scratch(int time, bool forward, int parity);   // G buffers of the mixed sweep: current = parity
   int init_g();   // init_g_T0(1) of every chain (needs ntime % ngroup == 0)
 };
 }  // namespace pqmc

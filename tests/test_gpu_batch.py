@@ -116,3 +116,25 @@ def test_tcgen05_flush_matches_mma_sync(L):
         assert np.array_equal(f0, f1)
         assert s0["positive_accept"] == s1["positive_accept"] and s0["positive_accept"] > 0
         assert rel_fro(g1, g0) < 2e-6
+
+
+def test_chain_groups_are_independent():
+    """A mixed batch of 16 chains runs as two groups on two streams; every
+    chain must come out bit-identical to the same chain advanced in a batch
+    of 8 (one group): chains share no data."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(16):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=80 + i)
+        ms.append((m, f, seed_words(800 + i)))
+    res = {}
+    for n in (16, 8):
+        b = PqmcBatch([m for m, _, _ in ms[:n]], [f for _, f, _ in ms[:n]], [w for _, _, w in ms[:n]], precision=1)
+        b.init()
+        b.sweep(1)
+        res[n] = [(c.field(), c.g(), c.state()["ln_cw"]) for c in b.chains]
+        b.close()
+    for k in range(8):
+        f16, g16, l16 = res[16][k]
+        f8, g8, l8 = res[8][k]
+        assert np.array_equal(f16, f8) and np.array_equal(g16, g8) and l16 == l8

@@ -355,7 +355,11 @@ def run_mixed(args, world, rank, local):
         pass
     roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
             "frac": achieved / pk["bf16_tflops_sustained"], "traffic": traffic,
-            "kernel": "k_bflush (rank-K flush G += A B, split-BF16 mma, FP32 accumulate)",
+            "traffic_note": "DRAM bytes of one full-depth flush launch (ncu, profiles/traffic.json), scaled to the "
+                            "chains of this run; achieved averages over all flush launches incl. short last rounds",
+            "kernel": ("k_bsplit + k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "
+                       "in tensor memory)" if (depth <= 64 and (args.flush or tune)) else
+                       "k_bflush (rank-K flush G += A B, mma.sync BF16x3 products, FP32 accumulate)"),
             "algorithmic": "8*Ns^2*dim flop per accepted move (complex GEMM counted once, not the 6 split "
                            "products)", "peak_source": f"{pk['source']} bf16 sustained (timed inside a long step)"}
     total_ms = sum(v[0] for v in phases.values())
@@ -379,7 +383,8 @@ def run_mixed(args, world, rank, local):
     out = {"metric": "sweeps/s @14x14 Lt=1000: batched mixed-prec vs plain FP64 on GB300",
            "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "fp32/bf16 fast path on an FP64 G",
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute",
            "data": "synthetic (x ~ N(0,0.5^2), seeds 3000+i)",
            "config": config_of(args.workload, m, world, C, {"delay_depth": depth, "autotune": tune,
                                                              "flush": "tcgen05" if (depth <= 64 and (args.flush or tune))

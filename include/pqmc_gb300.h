@@ -287,8 +287,17 @@ int pqmc_batch_set_delay(pqmc_batch* batch, int depth);
  * cores with the accumulator in tensor memory (delay depth <= 64; deeper
  * delays use 0), 0 = mma.sync split-BF16 tiles */
 int pqmc_batch_set_flush(pqmc_batch* batch, int mode);
-/* one sweep of every chain (Main_PQMC.f90:99-154), no measurement */
+/* one sweep of every chain (Main_PQMC.f90:99-154); equal-time
+ * measurements only after pqmc_batch_set_measure */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
+/* Equal-time measurement inside batched sweeps with the reference's window
+ * and cadence (loop > warmup, mod(loop-warmup, meas_interval) == 0, time in
+ * ntime/2 +- meas_number; Main_PQMC.f90:142-152).  Every chain needs a
+ * measurement layout.  Finished records accumulate per chain on the host. */
+int pqmc_batch_set_measure(pqmc_batch* batch, int warmup, int meas_interval, int meas_number);
+/* Takes up to `cap` finished records of chain i (oldest first; record width
+ * as pqmc_take_measurement); *n is the number copied. */
+int pqmc_batch_records(pqmc_batch* batch, int i, double* records, int cap, int* n);
 /* Delay-depth autotuner (no reference counterpart): runs n_slices slices
  * of the sweep order per candidate depth, starting at (loop, first_tc) and
  * continuing block after block (these are genuine Monte Carlo steps of every

@@ -180,6 +180,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_sweep": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_set_delay": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_set_flush": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_set_measure": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_records": ([vp, ctypes.c_int, _f64p, ctypes.c_int, _i32p], ctypes.c_int),
         "pqmc_batch_autotune": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, ctypes.c_int, _i32p, _f64p],
                                 ctypes.c_int),
         "pqmc_batch_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),

@@ -49,6 +49,10 @@ __device__ __forceinline__ float2 f2(cplx a) { return make_float2((float)a.x, (f
 __device__ __forceinline__ float2 fm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 fa(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 fsb(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// acc + a*b in four FMAs
+__device__ __forceinline__ float2 fcfma(float2 a, float2 b, float2 acc) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y)));
+}
 
 // ---------------------------------------------------------------------------
 __global__ void k_bdraw(const BDesc* D, int C, int pf) {
@@ -243,14 +247,16 @@ __device__ __forceinline__ float2 wf_det(int dim, const float2* R, int lane) {
   float2 v = make_float2(0.f, 0.f);
   if (dim == 4) {
     if (lane < 6) {
-      const int J[6] = {0, 0, 0, 1, 1, 2}, K[6] = {1, 2, 3, 2, 3, 3};
-      const int L[6] = {2, 1, 1, 0, 0, 0}, Mm[6] = {3, 3, 2, 3, 2, 1};
-      const float sg[6] = {1.f, -1.f, 1.f, 1.f, -1.f, 1.f};
-      int j = J[lane], k = K[lane], l = L[lane], m = Mm[lane];
+      // column pair (j,k) of rows 0,1 and the complementary pair (l,m) of
+      // rows 2,3, packed one hex digit per lane (no local-memory tables)
+      const int sh = 4 * lane;
+      const int j = (0x211000 >> sh) & 15, k = (0x332321 >> sh) & 15;
+      const int l = (0x000112 >> sh) & 15, m = (0x123233 >> sh) & 15;
+      const float sg = ((0x12 >> lane) & 1) ? -1.f : 1.f;
       float2 mi = fsb(fm(R[0 + 4 * j], R[1 + 4 * k]), fm(R[0 + 4 * k], R[1 + 4 * j]));
       float2 co = fsb(fm(R[2 + 4 * l], R[3 + 4 * m]), fm(R[2 + 4 * m], R[3 + 4 * l]));
       float2 t = fm(mi, co);
-      v = make_float2(sg[lane] * t.x, sg[lane] * t.y);
+      v = make_float2(sg * t.x, sg * t.y);
     }
     for (int o = 4; o > 0; o >>= 1) {
       float vx = __shfl_down_sync(0xffffffffu, v.x, o), vy = __shfl_down_sync(0xffffffffu, v.y, o);
@@ -362,7 +368,7 @@ __device__ __forceinline__ void scan_issue(float2* s_stage, uint64_t* s_full, co
   bulk_g2s(dB, B + (size_t)q0 * ldp, bytes, &s_full[st]);
 }
 
-template <int DIM>
+template <int DIM, int RPT>
 __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int t, int parity, int kd, int qc,
                                                          int* next_p) {
   constexpr int NW = SCAN_THREADS / 32;
@@ -441,7 +447,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
         if (act) {
           float2 a = make_float2(i == j ? 1.f : 0.f, 0.f);
 #pragma unroll
-          for (int k = 0; k < dim; ++k) a = fa(a, fm(ge[i + dim * k], de[k + dim * j]));
+          for (int k = 0; k < dim; ++k) a = fcfma(ge[i + dim * k], de[k + dim * j], a);
           s_R[warp][lane] = a;
         }
         __syncwarp();
@@ -475,7 +481,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
         const float2* de = s_delta + 16 * p;
         float2 a = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < dim; ++k) a = fa(a, fm(de[i + dim * k], s_R[warp][k + dim * j]));
+        for (int k = 0; k < dim; ++k) a = fcfma(de[i + dim * k], s_R[warp][k + dim * j], a);
         s_T[lane] = a;
       }
       if (lane == 0) {
@@ -490,21 +496,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       fence_proxy_async_global();   // this round's panel columns were written by generic stores
       for (int c = 0; c < nch && c < SCAN_NSTAGE; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
     }
-    // rows of G at the accepted sites; then warm L2 with the next plaquette's
-    float2 gm[SCAN_RPT][dim], bl[SCAN_RPT][dim];
+    // rows of G at the accepted sites, loaded now and added after the panel
+    // loop (their latency overlaps it); then warm L2 with the next plaquette's
+    float4 gcol[RPT][dim], grow[RPT][dim];
+    float2 gm[RPT][dim], bl[RPT][dim];
 #pragma unroll
-    for (int k = 0; k < SCAN_RPT; ++k) {
+    for (int k = 0; k < RPT; ++k) {
       const int r = tid + k * SCAN_THREADS;
 #pragma unroll
       for (int m = 0; m < dim; ++m) {
-        gm[k][m] = r < ns ? dg_f2(G[r + (size_t)ns * S[m]]) : make_float2(0.f, 0.f);
-        bl[k][m] = r < ns ? dg_f2(G[S[m] + (size_t)ns * r]) : make_float2(0.f, 0.f);
+        gcol[k][m] = r < ns ? G[r + (size_t)ns * S[m]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        grow[k][m] = r < ns ? G[S[m] + (size_t)ns * r] : make_float4(0.f, 0.f, 0.f, 0.f);
+        gm[k][m] = make_float2(0.f, 0.f);
+        bl[k][m] = make_float2(0.f, 0.f);
       }
     }
     if (p + 1 < npla) {
       const int* Sn = s_site + 4 * (p + 1);
 #pragma unroll
-      for (int k = 0; k < SCAN_RPT; ++k) {
+      for (int k = 0; k < RPT; ++k) {
         const int r = tid + k * SCAN_THREADS;
         if (r < ns)
 #pragma unroll
@@ -530,14 +540,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
           as[m] = cA[(size_t)qq * ldp + S[m]];
         }
 #pragma unroll
-        for (int k = 0; k < SCAN_RPT; ++k) {
+        for (int k = 0; k < RPT; ++k) {
           const int r = tid + k * SCAN_THREADS;
           if (r < ns) {
             const float2 ar = cA[(size_t)qq * ldp + r], bc = cB[(size_t)qq * ldp + r];
 #pragma unroll
             for (int m = 0; m < dim; ++m) {
-              gm[k][m] = fa(gm[k][m], fm(ar, bs[m]));
-              bl[k][m] = fa(bl[k][m], fm(as[m], bc));
+              gm[k][m] = fcfma(ar, bs[m], gm[k][m]);
+              bl[k][m] = fcfma(as[m], bc, bl[k][m]);
             }
           }
         }
@@ -552,14 +562,19 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     }
     if (nch == 0) __syncthreads();   // s_T visible
 #pragma unroll
-    for (int k = 0; k < SCAN_RPT; ++k) {
+    for (int k = 0; k < RPT; ++k) {
       const int r = tid + k * SCAN_THREADS;
       if (r >= ns) continue;
+#pragma unroll
+      for (int m = 0; m < dim; ++m) {
+        gm[k][m] = fa(gm[k][m], dg_f2(gcol[k][m]));
+        bl[k][m] = fa(bl[k][m], dg_f2(grow[k][m]));
+      }
 #pragma unroll
       for (int l = 0; l < dim; ++l) {
         float2 a = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int m = 0; m < dim; ++m) a = fa(a, fm(gm[k][m], s_T[m + dim * l]));
+        for (int m = 0; m < dim; ++m) a = fcfma(gm[k][m], s_T[m + dim * l], a);
         float2 bv = make_float2(-bl[k][l].x, -bl[k][l].y);
         if (r == S[l]) bv.x += 1.f;
         A[(size_t)(K + l) * ldp + r] = a;
@@ -575,7 +590,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       const int si = s_site[4 * pq + k % dim], sj = s_site[4 * pq + k / dim];
       float2 a = s_geff[16 * pq + k];
 #pragma unroll
-      for (int l = 0; l < dim; ++l) a = fa(a, fm(s_newA[(size_t)l * ns + si], s_newB[(size_t)l * ns + sj]));
+      for (int l = 0; l < dim; ++l) a = fcfma(s_newA[(size_t)l * ns + si], s_newB[(size_t)l * ns + sj], a);
       s_geff[16 * pq + k] = a;
     }
     K += dim;
@@ -1083,8 +1098,8 @@ __global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, in
 
 // G of every chain converted in place between FP64 complex (at rest) and the
 // double-float float4 form the mixed sweep works on
-__global__ void k_gconv(const BDesc* D, int to_df, long n) {
-  cplx* G = D[blockIdx.y].g;
+__global__ void k_gconv(const BDesc* D, int to_df, long n, int parity) {
+  cplx* G = parity ? D[blockIdx.y].g_alt : D[blockIdx.y].g;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
     if (to_df) {
       const cplx v = G[e];
@@ -1132,6 +1147,9 @@ struct pqmc_batch {
   cudaStream_t g_stream[2] = {nullptr, nullptr};
   pqmc::BatchRecompute rec[2];
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // equal-time measurement inside batched sweeps (ms_begin_measure semantics)
+  int meas_on = 0, meas_warmup = 0, meas_interval = 1, meas_number = 0;
+  std::vector<std::vector<double>> records;   // finished records per chain
 };
 
 using namespace pqmc;
@@ -1259,12 +1277,15 @@ static int bupdate(pqmc_batch* b, int g, int pf, int time) {
   for (int r = 0; r < rounds; ++r) {
     const size_t smem = scan_layout(npla, ns, b->h_desc[0].ldp, b->qc, kd).total;
     cudaEvent_t ts = gphase_begin(b, g);
+    const bool one = ns <= SCAN_THREADS;
+#define PQMC_SCAN(DM, R) k_bscan<DM, R><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next)
     switch (dim) {
-      case 1: k_bscan<1><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
-      case 2: k_bscan<2><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
-      case 3: k_bscan<3><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
-      default: k_bscan<4><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next); break;
+      case 1: if (one) PQMC_SCAN(1, 1); else PQMC_SCAN(1, 2); break;
+      case 2: if (one) PQMC_SCAN(2, 1); else PQMC_SCAN(2, 2); break;
+      case 3: if (one) PQMC_SCAN(3, 1); else PQMC_SCAN(3, 2); break;
+      default: if (one) PQMC_SCAN(4, 1); else PQMC_SCAN(4, 2); break;
     }
+#undef PQMC_SCAN
     PQMC_LAUNCHED();
     gphase_end(b, g, PQMC_PHASE_SCAN, ts);
     cudaEvent_t tf = gphase_begin(b, g);
@@ -1288,6 +1309,57 @@ static int bscratch(pqmc_batch* b, int g, int time, bool forward) {
   cudaEvent_t tr = gphase_begin(b, g);
   PQMC_TRY(b->rec[g].scratch(time, forward, b->parity));
   gphase_end(b, g, PQMC_PHASE_RECOMPUTE, tr);
+  return PQMC_OK;
+}
+
+// ms_begin_measure for every chain at `time` (src/mod_meas.f90:729-763): the
+// groups join, the current G goes back to FP64 for the measurement kernels of
+// each chain, and returns to double-float afterwards
+static int batch_measure(pqmc_batch* b, int time, bool forward) {
+  pqmc_chain* c0 = b->chains[0];
+  const int NG = b->n_groups, half = c0->ntime / 2, mn = b->meas_number;
+  if (NG > 1) {
+    PQMC_CUDA(cudaEventRecord(b->ev_join, b->g_stream[1]));
+    PQMC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
+  }
+  const long ng2 = (long)c0->ns * c0->ns;
+  const dim3 cgrid((unsigned)std::min<long>((ng2 + 255) / 256, 64), (unsigned)b->chains.size());
+  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2, b->parity);
+  PQMC_LAUNCHED();
+  PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  const bool last = (forward && time == half + mn) || (!forward && time == half - mn);
+  for (size_t i = 0; i < b->chains.size(); ++i) {
+    pqmc_chain* c = b->chains[i];
+    if (!c->have_meas) continue;
+    cplx* gsave = c->g;
+    c->g = b->parity ? c->g_alt : c->g;
+    int st = do_measure(c, time);
+    if (st == PQMC_OK && last) {
+      const int W = PQMC_N_SCALAR + 2 * PQMC_N_FIELD * c->n_cell;
+      st = do_finish_record(c, mn);
+      if (st == PQMC_OK) {
+        std::vector<double>& rec = b->records[i];
+        const size_t at = rec.size();
+        rec.resize(at + 2 * (size_t)W);
+        if (cudaMemcpyAsync(rec.data() + at, c->m_acc, sizeof(cplx) * W, cudaMemcpyDeviceToHost, c->stream) !=
+                cudaSuccess ||
+            cudaMemsetAsync(c->m_acc, 0, sizeof(cplx) * W, c->stream) != cudaSuccess)
+          st = PQMC_ERR_CUDA;
+      }
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess && st == PQMC_OK) st = PQMC_ERR_CUDA;
+    c->g = gsave;
+    if (st != PQMC_OK) {
+      set_error("batch measurement failed on chain %zu", i);
+      return st;
+    }
+  }
+  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 1, ng2, b->parity);
+  PQMC_LAUNCHED();
+  if (NG > 1) {
+    PQMC_CUDA(cudaEventRecord(b->ev_fork, b->stream));
+    PQMC_CUDA(cudaStreamWaitEvent(b->g_stream[1], b->ev_fork, 0));
+  }
   return PQMC_OK;
 }
 
@@ -1351,10 +1423,10 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       return PQMC_ERR_ARG;
     }
     b->qc = qc;
-    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-    PQMC_CUDA(cudaFuncSetAttribute(k_bscan<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+#define PQMC_SMEM(DM, R) PQMC_CUDA(cudaFuncSetAttribute(k_bscan<DM, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need))
+    PQMC_SMEM(1, 1); PQMC_SMEM(2, 1); PQMC_SMEM(3, 1); PQMC_SMEM(4, 1);
+    PQMC_SMEM(1, 2); PQMC_SMEM(2, 2); PQMC_SMEM(3, 2); PQMC_SMEM(4, 2);
+#undef PQMC_SMEM
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_err, sizeof(int)));
   PQMC_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
@@ -1544,6 +1616,39 @@ int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, con
   return PQMC_OK;
 }
 
+int pqmc_batch_set_measure(pqmc_batch* b, int warmup, int meas_interval, int meas_number) {
+  if (!b || meas_interval < 1 || meas_number < 0) { set_error("batch_set_measure: bad arguments"); return PQMC_ERR_ARG; }
+  pqmc_chain* c0 = b->chains[0];
+  if (c0->ntime / 2 - meas_number < 1 || c0->ntime / 2 + meas_number > c0->ntime - 1) {
+    set_error("measurement window ntime/2 +- %d leaves 1..ntime-1", meas_number);
+    return PQMC_ERR_ARG;
+  }
+  for (auto* c : b->chains)
+    if (!c->have_meas) { set_error("batch_set_measure: a chain has no measurement layout"); return PQMC_ERR_STATE; }
+  b->meas_on = 1;
+  b->meas_warmup = warmup;
+  b->meas_interval = meas_interval;
+  b->meas_number = meas_number;
+  b->records.assign(b->chains.size(), std::vector<double>());
+  return PQMC_OK;
+}
+
+int pqmc_batch_records(pqmc_batch* b, int i, double* out, int cap, int* n) {
+  if (!b || i < 0 || i >= (int)b->chains.size() || !n || (cap > 0 && !out)) {
+    set_error("batch_records: bad arguments");
+    return PQMC_ERR_ARG;
+  }
+  if (i >= (int)b->records.size()) { *n = 0; return PQMC_OK; }
+  pqmc_chain* c = b->chains[i];
+  const size_t w = 2 * (size_t)(PQMC_N_SCALAR + 2 * PQMC_N_FIELD * c->n_cell);
+  std::vector<double>& rec = b->records[i];
+  const int have = (int)(rec.size() / w), take = std::min(have, cap);
+  if (take > 0) memcpy(out, rec.data(), sizeof(double) * w * take);
+  rec.erase(rec.begin(), rec.begin() + (size_t)take * w);
+  *n = take;
+  return PQMC_OK;
+}
+
 int pqmc_batch_chain(pqmc_batch* b, int i, pqmc_chain** chain) {
   if (!b || !chain || i < 0 || i >= (int)b->chains.size()) { set_error("batch_chain: bad index"); return PQMC_ERR_ARG; }
   *chain = b->chains[i];
@@ -1572,7 +1677,7 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
   PQMC_TRY(batch_refresh(b));
   const long ng2 = (long)c0->ns * c0->ns;
   const dim3 cgrid((unsigned)std::min<long>((ng2 + 255) / 256, 64), (unsigned)b->chains.size());
-  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 1, ng2);
+  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 1, ng2, 0);
   PQMC_LAUNCHED();
   // fork: the other group's stream starts after the work queued so far
   const int NG = b->n_groups;
@@ -1605,6 +1710,10 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
       for (int g = 0; g < NG; ++g) PQMC_TRY(bscratch(b, g, forward ? time + 1 : time, forward));
       b->parity ^= 1;
     }
+    const int half = c0->ntime / 2;
+    if (b->meas_on && loop > b->meas_warmup && ((loop - b->meas_warmup) % b->meas_interval) == 0 &&
+        time >= half - b->meas_number && time <= half + b->meas_number)
+      PQMC_TRY(batch_measure(b, time, forward));
   }
   // join, then G back to FP64 in the current buffer of every chain
   if (NG > 1) {
@@ -1612,7 +1721,7 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
     PQMC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
   }
   PQMC_TRY(batch_sync_parity(b));
-  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2);
+  k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2, 0);
   PQMC_LAUNCHED();
   int err = 0;
   PQMC_CUDA(cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));

@@ -287,6 +287,20 @@ class PqmcBatch:
                                                       ms.ctypes.data_as(_f64p)), "pqmc_batch_autotune")
         return int(best[0]), {int(k): float(v) for k, v in zip(cand, ms)}
 
+    def set_measure(self, warmup: int, meas_interval: int = 1, meas_number: int = 0):
+        """Equal-time measurements in batched sweeps (chains built with meas=True)."""
+        check(self.lib, self.lib.pqmc_batch_set_measure(self.h, warmup, meas_interval, meas_number),
+              "pqmc_batch_set_measure")
+
+    def records(self, i: int, cap: int = 1024) -> np.ndarray:
+        """Finished measurement records of chain i, complex (n, width)."""
+        w = record_width(self.models[i])
+        out = np.zeros((cap, 2 * w))
+        n = np.zeros(1, dtype=np.int32)
+        check(self.lib, self.lib.pqmc_batch_records(self.h, i, out.ctypes.data_as(_f64p), cap,
+                                                     n.ctypes.data_as(_i32p)), "pqmc_batch_records")
+        return out[:n[0]].view(np.complex128)
+
     def set_flush(self, mode: int):
         """1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush."""
         check(self.lib, self.lib.pqmc_batch_set_flush(self.h, mode), "pqmc_batch_set_flush")

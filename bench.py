@@ -327,6 +327,7 @@ def run_mixed(args, world, rank, local):
     launches = kernel_launches() - n0
     phases = b.timing()
     b.set_timing(False)
+    binfo = b.info()
     t_step = max_over_ranks(world, ev0.elapsed_time(ev1) / 1000.0 / args.steps)
     per_gpu = C * (m.ngroup / m.ntime) / t_step
     value = world * per_gpu
@@ -386,9 +387,7 @@ def run_mixed(args, world, rank, local):
            "scaling": "weak", "vs_baseline": None,
            "dtype": "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute",
            "data": "synthetic (x ~ N(0,0.5^2), seeds 3000+i)",
-           "config": config_of(args.workload, m, world, C, {"delay_depth": depth, "autotune": tune,
-                                                             "flush": "tcgen05" if (depth <= 64 and (args.flush or tune))
-                                                             else "mma.sync"}),
+           "config": config_of(args.workload, m, world, C, {"autotune": tune, **binfo}),
            "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "clocks": clocks,
            "cpu_baseline": cb, "plain_fp64": plain,
            "speedup_vs_plain_fp64": (per_gpu / plain["value"]) if plain else None,

@@ -313,8 +313,14 @@ int pqmc_batch_sweep_slices(pqmc_batch* batch, int loop, int first_tc, int n_sli
  * (the fields set per chain first).  Mixed batches build the Q/D strings of
  * all chains together (double-float propagation + CholeskyQR2). */
 int pqmc_batch_init(pqmc_batch* batch);
-/* the CUDA stream every batched kernel runs on (cudaStream_t) */
+/* the CUDA stream of the batch (cudaStream_t): a batched call starts after
+ * the work queued on it and the call's last work is ordered before later
+ * work on it (the chain groups run on their own streams in between) */
 int pqmc_batch_stream(pqmc_batch* batch, void** stream);
+/* info[5] = {chains, chain groups (streams), delay depth, flush engine,
+ * precision}; the groups default to one per 16 chains (at most 4) and can
+ * be set with the environment variable PQMC_BATCH_GROUPS (1..4) at creation */
+int pqmc_batch_info(pqmc_batch* batch, int* info);
 /* CUDA-event timers per phase of the mixed family step; set_timing clears
  * the totals, get_timing returns PQMC_N_PHASES totals (ms) and counts. */
 #define PQMC_PHASE_PREP      0   /* ran2 draws + proposal data           */

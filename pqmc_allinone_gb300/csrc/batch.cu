@@ -17,6 +17,7 @@
 // FP64 stays in G itself, in the 4x4 ratio / T = Delta R^-1 of accepted
 // moves, and in the stabilised recompute and log-weight.
 #include <cuda_bf16.h>
+#include <stdlib.h>
 #include <string.h>
 #include <vector>
 #include "chain.cuh"
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       for (int c = 0; c < nch && c < SCAN_NSTAGE; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
     }
     // rows of G at the accepted sites, loaded now and added after the panel
-    // loop (their latency overlaps it); then warm L2 with the next plaquette's
+    // loop (their latency overlaps it)
     float4 gcol[RPT][dim], grow[RPT][dim];
     float2 gm[RPT][dim], bl[RPT][dim];
 #pragma unroll
@@ -509,19 +510,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
         grow[k][m] = r < ns ? G[S[m] + (size_t)ns * r] : make_float4(0.f, 0.f, 0.f, 0.f);
         gm[k][m] = make_float2(0.f, 0.f);
         bl[k][m] = make_float2(0.f, 0.f);
-      }
-    }
-    if (p + 1 < npla) {
-      const int* Sn = s_site + 4 * (p + 1);
-#pragma unroll
-      for (int k = 0; k < RPT; ++k) {
-        const int r = tid + k * SCAN_THREADS;
-        if (r < ns)
-#pragma unroll
-          for (int m = 0; m < dim; ++m) {
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(G + r + (size_t)ns * Sn[m]));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(G + Sn[m] + (size_t)ns * r));
-          }
       }
     }
     for (int c = 0; c < nch; ++c) {
@@ -1142,11 +1130,12 @@ struct pqmc_batch {
   cudaStream_t stream = nullptr;   // the stream of group 0, the batch's public stream
   // chain groups: each group has its own stream and recompute workspace, so
   // one group's latency-bound scan overlaps the other's flush and recompute
+  static constexpr int MAX_GROUPS = 4;
   int n_groups = 1;
-  int g_first[2] = {0, 0}, g_count[2] = {0, 0};
-  cudaStream_t g_stream[2] = {nullptr, nullptr};
-  pqmc::BatchRecompute rec[2];
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int g_first[MAX_GROUPS] = {}, g_count[MAX_GROUPS] = {};
+  cudaStream_t g_stream[MAX_GROUPS] = {};
+  pqmc::BatchRecompute rec[MAX_GROUPS];
+  cudaEvent_t ev_fork = nullptr, ev_join[MAX_GROUPS] = {};
   // equal-time measurement inside batched sweeps (ms_begin_measure semantics)
   int meas_on = 0, meas_warmup = 0, meas_interval = 1, meas_number = 0;
   std::vector<std::vector<double>> records;   // finished records per chain
@@ -1312,16 +1301,29 @@ static int bscratch(pqmc_batch* b, int g, int time, bool forward) {
   return PQMC_OK;
 }
 
+// every group stream waits for the work queued on the batch stream so far
+static int groups_fork(pqmc_batch* b) {
+  if (b->n_groups < 2) return PQMC_OK;
+  PQMC_CUDA(cudaEventRecord(b->ev_fork, b->stream));
+  for (int g = 1; g < b->n_groups; ++g) PQMC_CUDA(cudaStreamWaitEvent(b->g_stream[g], b->ev_fork, 0));
+  return PQMC_OK;
+}
+// the batch stream waits for every group stream
+static int groups_join(pqmc_batch* b) {
+  for (int g = 1; g < b->n_groups; ++g) {
+    PQMC_CUDA(cudaEventRecord(b->ev_join[g], b->g_stream[g]));
+    PQMC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join[g], 0));
+  }
+  return PQMC_OK;
+}
+
 // ms_begin_measure for every chain at `time` (src/mod_meas.f90:729-763): the
 // groups join, the current G goes back to FP64 for the measurement kernels of
 // each chain, and returns to double-float afterwards
 static int batch_measure(pqmc_batch* b, int time, bool forward) {
   pqmc_chain* c0 = b->chains[0];
-  const int NG = b->n_groups, half = c0->ntime / 2, mn = b->meas_number;
-  if (NG > 1) {
-    PQMC_CUDA(cudaEventRecord(b->ev_join, b->g_stream[1]));
-    PQMC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
-  }
+  const int half = c0->ntime / 2, mn = b->meas_number;
+  PQMC_TRY(groups_join(b));
   const long ng2 = (long)c0->ns * c0->ns;
   const dim3 cgrid((unsigned)std::min<long>((ng2 + 255) / 256, 64), (unsigned)b->chains.size());
   k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2, b->parity);
@@ -1356,11 +1358,7 @@ static int batch_measure(pqmc_batch* b, int time, bool forward) {
   }
   k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 1, ng2, b->parity);
   PQMC_LAUNCHED();
-  if (NG > 1) {
-    PQMC_CUDA(cudaEventRecord(b->ev_fork, b->stream));
-    PQMC_CUDA(cudaStreamWaitEvent(b->g_stream[1], b->ev_fork, 0));
-  }
-  return PQMC_OK;
+  return groups_fork(b);
 }
 
 extern "C" {
@@ -1468,17 +1466,24 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
   PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
   // two chain groups on two streams for mixed batches of 16 chains or more
-  b->n_groups = (precision == PQMC_PREC_MIXED && n_chains >= 16) ? 2 : 1;
+  // chain groups: PQMC_BATCH_GROUPS (1..4) when set, else 2 for 16 chains or more
+  {
+    int ng = precision == PQMC_PREC_MIXED ? n_chains / 16 : 1;
+    const char* env = getenv("PQMC_BATCH_GROUPS");
+    if (env && precision == PQMC_PREC_MIXED) ng = atoi(env);
+    ng = std::max(1, std::min(std::min(ng, (int)pqmc_batch::MAX_GROUPS), n_chains));
+    b->n_groups = ng;
+  }
   b->g_stream[0] = b->stream;
-  b->g_first[0] = 0;
-  b->g_count[0] = (n_chains + b->n_groups - 1) / b->n_groups;
-  if (b->n_groups == 2) {
-    b->g_first[1] = b->g_count[0];
-    b->g_count[1] = n_chains - b->g_count[0];
-    PQMC_CUDA(cudaStreamCreateWithFlags(&b->g_stream[1], cudaStreamNonBlocking));
+  for (int g = 0, first = 0; g < b->n_groups; ++g) {
+    const int cnt = (n_chains - first) / (b->n_groups - g);
+    b->g_first[g] = first;
+    b->g_count[g] = cnt;
+    first += cnt;
+    if (g > 0) PQMC_CUDA(cudaStreamCreateWithFlags(&b->g_stream[g], cudaStreamNonBlocking));
+    PQMC_CUDA(cudaEventCreateWithFlags(&b->ev_join[g], cudaEventDisableTiming));
   }
   PQMC_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
-  PQMC_CUDA(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
   if (precision == PQMC_PREC_MIXED)
     for (int g = 0; g < b->n_groups; ++g) {
       std::vector<pqmc_chain*> sub(b->chains.begin() + b->g_first[g],
@@ -1508,12 +1513,14 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
   if (b->d_img) cudaFree(b->d_img);
-  if (b->g_stream[1]) {
-    cudaStreamSynchronize(b->g_stream[1]);
-    cudaStreamDestroy(b->g_stream[1]);
-  }
+  for (int g = 1; g < pqmc_batch::MAX_GROUPS; ++g)
+    if (b->g_stream[g]) {
+      cudaStreamSynchronize(b->g_stream[g]);
+      cudaStreamDestroy(b->g_stream[g]);
+    }
+  for (int g = 0; g < pqmc_batch::MAX_GROUPS; ++g)
+    if (b->ev_join[g]) cudaEventDestroy(b->ev_join[g]);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
-  if (b->ev_join) cudaEventDestroy(b->ev_join);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return PQMC_OK;
@@ -1565,6 +1572,16 @@ int pqmc_batch_get_timing(pqmc_batch* b, double* ms, long long* launches) {
     ms[k] = b->phase_ms[k];
     launches[k] = b->phase_n[k];
   }
+  return PQMC_OK;
+}
+
+int pqmc_batch_info(pqmc_batch* b, int* info) {
+  if (!b || !info) { set_error("batch_info: null argument"); return PQMC_ERR_ARG; }
+  info[0] = (int)b->chains.size();
+  info[1] = b->n_groups;
+  info[2] = b->kd;
+  info[3] = b->flush_mode;
+  info[4] = b->precision;
   return PQMC_OK;
 }
 
@@ -1681,10 +1698,7 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
   PQMC_LAUNCHED();
   // fork: the other group's stream starts after the work queued so far
   const int NG = b->n_groups;
-  if (NG > 1) {
-    PQMC_CUDA(cudaEventRecord(b->ev_fork, b->stream));
-    PQMC_CUDA(cudaStreamWaitEvent(b->g_stream[1], b->ev_fork, 0));
-  }
+  PQMC_TRY(groups_fork(b));
   const bool forward = (loop % 2) == 0;
   const bool upd = c0->M.local_update != 0;
   for (int tc = first_tc; tc < first_tc + n_slices; ++tc) {
@@ -1716,10 +1730,7 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
       PQMC_TRY(batch_measure(b, time, forward));
   }
   // join, then G back to FP64 in the current buffer of every chain
-  if (NG > 1) {
-    PQMC_CUDA(cudaEventRecord(b->ev_join, b->g_stream[1]));
-    PQMC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
-  }
+  PQMC_TRY(groups_join(b));
   PQMC_TRY(batch_sync_parity(b));
   k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2, 0);
   PQMC_LAUNCHED();

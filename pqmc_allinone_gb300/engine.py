@@ -259,6 +259,12 @@ class PqmcBatch:
         check(self.lib, self.lib.pqmc_batch_stream(self.h, ctypes.byref(s)), "pqmc_batch_stream")
         return int(s.value or 0)
 
+    def info(self) -> dict:
+        v = np.zeros(5, dtype=np.int32)
+        check(self.lib, self.lib.pqmc_batch_info(self.h, v.ctypes.data_as(_i32p)), "pqmc_batch_info")
+        return {"chains": int(v[0]), "groups": int(v[1]), "delay_depth": int(v[2]),
+                "flush": "tcgen05" if v[3] == 1 else "mma.sync", "precision": int(v[4])}
+
     PHASES = ("prep", "scan", "flush", "wrap", "recompute")
 
     def set_timing(self, enable: bool):

@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="c4_mixed", choices=["c4_mixed", "c2_fp64", "small"])
+    p.add_argument("--workload", default="c4_mixed", choices=["c4_mixed", "c2_fp64", "small", "c5_adjoint"])
     p.add_argument("--chains", type=int, default=0, help="chains per GPU of the mixed batch (default 64)")
     p.add_argument("--delay", type=int, default=0,
                    help="delay depth of the mixed batch (0: chosen by the autotuner during warm-up)")
@@ -454,6 +454,50 @@ def run_plain_headline(args, world, rank, local):
     print(json.dumps(out))
 
 
+def run_adjoint(args, world, rank, local):
+    """--workload c5_adjoint: forward and hand-written adjoint of the projector
+    log-weight log det(P^H B(Lt..1) P) for 32 chains of 10x10 SOC (Ns=200),
+    Lt=400, through the torch.autograd.Function; gradients/s."""
+    import torch
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.autograd import log_weight
+    from pqmc_allinone_gb300.engine import PqmcChain, kernel_launches
+    from pqmc_allinone_gb300.rng import seed_words
+    torch.cuda.set_device(local)
+    spec = M.epsocz_spec(10, lam=0.8, alpha=0.3, ntime=400, ngroup=10, filling=0.5, jump_distance=0.5)
+    m = M.build_model(spec, twist_seed=11, twist=1e-3)
+    B = args.chains or 32
+    fields = [M.field_gaussian(m, 5000 + i + 1000 * rank) for i in range(B)]
+    chains = [PqmcChain(m, field=f, rng_words=seed_words(5000 + i)) for i, f in enumerate(fields)]
+    x = torch.tensor(np.stack(fields), dtype=torch.float64, device="cuda", requires_grad=True)
+
+    def step():
+        x.grad = None
+        w = log_weight(x, chains)
+        w.sum().backward()
+        return w
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    n0 = kernel_launches()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    dt = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
+    if rank != 0:
+        return
+    out = {"metric": "log-weight gradients/s (forward + adjoint) @10x10 Lt=400", "value": world * B / dt,
+           "unit": "chain-gradients/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": dt * 1000.0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "c128", "data": "synthetic (x ~ N(0,0.5^2), seeds 5000+i)",
+           "config": {"workload": f"10x10 SOC EPSOCZ, Lt=400, {B} chains, checkpoint every ngroup=10 slices",
+                      "ns": m.ns, "nelec": m.nelec, "ntime": m.ntime, "chains": B},
+           "gpu_launches": int(kernel_launches() - n0), "roofline": None, "cpu_baseline": None, "e2e": None}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -463,6 +507,8 @@ def main():
     world, rank, local = dist_setup()
     if args.workload == "c2_fp64":
         run_plain_headline(args, world, rank, local)
+    elif args.workload == "c5_adjoint":
+        run_adjoint(args, world, rank, local)
     else:
         run_mixed(args, world, rank, local)
 

@@ -269,26 +269,25 @@ __device__ __forceinline__ float2 wf_det(int dim, const float2* R, int lane) {
   return make_float2(__shfl_sync(0xffffffffu, v.x, 0), __shfl_sync(0xffffffffu, v.y, 0));
 }
 
-// R <- R^-1 in place (shared, column-major): adjugate over 16 lanes for dim 4,
-// lane-0 Gauss-Jordan otherwise
+// R <- R^-1 in place (shared, column-major): adjugate over 16 lanes for dim 4
+// (the complementary row/column triples formed branch-free, one reciprocal
+// of |det|^2 per lane), lane-0 Gauss-Jordan otherwise
 __device__ __forceinline__ void wf_inverse(int dim, float2* R, float2 det, int lane) {
   if (dim == 4) {
     float2 cof = make_float2(0.f, 0.f);
     const int i = lane & 3, j = lane >> 2;
     if (lane < 16) {
-      int r[3], c[3], n = 0;
-      for (int k = 0; k < 4; ++k)
-        if (k != i) r[n++] = k;
-      n = 0;
-      for (int k = 0; k < 4; ++k)
-        if (k != j) c[n++] = k;
-#define S(a, b) R[r[a] + 4 * c[b]]
-      cof = fa(fsb(fm(S(0, 0), fsb(fm(S(1, 1), S(2, 2)), fm(S(1, 2), S(2, 1)))),
-                   fm(S(0, 1), fsb(fm(S(1, 0), S(2, 2)), fm(S(1, 2), S(2, 0))))),
-               fm(S(0, 2), fsb(fm(S(1, 0), S(2, 1)), fm(S(1, 1), S(2, 0)))));
-#undef S
+      // rows other than i and columns other than j, ascending
+      const int r0 = i == 0 ? 1 : 0, r1 = i <= 1 ? 2 : 1, r2 = i <= 2 ? 3 : 2;
+      const int c0 = j == 0 ? 1 : 0, c1 = j <= 1 ? 2 : 1, c2 = j <= 2 ? 3 : 2;
+      const float2 a00 = R[r0 + 4 * c0], a01 = R[r0 + 4 * c1], a02 = R[r0 + 4 * c2];
+      const float2 a10 = R[r1 + 4 * c0], a11 = R[r1 + 4 * c1], a12 = R[r1 + 4 * c2];
+      const float2 a20 = R[r2 + 4 * c0], a21 = R[r2 + 4 * c1], a22 = R[r2 + 4 * c2];
+      cof = fa(fsb(fm(a00, fsb(fm(a11, a22), fm(a12, a21))), fm(a01, fsb(fm(a10, a22), fm(a12, a20)))),
+               fm(a02, fsb(fm(a10, a21), fm(a11, a20))));
       if ((i + j) & 1) cof = make_float2(-cof.x, -cof.y);
-      cof = fm(cof, fdiv1(det));
+      const float rn = __frcp_rn(det.x * det.x + det.y * det.y);   // 1/det = conj(det)/|det|^2
+      cof = fm(cof, make_float2(det.x * rn, -det.y * rn));
     }
     __syncwarp();
     if (lane < 16) R[j + 4 * i] = cof;

@@ -16,7 +16,9 @@
 //             (A-I)(G B) + G (B-I) added to the FP64 G
 // FP64 stays in G itself, in the 4x4 ratio / T = Delta R^-1 of accepted
 // moves, and in the stabilised recompute and log-weight.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 #include <stdlib.h>
 #include <string.h>
 #include <vector>
@@ -44,6 +46,11 @@ struct BDesc {
   PlaqPre* pre;
   DevScalars* sc;
   int* kcount;
+  // TMA tensor maps over the two G buffers (double-float, Ns rows x Ns
+  // columns, a row read as nrb boxes of rb columns)
+  const CUtensorMap* tm_g;
+  const CUtensorMap* tm_galt;
+  int rb, nrb;
 };
 
 __device__ __forceinline__ float2 f2(cplx a) { return make_float2((float)a.x, (float)a.y); }
@@ -329,6 +336,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                : "memory");
 }
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+// 2-D tiled TMA load of the box at (x, y) of the tensor map into shared memory
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_addr(b))
+      : "memory");
+}
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 constexpr int SCAN_NSTAGE = 3;   // panel chunks in flight
@@ -338,11 +353,13 @@ __host__ __device__ __forceinline__ size_t al16(size_t b) { return (b + 15) & ~(
 
 // dynamic shared memory of k_bscan (byte offsets, 16-byte aligned pieces)
 struct ScanLayout {
-  size_t stage, delta, geff, newA, newB, thr, site, accp, accd, total;
+  size_t rows, stage, delta, geff, newA, newB, thr, site, accp, accd, total;
 };
-__host__ __device__ __forceinline__ ScanLayout scan_layout(int npla, int ns, int ldp, int qc, int kd) {
+// rows first: the TMA tile destination wants a 128-byte aligned address
+__host__ __device__ __forceinline__ ScanLayout scan_layout(int npla, int ns, int ldp, int qc, int kd, int rows_bytes) {
   ScanLayout L;
   size_t o = 0;
+  L.rows = o;  o += (size_t)((rows_bytes + 127) & ~127);
   L.stage = o; o += al16(sizeof(float2) * (size_t)SCAN_NSTAGE * 2 * qc * ldp);
   L.delta = o; o += al16(sizeof(float2) * 16 * (size_t)npla);
   L.geff = o;  o += al16(sizeof(float2) * 16 * (size_t)npla);
@@ -378,12 +395,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   __shared__ float2 s_det[NW];
   __shared__ int s_dec[NW];
   __shared__ __align__(8) uint64_t s_full[SCAN_NSTAGE];
+  __shared__ __align__(8) uint64_t s_rowbar;
   __shared__ int s_abort;
-  extern __shared__ __align__(16) unsigned char s_dyn[];
+  extern __shared__ __align__(1024) unsigned char s_dyn[];
   if (threadIdx.x == 0) {
     sd = D[blockIdx.x];
     s_abort = 0;
     for (int k = 0; k < SCAN_NSTAGE; ++k) mbar_init(&s_full[k], 1);
+    mbar_init(&s_rowbar, 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -397,7 +416,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     if (tid == 0) *d.kcount = 0;
     return;
   }
-  const ScanLayout L = scan_layout(npla, ns, ldp, qc, kd);
+  const int rb = d.rb, nrb = d.nrb;
+  const ScanLayout L = scan_layout(npla, ns, ldp, qc, kd, 4 * nrb * rb * (int)sizeof(float4));
+  float4* s_rows = reinterpret_cast<float4*>(s_dyn + L.rows);     // [dim][nrb*rb] rows of G at S
   float2* s_stage = reinterpret_cast<float2*>(s_dyn + L.stage);
   float2* s_delta = reinterpret_cast<float2*>(s_dyn + L.delta);   // [npla][16]
   float2* s_geff = reinterpret_cast<float2*>(s_dyn + L.geff);     // [npla][16]
@@ -408,6 +429,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   int* s_accp = reinterpret_cast<int*>(s_dyn + L.accp);
   float2* s_accd = reinterpret_cast<float2*>(s_dyn + L.accd);
   const float4* G = reinterpret_cast<const float4*>(parity ? d.g_alt : d.g);   // double-float G
+  const CUtensorMap* tmG = parity ? d.tm_galt : d.tm_g;
   float2* A = d.A;
   float2* B = d.B;
   const PlaqPre* pre = d.pre;
@@ -430,6 +452,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   int K = 0, n_acc = 0;
   long long na = 0;
   uint32_t phase = 0;   // bit s: parity of the next completion of stage s
+  uint32_t rowphase = 0;
+  int npre = 0;         // panel chunks already in flight for the next accepted move
   bool aborted = false;
   int p = p0;
   const int i = lane % dim, j = lane / dim;
@@ -492,13 +516,20 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     ++n_acc;
     const int* S = s_site + 4 * p;
     const int nch = (K + qc - 1) / qc;
-    if (tid == 0 && nch > 0) {
-      fence_proxy_async_global();   // this round's panel columns were written by generic stores
-      for (int c = 0; c < nch && c < SCAN_NSTAGE; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
+    if (tid == 0) {
+      // rows G(S_m, :) by the tensor engine (strided: one 16-byte element per column)
+      mbar_arrive_tx(&s_rowbar, (uint32_t)(dim * nrb * rb * sizeof(float4)));
+      for (int m = 0; m < dim; ++m)
+        for (int bx = 0; bx < nrb; ++bx) tma_load_2d(s_rows + (size_t)(m * nrb + bx) * rb, tmG, 4 * S[m], bx * rb, &s_rowbar);
+      if (nch > npre) {
+        if (npre == 0) fence_proxy_async_global();   // this round's panel columns were written by generic stores
+        for (int c = npre; c < nch && c < SCAN_NSTAGE; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
+      }
     }
+    npre = 0;
     // rows of G at the accepted sites, loaded now and added after the panel
     // loop (their latency overlaps it)
-    float4 gcol[RPT][dim], grow[RPT][dim];
+    float4 gcol[RPT][dim];
     float2 gm[RPT][dim], bl[RPT][dim];
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
@@ -506,7 +537,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
 #pragma unroll
       for (int m = 0; m < dim; ++m) {
         gcol[k][m] = r < ns ? G[r + (size_t)ns * S[m]] : make_float4(0.f, 0.f, 0.f, 0.f);
-        grow[k][m] = r < ns ? G[S[m] + (size_t)ns * r] : make_float4(0.f, 0.f, 0.f, 0.f);
         gm[k][m] = make_float2(0.f, 0.f);
         bl[k][m] = make_float2(0.f, 0.f);
       }
@@ -548,6 +578,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       break;
     }
     if (nch == 0) __syncthreads();   // s_T visible
+    if (!mbar_wait_bounded(&s_rowbar, rowphase)) s_abort = 1;   // checked after the next barrier
+    rowphase ^= 1u;
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
       const int r = tid + k * SCAN_THREADS;
@@ -555,7 +587,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
 #pragma unroll
       for (int m = 0; m < dim; ++m) {
         gm[k][m] = fa(gm[k][m], dg_f2(gcol[k][m]));
-        bl[k][m] = fa(bl[k][m], dg_f2(grow[k][m]));
+        bl[k][m] = fa(bl[k][m], dg_f2(s_rows[(size_t)m * nrb * rb + r]));
       }
 #pragma unroll
       for (int l = 0; l < dim; ++l) {
@@ -571,6 +603,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       }
     }
     __syncthreads();
+    if (s_abort) {
+      aborted = true;
+      break;
+    }
     // ---- the new block's contribution to the cached Geff of later plaquettes
     for (int e = tid; e < (npla - p - 1) * dd; e += blockDim.x) {
       const int pq = p + 1 + e / dd, k = e % dd;
@@ -583,12 +619,26 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     K += dim;
     ++p;
     __syncthreads();
+    // the next accepted move of this round streams columns [0, K): start it now
+    if (p < npla && K + dim <= kd) {
+      npre = min((K + qc - 1) / qc, SCAN_NSTAGE);
+      if (tid == 0) {
+        fence_proxy_async_global();
+        for (int c = 0; c < npre; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
+      }
+    }
+  }
+  // chunks started for an accepted move that did not come: drain them
+  for (int c = 0; c < npre && !aborted; ++c) {
+    if (!mbar_wait_bounded(&s_full[c], (phase >> c) & 1u)) aborted = true;
+    phase ^= 1u << c;
   }
   if (aborted) {
     // a panel chunk never arrived: give the copies still in flight a bounded
     // wait, flag the chain and stop (the host reports PQMC_ERR_TIMEOUT)
     if (tid == 0) {
       for (int st = 0; st < SCAN_NSTAGE; ++st) mbar_wait_bounded(&s_full[st], (phase >> st) & 1u);
+      mbar_wait_bounded(&s_rowbar, rowphase);
       d.sc->status = PQMC_ERR_TIMEOUT;
       atomicExch(d.err, PQMC_ERR_TIMEOUT);
       *d.kcount = 0;
@@ -1124,6 +1174,9 @@ struct pqmc_batch {
   int qc = 8;             // panel columns per streamed chunk of the scan
   int flush_mode = 1;     // 1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush
   unsigned char* d_img = nullptr;   // split operand tile images of the tcgen05 flush
+  CUtensorMap* d_tmaps = nullptr;   // per chain: maps of its two G buffers
+  int rb = 0, nrb = 0;              // row box of the maps (columns) and boxes per row
+  std::vector<cplx*> tm_buf;        // per chain x 2: the buffer each map describes
   int* d_err = nullptr;   // device error word shared by all chains
   int* d_next = nullptr;  // per chain: next plaquette of the current family step
   cudaStream_t stream = nullptr;   // the stream of group 0, the batch's public stream
@@ -1195,6 +1248,11 @@ static int batch_refresh(pqmc_batch* b) {
   for (size_t i = 0; i < b->chains.size(); ++i) {
     b->h_desc[i].g = b->chains[i]->g;
     b->h_desc[i].g_alt = b->chains[i]->g_alt;
+    if (b->d_tmaps) {
+      const bool same = b->tm_buf[2 * i] == b->chains[i]->g;
+      b->h_desc[i].tm_g = b->d_tmaps + 2 * i + (same ? 0 : 1);
+      b->h_desc[i].tm_galt = b->d_tmaps + 2 * i + (same ? 1 : 0);
+    }
   }
   b->parity = 0;
   PQMC_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), sizeof(BDesc) * b->h_desc.size(), cudaMemcpyHostToDevice,
@@ -1263,7 +1321,8 @@ static int bupdate(pqmc_batch* b, int g, int pf, int time) {
   const int ns = c0->ns;
   unsigned char* img = b->d_img ? b->d_img + um_chain_bytes(ns) * c_first : nullptr;
   for (int r = 0; r < rounds; ++r) {
-    const size_t smem = scan_layout(npla, ns, b->h_desc[0].ldp, b->qc, kd).total;
+    const BDesc& h0 = b->h_desc[0];
+    const size_t smem = scan_layout(npla, ns, h0.ldp, b->qc, kd, 4 * h0.nrb * h0.rb * (int)sizeof(float4)).total;
     cudaEvent_t ts = gphase_begin(b, g);
     const bool one = ns <= SCAN_THREADS;
 #define PQMC_SCAN(DM, R) k_bscan<DM, R><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next)
@@ -1410,9 +1469,13 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     PQMC_CUDA(cudaGetDevice(&dev));
     PQMC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const size_t stat = 4096;   // static shared memory of k_bscan (descriptor, per-warp R and T, barriers)
+    // rows of G by TMA boxes of rb columns (rb a multiple of 8: 128-byte aligned boxes)
+    const int nrb = (c0->ns + 255) / 256;
+    const int rb = (((c0->ns + nrb - 1) / nrb) + 7) & ~7;
+    const int rows_bytes = 4 * nrb * rb * (int)sizeof(float4);
     int qc = 8;
-    while (qc > 1 && scan_layout(max_pla, c0->ns, ldp, qc, SCAN_KSTAGE).total + stat > (size_t)optin) qc /= 2;
-    const size_t need = scan_layout(max_pla, c0->ns, ldp, qc, SCAN_KSTAGE).total;
+    while (qc > 1 && scan_layout(max_pla, c0->ns, ldp, qc, SCAN_KSTAGE, rows_bytes).total + stat > (size_t)optin) --qc;
+    const size_t need = scan_layout(max_pla, c0->ns, ldp, qc, SCAN_KSTAGE, rows_bytes).total;
     if (need + stat > (size_t)optin) {
       set_error("batch_create: scan staging needs %zu bytes of shared memory, the device offers %d", need + stat,
                 optin);
@@ -1420,6 +1483,39 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       return PQMC_ERR_ARG;
     }
     b->qc = qc;
+    // tensor maps over every chain's two G buffers (double-float: 4 FP32 per element)
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      set_error("batch_create: cuTensorMapEncodeTiled unavailable");
+      pqmc_batch_destroy(b);
+      return PQMC_ERR_CUDA;
+    }
+    auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    std::vector<CUtensorMap> maps(2 * (size_t)n_chains);
+    b->tm_buf.resize(2 * (size_t)n_chains);
+    for (int i = 0; i < n_chains; ++i)
+      for (int k = 0; k < 2; ++k) {
+        cplx* buf = k == 0 ? b->chains[i]->g : b->chains[i]->g_alt;
+        b->tm_buf[2 * i + k] = buf;
+        const cuuint64_t dims[2] = {4ull * (cuuint64_t)c0->ns, (cuuint64_t)c0->ns};
+        const cuuint64_t strides[1] = {16ull * (cuuint64_t)c0->ns};
+        const cuuint32_t box[2] = {4u, (cuuint32_t)rb};
+        const cuuint32_t estr[2] = {1u, 1u};
+        const CUresult r = encode(&maps[2 * i + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)buf, dims, strides, box,
+                                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+          set_error("batch_create: cuTensorMapEncodeTiled failed (%d)", (int)r);
+          pqmc_batch_destroy(b);
+          return PQMC_ERR_CUDA;
+        }
+      }
+    PQMC_CUDA(cudaMalloc((void**)&b->d_tmaps, sizeof(CUtensorMap) * maps.size()));
+    PQMC_CUDA(cudaMemcpy(b->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
+    b->rb = rb;
+    b->nrb = nrb;
 #define PQMC_SMEM(DM, R) PQMC_CUDA(cudaFuncSetAttribute(k_bscan<DM, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need))
     PQMC_SMEM(1, 1); PQMC_SMEM(2, 1); PQMC_SMEM(3, 1); PQMC_SMEM(4, 1);
     PQMC_SMEM(1, 2); PQMC_SMEM(2, 2); PQMC_SMEM(3, 2); PQMC_SMEM(4, 2);
@@ -1447,6 +1543,8 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     h.g_alt = c->g_alt;
     h.kmax = kmax;
     h.ldp = ldp;
+    h.rb = b->rb;
+    h.nrb = b->nrb;
     h.err = b->d_err;
     h.pre = c->pre;
     h.sc = c->sc;
@@ -1512,6 +1610,7 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
   if (b->d_img) cudaFree(b->d_img);
+  if (b->d_tmaps) cudaFree(b->d_tmaps);
   for (int g = 1; g < pqmc_batch::MAX_GROUPS; ++g)
     if (b->g_stream[g]) {
       cudaStreamSynchronize(b->g_stream[g]);

@@ -412,11 +412,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   const int ns = M.ns, npla = M.pf_npla[pf], pd = M.pdim, ldp = d.ldp;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int p0 = next_p[blockIdx.x];
+  // the thread that drives the copy engine: lane 0 of the last warp when that
+  // warp holds no row of G (its issue cost stays off the row workers' path)
   if (p0 >= npla) {
     if (tid == 0) *d.kcount = 0;
     return;
   }
   const int rb = d.rb, nrb = d.nrb;
+  const int io = (ns <= SCAN_THREADS - 32) ? SCAN_THREADS - 32 : 0;
   const ScanLayout L = scan_layout(npla, ns, ldp, qc, kd, 4 * nrb * rb * (int)sizeof(float4));
   float4* s_rows = reinterpret_cast<float4*>(s_dyn + L.rows);     // [dim][nrb*rb] rows of G at S
   float2* s_stage = reinterpret_cast<float2*>(s_dyn + L.stage);
@@ -516,7 +519,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     ++n_acc;
     const int* S = s_site + 4 * p;
     const int nch = (K + qc - 1) / qc;
-    if (tid == 0) {
+    if (tid == io) {
       // rows G(S_m, :) by the tensor engine (strided: one 16-byte element per column)
       mbar_arrive_tx(&s_rowbar, (uint32_t)(dim * nrb * rb * sizeof(float4)));
       for (int m = 0; m < dim; ++m)
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       }
       __syncthreads();
       if (s_abort) break;
-      if (tid == 0 && c + SCAN_NSTAGE < nch) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c + SCAN_NSTAGE);
+      if (tid == io && c + SCAN_NSTAGE < nch) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c + SCAN_NSTAGE);
     }
     if (s_abort) {
       aborted = true;
@@ -622,21 +625,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     // the next accepted move of this round streams columns [0, K): start it now
     if (p < npla && K + dim <= kd) {
       npre = min((K + qc - 1) / qc, SCAN_NSTAGE);
-      if (tid == 0) {
+      if (tid == io) {
         fence_proxy_async_global();
         for (int c = 0; c < npre; ++c) scan_issue(s_stage, s_full, A, B, ldp, qc, K, c);
       }
     }
   }
   // chunks started for an accepted move that did not come: drain them
-  for (int c = 0; c < npre && !aborted; ++c) {
-    if (!mbar_wait_bounded(&s_full[c], (phase >> c) & 1u)) aborted = true;
-    phase ^= 1u << c;
+  if (!aborted && npre > 0) {
+    for (int c = 0; c < npre; ++c) {
+      if (!mbar_wait_bounded(&s_full[c], (phase >> c) & 1u)) s_abort = 1;
+      phase ^= 1u << c;
+    }
+    __syncthreads();
+    aborted = s_abort != 0;
   }
   if (aborted) {
     // a panel chunk never arrived: give the copies still in flight a bounded
     // wait, flag the chain and stop (the host reports PQMC_ERR_TIMEOUT)
-    if (tid == 0) {
+    if (tid == io) {
       for (int st = 0; st < SCAN_NSTAGE; ++st) mbar_wait_bounded(&s_full[st], (phase >> st) & 1u);
       mbar_wait_bounded(&s_rowbar, rowphase);
       d.sc->status = PQMC_ERR_TIMEOUT;

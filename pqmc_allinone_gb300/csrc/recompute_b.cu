@@ -479,10 +479,17 @@ __global__ void __launch_bounds__(256) k_bprop_df(const PropArgs* args, const df
 #pragma unroll
           for (int r = 0; r < DIM; ++r) {
             if (r >= dim) break;
-            dfc acc = dfc_mul(e[r][0], v[0]);
+            // compensated dot product of the plaquette row with the column (Dot2)
+            d2acc ar{0.f, 0.f}, ai{0.f, 0.f};
 #pragma unroll
-            for (int k = 1; k < DIM; ++k) acc = dfc_add(acc, dfc_mul(e[r][k], v[k]));
-            x[S[r]] = acc;
+            for (int k = 0; k < DIM; ++k) {
+              const dfc& ek = e[r][k];
+              dot2_mac(ar, ek.re.hi, ek.re.lo, v[k].re.hi, v[k].re.lo);
+              dot2_mac(ar, -ek.im.hi, -ek.im.lo, v[k].im.hi, v[k].im.lo);
+              dot2_mac(ai, ek.re.hi, ek.re.lo, v[k].im.hi, v[k].im.lo);
+              dot2_mac(ai, ek.im.hi, ek.im.lo, v[k].re.hi, v[k].re.lo);
+            }
+            x[S[r]] = dfc{quick_two_sum(ar.h, ar.l), quick_two_sum(ai.h, ai.l)};
           }
         }
       }

@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="c4_mixed", choices=["c4_mixed", "c2_fp64", "small", "c5_adjoint"])
+    p.add_argument("--workload", default="c4_mixed", choices=["c4_mixed", "c2_fp64", "small", "c5_adjoint", "c3_uneven"])
     p.add_argument("--chains", type=int, default=0, help="chains per GPU of the mixed batch (default 64)")
     p.add_argument("--delay", type=int, default=0,
                    help="delay depth of the mixed batch (0: chosen by the autotuner during warm-up)")
@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--cpu-slices", type=int, default=0, help="slices per chain in the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--graphs", type=int, default=1, choices=[0, 1],
+                   help="replay each slice's family steps from a captured CUDA graph (mixed batches)")
     return p.parse_args()
 
 
@@ -246,6 +248,39 @@ class Cursor:
         return out
 
 
+def g_error_full_size(m, rank: int) -> dict:
+    """Green's-function error of the mixed form at full size: two chains run
+    the first block of sweep 1 (slices Lt..Lt-9, the stabilised recompute at
+    its end) in a mixed batch; the plain FP64 chain then recomputes G at the
+    same slice from the mixed chain's own field (init_g_T0 + get_g_scratch_T0)
+    and the two G are compared (relative Frobenius), with ln_cw beside."""
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.engine import PqmcBatch, PqmcChain
+    from pqmc_allinone_gb300.rng import seed_words
+    seeds = [3900 + i + 1000 * rank for i in range(2)]
+    b = PqmcBatch([m] * 2, [M.field_gaussian(m, s) for s in seeds], [seed_words(s) for s in seeds], precision=1)
+    b.init()
+    b.sweep_slices(1, 1, m.ngroup)
+    t = m.ntime - m.ngroup + 1
+    errs, dl = [], []
+    for c in b.chains:
+        p = PqmcChain(m, field=c.field(), rng_words=seed_words(1))
+        p.init_expkv()
+        p.init_g(1)
+        p.get_g_scratch(t, False, 1)
+        g0, g1 = p.g(), c.g()
+        errs.append(float(np.linalg.norm(g1 - g0) / np.linalg.norm(g0)))
+        dl.append(abs(c.state()["ln_cw"] - p.state()["ln_cw"]))
+        p.close()
+    drift = max(c.state()["err_g_rel_max"] for c in b.chains)
+    b.close()
+    return {"recompute_vs_fp64_rel_max": max(errs), "ln_cw_abs_diff_max": max(dl),
+            "fast_path_drift_in_block_rel_max": drift,
+            "definition": "||G_mixed - G_fp64||_F / ||G_fp64||_F at the recompute closing the first block of "
+                          f"sweep 1 (slice {t}), same phonon field, 2 chains at full size; the FP64 G from the "
+                          "plain single-chain path (parity-tested against the oracle)"}
+
+
 def run_plain(m, steps: int, rank: int) -> dict:
     """Plain single-chain FP64 form on this GPU (bit-identical decisions to
     the oracle), same block definition; wall time between device syncs (every
@@ -288,6 +323,7 @@ def run_mixed(args, world, rank, local):
     seeds = [3000 + i + 1000 * rank for i in range(C)]
     fields = [M.field_gaussian(m, s) for s in seeds]
     b = PqmcBatch([m] * C, fields, [seed_words(s) for s in seeds], precision=1)
+    b.set_graphs(bool(args.graphs))
     t0 = time.perf_counter()
     b.init()
     t_init = time.perf_counter() - t0
@@ -312,7 +348,6 @@ def run_mixed(args, world, rank, local):
     stream = torch.cuda.ExternalStream(b.stream())
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    b.set_timing(True)
     clk = ClockSampler(local)
     barrier(world)
     clk.start()
@@ -325,9 +360,8 @@ def run_mixed(args, world, rank, local):
     clocks = clk.stop()
     barrier(world)
     launches = kernel_launches() - n0
-    phases = b.timing()
-    b.set_timing(False)
     binfo = b.info()
+    binfo["slice_graphs"] = bool(args.graphs)
     t_step = max_over_ranks(world, ev0.elapsed_time(ev1) / 1000.0 / args.steps)
     per_gpu = C * (m.ngroup / m.ntime) / t_step
     value = world * per_gpu
@@ -335,42 +369,68 @@ def run_mixed(args, world, rank, local):
     acc = sum(s1["positive_accept"] - s0["positive_accept"] for s0, s1 in zip(st0, st1))
     rej = sum(s1["negative_accept"] - s0["negative_accept"] for s0, s1 in zip(st0, st1))
     drift = max(s["err_g_rel_max"] for s in st1)
+    # phase breakdown on two further blocks, outside the timed region (the
+    # event timers between phases bypass the slice graphs)
+    b.set_timing(True)
+    for _ in range(2):
+        b.sweep_slices(*cur.next(), m.ngroup)
+    torch.cuda.synchronize()
+    phases = b.timing()
+    b.set_timing(False)
+    st2 = [c.state() for c in b.chains]
+    # the phase timers follow chain group 0 (the first C/groups chains)
+    g0 = C // max(1, binfo["groups"])
+    acc_ph = sum(s2["positive_accept"] - s1["positive_accept"] for s1, s2 in zip(st1[:g0], st2[:g0]))
 
-    # dominant contraction: the rank-K flush G += A B on the tensor cores.
-    # Algorithmic flops counted once (complex GEMM, 8 flop per CMAC): every
-    # accepted move adds dim panel columns, each flushed column costs Ns^2 CMAC.
+    # the delayed-update contraction G += A B (rank-K flush).  At delay depth
+    # K it does 8*Ns^2*K flop against 32*Ns^2 bytes of G (double-float read
+    # and write): 2K/8 = 16 flop/B at K=64, under the HBM roof (7.3 TB/s x 16
+    # = 117 TFLOP/s), far below the tensor roof.  Algorithmic bytes per
+    # accepted move: a full-depth flush serves K/dim accepted moves, so
+    # 32*Ns^2*dim/K bytes per move (short last rounds move the same bytes for
+    # fewer moves: this count is a lower bound of the real traffic).
     pk = peaks()
     dim = 4
     flush_ms, flush_n = phases["flush"]
-    flops = 8.0 * m.ns * m.ns * dim * acc
-    per_launch = flops / max(1, flush_n)
-    achieved = per_launch / (flush_ms / max(1, flush_n) * 1e-3) / 1e12 if flush_ms > 0 else 0.0
+    bytes_alg = 32.0 * m.ns * m.ns * dim / depth * acc_ph
+    flops = 8.0 * m.ns * m.ns * dim * acc_ph
+    secs = flush_ms * 1e-3
+    achieved = bytes_alg / secs / 1e9 if secs > 0 else 0.0
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            tj = json.load(f).get("k_bflush")
+            tj = json.load(f).get("k_bflush_um")
             if tj and tj.get("ns") == m.ns:
-                # bytes per launch scale with the chains in the launch
-                traffic = tj["bytes_per_launch"] * C / tj["chains"]
+                # DRAM bytes of one full-depth launch, scaled to group 0's chains
+                traffic = tj["bytes_per_launch"] * g0 / tj["chains"]
     except Exception:
         pass
-    roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
-            "frac": achieved / pk["bf16_tflops_sustained"], "traffic": traffic,
-            "traffic_note": "DRAM bytes of one full-depth flush launch (ncu, profiles/traffic.json), scaled to the "
-                            "chains of this run; achieved averages over all flush launches incl. short last rounds",
+    roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+            "per_launch_bytes_algorithmic": bytes_alg / max(1, flush_n),
+            "traffic_note": "ncu dram__bytes_read+write of one full-depth flush launch (profiles/traffic.json), "
+                            "scaled to the chains of one launch (chain group 0)",
+            "tensor_achieved_tflops": flops / secs / 1e12 if secs > 0 else 0.0,
+            "tensor_peak_tflops": pk["bf16_tflops_sustained"],
             "kernel": ("k_bsplit + k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "
                        "in tensor memory)" if (depth <= 64 and (args.flush or tune)) else
                        "k_bflush (rank-K flush G += A B, mma.sync BF16x3 products, FP32 accumulate)"),
-            "algorithmic": "8*Ns^2*dim flop per accepted move (complex GEMM counted once, not the 6 split "
-                           "products)", "peak_source": f"{pk['source']} bf16 sustained (timed inside a long step)"}
+            "algorithmic": "32*Ns^2*dim/K bytes (G read + write, double-float) and 8*Ns^2*dim flop per accepted "
+                           "move, K = delay depth; chain group 0's moves over its flush-phase event time (the "
+                           "other groups' kernels share the GPU meanwhile)",
+            "peak_source": f"{pk['source']} HBM copy bandwidth; bf16 sustained for the tensor figure",
+            "dominant_by_time": "k_bscan (the sequential ratio scan, one CTA per chain: latency-bound by the "
+                                "Markov order, see phases)"}
     total_ms = sum(v[0] for v in phases.values())
-    phase_out = {k: {"ms_per_step": v[0] / args.steps, "share": v[0] / total_ms if total_ms else None,
+    phase_out = {k: {"ms_per_step": v[0] / 2, "share": v[0] / total_ms if total_ms else None,
                      "launch_groups": v[1]} for k, v in phases.items()}
 
     # end to end through the C-ABI with host buffers: every chain's field block
     # for the step goes host->device (the host copy, kept in step), the block
     # runs, the updated block and each chain's state come back
     e2e = run_e2e_mixed(b, m, cur, min(args.steps, 5))
+    b.close()
+    gerr = g_error_full_size(m, rank)
 
     plain = None if args.no_plain else run_plain(m, args.plain_steps, rank)
     cb = None
@@ -378,7 +438,6 @@ def run_mixed(args, world, rank, local):
         from pqmc_allinone_gb300 import model as M2
         from pqmc_allinone_gb300.rng import seed_words as sw
         cb = cpu_baseline(m, M2.field_gaussian(m, 2), sw(42), args.cpu_slices or 10)
-    b.close()
     if rank != 0:
         return
     out = {"metric": "sweeps/s @14x14 Lt=1000: batched mixed-prec vs plain FP64 on GB300",
@@ -394,7 +453,8 @@ def run_mixed(args, world, rank, local):
            "g_error": {"fast_path_drift_rel_max": drift,
                        "definition": "max over chains and recomputes in the timed region of "
                                      "||G_fast - G_recomputed||_F / ||G_recomputed||_F (drift of the FP32 "
-                                     "fast path over one ngroup block; the recompute is FP64-class)"},
+                                     "fast path over one ngroup block; the recompute is FP64-class)",
+                       "recompute_vs_fp64": gerr},
            "accept_ratio": acc / max(1, acc + rej), "phases": phase_out, "init_s": t_init}
     print(json.dumps(out))
 
@@ -454,6 +514,130 @@ def run_plain_headline(args, world, rank, local):
     print(json.dumps(out))
 
 
+def uneven_models(C: int, rank: int):
+    """Chains of uneven size: per chain i a seed 1000+i draws L from {8,10,12},
+    Lt from {200,400,600} and lambda ~ U(0.5,1.0); spin-orbit lattice with
+    static alpha=0.3, dtau=0.1, half filling, omega=1, ngroup=10; the field is
+    x ~ N(0,0.5^2) from the same seed."""
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.rng import seed_words
+    out = []
+    for i in range(C):
+        seed = 1000 + i + 100000 * rank
+        r = np.random.default_rng(seed)
+        L = int(r.choice([8, 10, 12]))
+        nt = int(r.choice([200, 400, 600]))
+        lam = float(r.uniform(0.5, 1.0))
+        spec = M.epsocz_spec(L, lam=lam, alpha=0.3, ntime=nt, ngroup=10, filling=0.5, jump_distance=0.5)
+        m = M.build_model(spec, twist_seed=11, twist=1e-3)
+        out.append((m, M.field_gaussian(m, seed), seed_words(seed)))
+    return out
+
+
+def run_uneven(args, world, rank, local):
+    """--workload c3_uneven: 256 chains of uneven L and Lt in one mixed batch
+    (geometry classes interleaved on their own streams, slice graphs, delay
+    depth autotuned per class); a step is one sweep of every chain (each over
+    its own Lt slices)."""
+    import torch
+    from pqmc_allinone_gb300.engine import PqmcBatch, PqmcChain, kernel_launches
+    torch.cuda.set_device(local)
+    C = args.chains or 256
+    t0 = time.perf_counter()
+    ms = uneven_models(C, rank)
+    t_models = time.perf_counter() - t0
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    b.set_graphs(bool(args.graphs))
+    t0 = time.perf_counter()
+    b.init()
+    t_init = time.perf_counter() - t0
+    # autotune on the first blocks of sweep 1, then finish sweep 1
+    cands = (32, 64, 96) if args.delay == 0 else (args.delay,)
+    best, table = b.autotune(1, 1, 10, cands)
+    b.sweep_slices(1, 1 + 10 * len(cands), max(m.ntime for m, _, _ in ms))
+    loop = 2
+    for _ in range(args.warmup):
+        b.sweep(loop)
+        loop += 1
+    torch.cuda.synchronize()
+    st0 = [c.state() for c in b.chains]
+    n0 = kernel_launches()
+    stream = torch.cuda.ExternalStream(b.stream())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(local)
+    barrier(world)
+    clk.start()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.sweep(loop)
+        loop += 1
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier(world)
+    launches = kernel_launches() - n0
+    t_step = max_over_ranks(world, ev0.elapsed_time(ev1) / 1000.0 / args.steps)
+    st1 = [c.state() for c in b.chains]
+    acc = sum(s1["positive_accept"] - s0["positive_accept"] for s0, s1 in zip(st0, st1))
+    rej = sum(s1["negative_accept"] - s0["negative_accept"] for s0, s1 in zip(st0, st1))
+    drift = max(s["err_g_rel_max"] for s in st1)
+    classes = b.classes()
+    n_graphs = b.graph_count()
+    b.close()
+    # plain FP64 single chains on a sample (one chain per L at Lt=200, one
+    # sweep each), scaled to the batch's mix by Lt: the sequential FP64 form
+    plain = None
+    if not args.no_plain:
+        secs = {}
+        for L in (8, 10, 12):
+            m, f, w = next((x for x in ms if int(x[0].lat.dlength[0]) == L), (None, None, None))
+            if m is None:
+                continue
+            from pqmc_allinone_gb300 import model as M
+            spec = M.epsocz_spec(L, lam=m.spec.ep_parameter, alpha=0.3, ntime=200, ngroup=10, filling=0.5,
+                                 jump_distance=0.5)
+            m2 = M.build_model(spec, twist_seed=11, twist=1e-3)
+            ch = PqmcChain(m2, field=M.field_gaussian(m2, 7), rng_words=w)
+            ch.init_expkv()
+            ch.init_g(1)
+            torch.cuda.synchronize()
+            ta = time.perf_counter()
+            ch.sweep(1, 1)
+            torch.cuda.synchronize()
+            secs[L] = time.perf_counter() - ta
+            ch.close()
+        est = sum(secs[int(m.lat.dlength[0])] * m.ntime / 200 for m, _, _ in ms)
+        plain = {"value": C / est, "unit": "chain-sweeps/s", "sample_s_per_sweep_at_lt200": secs,
+                 "method": "one plain FP64 chain per L at Lt=200 timed over one sweep; the batch's "
+                           "sum of per-chain sweep times scaled by Lt (chains one after another)"}
+    if rank != 0:
+        return
+    Ls = [int(m.lat.dlength[0]) for m, _, _ in ms]
+    Lts = [m.ntime for m, _, _ in ms]
+    out = {"metric": "chain-sweeps/s, 256 chains of uneven L in {8,10,12} and Lt in {200,400,600}",
+           "value": world * C / t_step, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None,
+           "dtype": "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute",
+           "data": "synthetic (per chain i: seed 1000+i draws L, Lt, lambda~U(0.5,1); x ~ N(0,0.5^2))",
+           "config": {"workload": f"{C} chains of uneven size, mixed precision, one batch per GPU",
+                      "chains_by_L": {L: Ls.count(L) for L in (8, 10, 12)},
+                      "chains_by_Lt": {t: Lts.count(t) for t in (200, 400, 600)},
+                      "classes": classes, "graphs": bool(args.graphs), "slice_graphs_held": n_graphs,
+                      "autotune": {"candidates_ms_per_slice_summed_over_classes": table, "class0_depth": best},
+                      "step": "one sweep of every chain (its own Lt slices, one recompute per 10 slices)",
+                      "l2": "no flush: the batch's G, expKV and Q strings (tens of GB) far exceed the 129 MB L2",
+                      "parallelism": f"replicas x{world}"},
+           "gpu_launches": int(launches), "clocks": clocks, "plain_fp64_sequential_estimate": plain,
+           "speedup_vs_plain_fp64": (C / t_step / plain["value"]) if plain else None,
+           "g_error": {"fast_path_drift_rel_max": drift},
+           "accept_ratio": acc / max(1, acc + rej), "models_s": t_models, "init_s": t_init,
+           "roofline": None, "cpu_baseline": None, "e2e": None}
+    print(json.dumps(out))
+
+
 def run_adjoint(args, world, rank, local):
     """--workload c5_adjoint: forward and hand-written adjoint of the projector
     log-weight log det(P^H B(Lt..1) P) for 32 chains of 10x10 SOC (Ns=200),
@@ -509,6 +693,8 @@ def main():
         run_plain_headline(args, world, rank, local)
     elif args.workload == "c5_adjoint":
         run_adjoint(args, world, rank, local)
+    elif args.workload == "c3_uneven":
+        run_uneven(args, world, rank, local)
     else:
         run_mixed(args, world, rank, local)
 

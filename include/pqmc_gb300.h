@@ -204,6 +204,11 @@ int pqmc_get_state(pqmc_chain* chain, pqmc_state* state);
 /* ran2 state words; replaces init_rng_by_seed (mod_ranstate.f90:267-283)
  * when called with the five seeded words. */
 int pqmc_set_rng(pqmc_chain* chain, const int32_t rng[5]);
+/* Restore the ran2 state, accept counters and error maxima of a checkpoint
+ * (pqmc_get_state of the saved chain; no reference counterpart: the
+ * reference has no checkpoint writer, Main_PQMC.f90:166).  ln_cw is not
+ * taken: the init_g_T0 that follows a restore recomputes it. */
+int pqmc_set_state(pqmc_chain* chain, const pqmc_state* state);
 /* Q_string(:,:,block) and D_string(:,block), block 1-based. */
 int pqmc_get_qd(pqmc_chain* chain, int block, double* q, double* d);
 
@@ -253,6 +258,58 @@ int pqmc_sweep(pqmc_chain* chain, int first_loop, int n_sweeps, int warmup,
  * body (no measurement); n_slices = ntime from first_tc = 1 is one whole
  * sweep.  Lets a driver advance a sweep in stabilisation blocks. */
 int pqmc_sweep_slices(pqmc_chain* chain, int loop, int first_tc, int n_slices);
+
+/* ---- global moves (update_global, src/mod_update.f90:250-467) ---------- */
+/* update_type of update_global / generate_newfield_global */
+#define PQMC_GLOBAL_SINGLE 0      /* default branch: flip or shift the whole
+                                     time line of n_global_update bonds      */
+#define PQMC_GLOBAL_EXCHANGE 1    /* "exchange": swap the time lines of two
+                                     bonds, n_global_update times            */
+#define PQMC_GLOBAL_KSPACE 2      /* "kspace": add a (pi,pi) staggered pattern
+                                     to every slice                          */
+#define PQMC_GLOBAL_KSPACE_TIME 3 /* "kspace_time": the same pattern on
+                                     slices start_time..end_time             */
+#define PQMC_GLOBAL_ROTATE 4      /* "rotate": rotate (or reflect) the two
+                                     boson fields of every cell              */
+typedef struct pqmc_global_params {
+  int32_t n_global_update;    /* n_global_update (input.f90:74)             */
+  int32_t global_update_loop; /* global_update_loop (input.f90:75)          */
+  int32_t flip;               /* global_update_flip                          */
+  int32_t shift;              /* global_update_shift                         */
+  int32_t rotate;             /* the driver adds the "rotate" move (EPSOCZ
+                                 models, Main_PQMC.f90:92)                   */
+  int32_t lat_dim;            /* Lat%dim (2 for the k-space moves)          */
+  int32_t n_cell;             /* Lat%N_cell                                  */
+  int32_t bf_sets;            /* boson fields per cell (2 for "rotate")      */
+  double distance;            /* global_update_distance*char_length
+                                 (input.f90:184)                             */
+  const double* cell_rpos;    /* (lat_dim, n_cell) p_cells(i)%rpos          */
+} pqmc_global_params;
+/* The field generation alone, on the host: the new boson_field (n_bf,
+ * ntime, in place), the phonon-action part of the weight ph_ln_cw
+ * (-delta_energy*delt) and the slices whose expKV change (1-based
+ * t_first..t_last), advancing the ran2 state rng[5] by the draws the move
+ * takes (generate_newfield_global, mod_update.f90:298-438).  Needs no GPU. */
+int pqmc_global_generate(const pqmc_model* model, const pqmc_global_params* params,
+                         int kind, int32_t rng[5], double* boson_field,
+                         double* ph_ln_cw, int* t_first, int* t_last);
+/* Copies the parameters into the chain (and enables the global step of
+ * pqmc_sweep). */
+int pqmc_set_global(pqmc_chain* chain, const pqmc_global_params* params);
+/* update_global(update_type) (mod_update.f90:250-292): the new field, its
+ * expKV and cal_new_weight_T0 on the device, the Metropolis test of
+ * ln_cw_new + ph_ln_cw - ln_cw_old (cal_prob) with one more ran2 draw;
+ * a rejected move restores field, expKV and ln_cw.  *accepted = 0 or 1.
+ * G is not touched (the caller re-initialises it after accepted moves). */
+int pqmc_update_global(pqmc_chain* chain, int kind, int* accepted);
+/* The driver's global step before sweep `loop` (Main_PQMC.f90:87-96): when
+ * the sweep runs backward and mod(loop+1, global_update_loop) == 0, the
+ * "kspace", "rotate" (when enabled) and "kspace_time" moves, then
+ * init_g_T0(1) if any was accepted.  *n_accepted (may be NULL) counts them.
+ * pqmc_sweep runs this step itself once pqmc_set_global was called. */
+int pqmc_global_step(pqmc_chain* chain, int loop, int* n_accepted);
+/* global_accept / global_reject counters (input.f90:7) */
+int pqmc_global_counters(pqmc_chain* chain, int64_t* accepted, int64_t* rejected);
 
 /* ---- differentiable log-weight ---------------------------------------- */
 /* boson_field from a DEVICE pointer (n_bf, ntime), e.g. a torch tensor. */
@@ -321,6 +378,17 @@ int pqmc_batch_stream(pqmc_batch* batch, void** stream);
  * precision}; the groups default to one per 16 chains (at most 4) and can
  * be set with the environment variable PQMC_BATCH_GROUPS (1..4) at creation */
 int pqmc_batch_info(pqmc_batch* batch, int* info);
+/* Uneven batches (mixed precision): chains of different geometry (Ns, Lt,
+ * families) are grouped into classes of equal geometry; each class runs
+ * as a homogeneous batch with its own streams, chain groups, delay depth
+ * and slice graphs, and the classes interleave their slices within one
+ * call (pqmc_batch_sweep: every chain one sweep of its own ntime slices).
+ * pqmc_batch_classes gives the number of classes (1 for an even batch);
+ * pqmc_batch_class_info(k) fills info[6] = {chains, Ns, ntime, delay depth,
+ * flush engine, chain groups} of class k.  Chain indices stay those of the
+ * models array. */
+int pqmc_batch_classes(pqmc_batch* batch, int* n);
+int pqmc_batch_class_info(pqmc_batch* batch, int k, int* info);
 /* CUDA-event timers per phase of the mixed family step; set_timing clears
  * the totals, get_timing returns PQMC_N_PHASES totals (ms) and counts. */
 #define PQMC_PHASE_PREP      0   /* ran2 draws + proposal data           */
@@ -331,6 +399,17 @@ int pqmc_batch_info(pqmc_batch* batch, int* info);
 #define PQMC_N_PHASES        5
 int pqmc_batch_set_timing(pqmc_batch* batch, int enable);
 int pqmc_batch_get_timing(pqmc_batch* batch, double* ms, long long* launches);
+/* Slice graphs (mixed batches; no reference counterpart): with enable=1 the
+ * family steps of a slice (draws, proposals, scan rounds, flushes, wraps)
+ * are captured once per chain group, direction and G-buffer parity into a
+ * CUDA graph and replayed for every later slice; the slice's time index
+ * lives in device memory, so one graph serves all slices.  The stabilised
+ * recompute and the measurement window still run as plain launches, and
+ * phase timing (pqmc_batch_set_timing) bypasses the graphs.  Results are
+ * bit-identical with and without graphs. */
+int pqmc_batch_set_graphs(pqmc_batch* batch, int enable);
+/* number of captured slice graphs held by the batch */
+int pqmc_batch_graph_count(pqmc_batch* batch, int* n);
 
 /* ---- recompute without device allocation ---------------------------- */
 /* No counterpart in the reference.  g_out = R (X^H R)^-1 X^H and

@@ -60,11 +60,56 @@ class PqmcState(ctypes.Structure):
         ("reserved", ctypes.c_int32), ("err_g", ctypes.c_double), ("err_g_rel_max", ctypes.c_double),
     ]
 
+    @classmethod
+    def from_dict(cls, d: dict) -> "PqmcState":
+        s = cls()
+        s.ln_cw[0], s.ln_cw[1] = complex(d.get("ln_cw", 0)).real, complex(d.get("ln_cw", 0)).imag
+        s.err_fast_max, s.err_fast = float(d["err_fast_max"]), float(d["err_fast"])
+        s.positive_accept, s.negative_accept = int(d["positive_accept"]), int(d["negative_accept"])
+        for k in range(5):
+            s.rng[k] = int(d["rng"][k])
+        s.err_g, s.err_g_rel_max = float(d["err_g"]), float(d["err_g_rel_max"])
+        return s
+
     def as_dict(self) -> dict:
         return dict(ln_cw=complex(self.ln_cw[0], self.ln_cw[1]), err_fast_max=self.err_fast_max,
                     err_fast=self.err_fast, positive_accept=self.positive_accept,
                     negative_accept=self.negative_accept, rng=list(self.rng), err_g=self.err_g,
                     err_g_rel_max=self.err_g_rel_max)
+
+
+class GlobalParams(ctypes.Structure):
+    """pqmc_global_params (global moves, src/mod_update.f90:250-467)."""
+    _fields_ = [
+        ("n_global_update", ctypes.c_int32), ("global_update_loop", ctypes.c_int32),
+        ("flip", ctypes.c_int32), ("shift", ctypes.c_int32), ("rotate", ctypes.c_int32),
+        ("lat_dim", ctypes.c_int32), ("n_cell", ctypes.c_int32), ("bf_sets", ctypes.c_int32),
+        ("distance", ctypes.c_double), ("cell_rpos", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+def global_params(m: Model, *, global_update_distance: float = 1.0, n_global_update: int = 1,
+                  global_update_loop: int = 2, flip: bool = False, shift: bool = False,
+                  rotate: bool | None = None) -> dict:
+    """The global-update namelist values of input.f90:19-22,71-75 for model m
+    (distance scaled by char_length as in input.f90:184; the "rotate" move
+    for EPSOCZ models as in Main_PQMC.f90:92)."""
+    if rotate is None:
+        rotate = m.spec.model_name.strip() == "EPSOCZ"
+    return {"n_global_update": int(n_global_update), "global_update_loop": int(global_update_loop),
+            "flip": int(flip), "shift": int(shift), "rotate": int(rotate), "lat_dim": int(m.lat.dim),
+            "n_cell": int(m.lat.n_cell), "bf_sets": int(m.spec.bf_sets),
+            "distance": float(global_update_distance) * float(m.char_length),
+            "cell_rpos": np.ascontiguousarray(m.lat.cell_rpos, dtype=np.float64)}
+
+
+def global_struct(gp: dict):
+    """(ctypes struct, kept buffers) of a global_params dict."""
+    rpos = np.ascontiguousarray(gp["cell_rpos"], dtype=np.float64)   # (n_cell, dim) == Fortran (dim, n_cell)
+    s = GlobalParams(gp["n_global_update"], gp["global_update_loop"], gp["flip"], gp["shift"], gp["rotate"],
+                     gp["lat_dim"], gp["n_cell"], gp["bf_sets"], gp["distance"],
+                     rpos.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return s, rpos
 
 
 def _ptr(a: np.ndarray, ty):
@@ -156,6 +201,14 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_set_g": ([vp, _f64p], ctypes.c_int),
         "pqmc_get_state": ([vp, ctypes.POINTER(PqmcState)], ctypes.c_int),
         "pqmc_set_rng": ([vp, _i32p], ctypes.c_int),
+        "pqmc_set_state": ([vp, ctypes.POINTER(PqmcState)], ctypes.c_int),
+        "pqmc_global_generate": ([ctypes.POINTER(PqmcModel), ctypes.POINTER(GlobalParams), ctypes.c_int, _i32p,
+                                  _f64p, _f64p, _i32p, _i32p], ctypes.c_int),
+        "pqmc_set_global": ([vp, ctypes.POINTER(GlobalParams)], ctypes.c_int),
+        "pqmc_update_global": ([vp, ctypes.c_int, _i32p], ctypes.c_int),
+        "pqmc_global_step": ([vp, ctypes.c_int, _i32p], ctypes.c_int),
+        "pqmc_global_counters": ([vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
+                                 ctypes.c_int),
         "pqmc_get_qd": ([vp, ctypes.c_int, _f64p, _f64p], ctypes.c_int),
         "pqmc_init_expkv": ([vp], ctypes.c_int),
         "pqmc_init_g": ([vp, ctypes.c_int], ctypes.c_int),
@@ -193,6 +246,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_info": ([vp, _i32p], ctypes.c_int),
         "pqmc_batch_set_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_get_timing": ([vp, _f64p, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "pqmc_batch_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_classes": ([vp, _i32p], ctypes.c_int),
+        "pqmc_batch_class_info": ([vp, ctypes.c_int, _i32p], ctypes.c_int),
+        "pqmc_batch_graph_count": ([vp, _i32p], ctypes.c_int),
         "pqmc_version": ([], ctypes.c_char_p),
         "pqmc_last_error": ([], ctypes.c_char_p),
         "pqmc_kernel_launches": ([], ctypes.c_int64),

@@ -21,6 +21,8 @@
 #include <cudaTypedefs.h>
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
+#include <deque>
 #include <vector>
 #include "chain.cuh"
 #include "linalg.cuh"
@@ -51,6 +53,7 @@ struct BDesc {
   const CUtensorMap* tm_g;
   const CUtensorMap* tm_galt;
   int rb, nrb;
+  int t;         // 0-based time index of the slice in progress (k_bsettime)
 };
 
 __device__ __forceinline__ float2 f2(cplx a) { return make_float2((float)a.x, (float)a.y); }
@@ -99,11 +102,19 @@ __device__ __forceinline__ double b_threshold(const DevModel& M, double dE, doub
   return pow(q, 2.0 / n);
 }
 
-__global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf, int t) {
+// the slice every chain of a group works on; kept on the device so that one
+// captured graph of a slice's launches serves every time index
+__global__ void k_bsettime(BDesc* D, int C, int t) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < C) D[c].t = t;
+}
+
+__global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf) {
   __shared__ BDesc sd;
   if (threadIdx.x == 0) sd = D[blockIdx.y];
   __syncthreads();
   const BDesc& d = sd;
+  const int t = d.t;
   const DevModel& M = d.M;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int npla = M.pf_npla[pf], dim = M.pf_dim[pf], pd = M.pdim;
@@ -386,7 +397,7 @@ __device__ __forceinline__ void scan_issue(float2* s_stage, uint64_t* s_full, co
 }
 
 template <int DIM, int RPT>
-__global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int t, int parity, int kd, int qc,
+__global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int parity, int kd, int qc,
                                                          int* next_p) {
   constexpr int NW = SCAN_THREADS / 32;
   __shared__ BDesc sd;
@@ -408,6 +419,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   __syncthreads();
   const BDesc& d = sd;
   const DevModel& M = d.M;
+  const int t = d.t;
   constexpr int dim = DIM, dd = DIM * DIM;
   const int ns = M.ns, npla = M.pf_npla[pf], pd = M.pdim, ldp = d.ldp;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1075,7 +1087,7 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigne
 // are the family's plaquettes (DIM sites) and uncovered singletons, so every
 // block is at most DIM x DIM and lives in registers.
 template <int DIM>
-__global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, int left, int n_items, int parity,
+__global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int left, int n_items, int parity,
                                                const int* __restrict__ wpla, const int* __restrict__ wsites,
                                                const int* __restrict__ wdim) {
   __shared__ BDesc sd;
@@ -1085,6 +1097,7 @@ __global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int t, in
   const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (pair >= (long)n_items * n_items) return;
   const DevModel& M = d.M;
+  const int t = d.t;
   const int ir = (int)(pair % n_items), ic = (int)(pair / n_items);
   const int ns = M.ns, pd = M.pdim;
   const int dr = wdim[ir], dc = wdim[ic];
@@ -1195,6 +1208,18 @@ struct pqmc_batch {
   cudaStream_t g_stream[MAX_GROUPS] = {};
   pqmc::BatchRecompute rec[MAX_GROUPS];
   cudaEvent_t ev_fork = nullptr, ev_join[MAX_GROUPS] = {};
+  // uneven batch (mixed precision, chains of more than one geometry): one
+  // homogeneous batch per geometry class; `chains` then borrows their chains
+  std::vector<pqmc_batch*> parts;
+  std::vector<int> part_of, index_in_part;
+  // slice graphs (pqmc_batch_set_graphs): captured family steps of one slice
+  struct SliceGraph {
+    int key[6];   // group, forward, parity, delay depth, flush engine, chunk
+    cudaGraphExec_t exec;
+    int kernels;  // kernel nodes per replay
+  };
+  bool graphs = false;
+  std::deque<SliceGraph> gcache;
   // equal-time measurement inside batched sweeps (ms_begin_measure semantics)
   int meas_on = 0, meas_warmup = 0, meas_interval = 1, meas_number = 0;
   std::vector<std::vector<double>> records;   // finished records per chain
@@ -1285,8 +1310,9 @@ static void gphase_end(pqmc_batch* b, int g, int phase, cudaEvent_t a) {
   if (g == 0) phase_end(b, phase, a);
 }
 
-// two-way wrap of group g's chains by family pf (the caller flips the parity)
-static int bwrap(pqmc_batch* b, int g, int pf, int time, bool left) {
+// two-way wrap of group g's chains by family pf at the group's slice (the
+// caller flips the parity)
+static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
   pqmc_chain* c0 = b->chains[0];
   const WrapItems& w = c0->wrap[pf];
   const int C = b->g_count[g];
@@ -1297,17 +1323,18 @@ static int bwrap(pqmc_batch* b, int g, int pf, int time, bool left) {
   const int l = left ? 1 : 0;
   cudaEvent_t tw = gphase_begin(b, g);
   switch (c0->h_pf_dim[pf]) {
-    case 1: k_bwrap<1><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
-    case 2: k_bwrap<2><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
-    case 3: k_bwrap<3><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
-    default: k_bwrap<4><<<grid, 128, 0, st>>>(D, pf, time - 1, l, w.n_items, b->parity, w.d_pla, w.d_sites, w.d_dim); break;
+    case 1: k_bwrap<1><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+    case 2: k_bwrap<2><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+    case 3: k_bwrap<3><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+    default: k_bwrap<4><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
   }
   PQMC_LAUNCHED();
   gphase_end(b, g, PQMC_PHASE_WRAP, tw);
   return PQMC_OK;
 }
 
-static int bupdate(pqmc_batch* b, int g, int pf, int time) {
+// update_phonon_field of family pf for group g's chains at the group's slice
+static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
   const int C = b->g_count[g], c_first = b->g_first[g];
   const BDesc* Dg = b->d_desc + c_first;
   int* next = b->d_next + c_first;
@@ -1317,7 +1344,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int time) {
   cudaEvent_t tp = gphase_begin(b, g);
   k_bdraw<<<(C + 63) / 64, 64, 0, st>>>(Dg, C, pf);
   PQMC_LAUNCHED();
-  k_bprep<<<dim3((npla + 7) / 8, C), 256, 0, st>>>(Dg, pf, time - 1);
+  k_bprep<<<dim3((npla + 7) / 8, C), 256, 0, st>>>(Dg, pf);
   PQMC_LAUNCHED();
   gphase_end(b, g, PQMC_PHASE_PREP, tp);
   PQMC_CUDA(cudaMemsetAsync(next, 0, sizeof(int) * C, st));
@@ -1332,7 +1359,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int time) {
     const size_t smem = scan_layout(npla, ns, h0.ldp, b->qc, kd, 4 * h0.nrb * h0.rb * (int)sizeof(float4)).total;
     cudaEvent_t ts = gphase_begin(b, g);
     const bool one = ns <= SCAN_THREADS;
-#define PQMC_SCAN(DM, R) k_bscan<DM, R><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, time - 1, b->parity, kd, b->qc, next)
+#define PQMC_SCAN(DM, R) k_bscan<DM, R><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, parity, kd, b->qc, next)
     switch (dim) {
       case 1: if (one) PQMC_SCAN(1, 1); else PQMC_SCAN(1, 2); break;
       case 2: if (one) PQMC_SCAN(2, 1); else PQMC_SCAN(2, 2); break;
@@ -1347,10 +1374,10 @@ static int bupdate(pqmc_batch* b, int g, int pf, int time) {
       const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * (((kd + 15) & ~15) / 8);
       k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, st>>>(Dg, img);
       PQMC_LAUNCHED();
-      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, st>>>(Dg, img, b->parity);
+      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, st>>>(Dg, img, parity);
       PQMC_LAUNCHED();
     } else {
-      k_bflush<<<dim3(tiles, C), 256, 0, st>>>(Dg, b->parity);
+      k_bflush<<<dim3(tiles, C), 256, 0, st>>>(Dg, parity);
       PQMC_LAUNCHED();
     }
     gphase_end(b, g, PQMC_PHASE_FLUSH, tf);
@@ -1358,10 +1385,95 @@ static int bupdate(pqmc_batch* b, int g, int pf, int time) {
   return PQMC_OK;
 }
 
+// the family steps of one slice for group g (Main_PQMC.f90:99-154: forward,
+// update then wrap per family; backward, wrap then update in reverse family
+// order), starting at `parity`; one parity flip per family
+static int slice_ops(pqmc_batch* b, int g, bool forward, int parity) {
+  pqmc_chain* c0 = b->chains[0];
+  const bool upd = c0->M.local_update != 0;
+  if (!forward) {
+    for (int pf = c0->n_pf - 1; pf >= 0; --pf) {
+      PQMC_TRY(bwrap(b, g, pf, false, parity));
+      parity ^= 1;
+      if (upd && c0->h_pf_v_exist[pf]) PQMC_TRY(bupdate(b, g, pf, parity));
+    }
+  } else {
+    for (int pf = 0; pf < c0->n_pf; ++pf) {
+      if (upd && c0->h_pf_v_exist[pf]) PQMC_TRY(bupdate(b, g, pf, parity));
+      PQMC_TRY(bwrap(b, g, pf, true, parity));
+      parity ^= 1;
+    }
+  }
+  return PQMC_OK;
+}
+
+// the executable graph of slice_ops(g, forward, parity) under the current
+// delay depth, flush engine and chunk size, captured on first use.  Nothing
+// a slice launches depends on its time index (read from the descriptors), so
+// one graph serves every slice of that direction and parity.
+static int slice_graph(pqmc_batch* b, int g, bool forward, int parity, pqmc_batch::SliceGraph** out) {
+  const int key[6] = {g, forward ? 1 : 0, parity, b->kd, b->flush_mode, b->qc};
+  for (auto& e : b->gcache)
+    if (std::equal(key, key + 6, e.key)) {
+      *out = &e;
+      return PQMC_OK;
+    }
+  cudaStream_t st = b->g_stream[g];
+  const int64_t n0 = g_launches.load();
+  PQMC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int rc = slice_ops(b, g, forward, parity);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+  const int n_kernels = (int)(g_launches.load() - n0);
+  count_launch(-n_kernels);   // counted again at every replay
+  if (rc != PQMC_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ec != cudaSuccess) {
+    set_error("slice graph capture: %s", cudaGetErrorString(ec));
+    return PQMC_ERR_CUDA;
+  }
+  pqmc_batch::SliceGraph e{};
+  std::copy(key, key + 6, e.key);
+  e.kernels = n_kernels;
+  const cudaError_t ei = cudaGraphInstantiate(&e.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    set_error("slice graph instantiate: %s", cudaGetErrorString(ei));
+    return PQMC_ERR_CUDA;
+  }
+  b->gcache.push_back(e);
+  *out = &b->gcache.back();
+  return PQMC_OK;
+}
+
+static void drop_graphs(pqmc_batch* b) {
+  for (auto& e : b->gcache) cudaGraphExecDestroy(e.exec);
+  b->gcache.clear();
+}
+
+// one slice of group g at 1-based `time`: its time index goes to the
+// descriptors, then the family steps run as a graph replay or as launches
+static int group_slice(pqmc_batch* b, int g, bool forward, int time, int parity) {
+  cudaStream_t st = b->g_stream[g];
+  const int C = b->g_count[g];
+  k_bsettime<<<(C + 127) / 128, 128, 0, st>>>(b->d_desc + b->g_first[g], C, time - 1);
+  PQMC_LAUNCHED();
+  if (b->graphs && !b->timing) {
+    pqmc_batch::SliceGraph* e = nullptr;
+    PQMC_TRY(slice_graph(b, g, forward, parity, &e));
+    PQMC_CUDA(cudaGraphLaunch(e->exec, st));
+    count_launch(e->kernels);
+    return PQMC_OK;
+  }
+  return slice_ops(b, g, forward, parity);
+}
+
 // stabilised recompute of group g (the caller flips the parity)
-static int bscratch(pqmc_batch* b, int g, int time, bool forward) {
+static int bscratch(pqmc_batch* b, int g, int time, bool forward, int parity) {
   cudaEvent_t tr = gphase_begin(b, g);
-  PQMC_TRY(b->rec[g].scratch(time, forward, b->parity));
+  PQMC_TRY(b->rec[g].scratch(time, forward, parity));
   gphase_end(b, g, PQMC_PHASE_RECOMPUTE, tr);
   return PQMC_OK;
 }
@@ -1426,6 +1538,57 @@ static int batch_measure(pqmc_batch* b, int time, bool forward) {
   return groups_fork(b);
 }
 
+// geometry of a mixed batch: chains of one class share every launch shape
+static bool same_geometry(const pqmc_model* a, const pqmc_model* b) {
+  if (a->ns != b->ns || a->nelec != b->nelec || a->ntime != b->ntime || a->ngroup != b->ngroup ||
+      a->n_pf != b->n_pf || a->max_dim != b->max_dim || a->max_pla != b->max_pla || a->n_bf != b->n_bf ||
+      a->local_update != b->local_update)
+    return false;
+  for (int f = 0; f < a->n_pf; ++f)
+    if (a->pf_dim[f] != b->pf_dim[f] || a->pf_npla[f] != b->pf_npla[f] || a->pf_v_exist[f] != b->pf_v_exist[f])
+      return false;
+  return true;
+}
+
+extern "C" int pqmc_batch_destroy(pqmc_batch* b);
+extern "C" int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precision, pqmc_batch** out);
+
+// an uneven mixed batch: one homogeneous batch per geometry class, each with
+// its own streams, chain groups, delay depth and graphs
+static int create_uneven(const pqmc_model* const* models, int n_chains, const std::vector<int>& cls, int n_cls,
+                         pqmc_batch** out) {
+  pqmc_batch* b = new pqmc_batch();
+  b->precision = PQMC_PREC_MIXED;
+  b->part_of.assign(n_chains, 0);
+  b->index_in_part.assign(n_chains, 0);
+  for (int k = 0; k < n_cls; ++k) {
+    std::vector<const pqmc_model*> sub;
+    for (int i = 0; i < n_chains; ++i)
+      if (cls[i] == k) {
+        b->part_of[i] = k;
+        b->index_in_part[i] = (int)sub.size();
+        sub.push_back(models[i]);
+      }
+    pqmc_batch* part = nullptr;
+    const int st = pqmc_batch_create(sub.data(), (int)sub.size(), PQMC_PREC_MIXED, &part);
+    if (st != PQMC_OK) {
+      pqmc_batch_destroy(b);
+      return st;
+    }
+    b->parts.push_back(part);
+  }
+  for (int i = 0; i < n_chains; ++i) b->chains.push_back(b->parts[b->part_of[i]]->chains[b->index_in_part[i]]);
+  PQMC_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  PQMC_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  int groups = 0;
+  for (auto* p : b->parts) groups += p->n_groups;
+  b->n_groups = groups;
+  b->kd = b->parts[0]->kd;
+  b->flush_mode = b->parts[0]->flush_mode;
+  *out = b;
+  return PQMC_OK;
+}
+
 extern "C" {
 
 int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precision, pqmc_batch** out) {
@@ -1433,6 +1596,21 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   if (precision != PQMC_PREC_FP64 && precision != PQMC_PREC_MIXED) {
     set_error("batch_create: unknown precision %d", precision);
     return PQMC_ERR_ARG;
+  }
+  if (precision == PQMC_PREC_MIXED) {
+    // chains of more than one geometry: one class per geometry
+    std::vector<int> cls(n_chains, -1);
+    std::vector<int> rep;   // first chain of each class
+    for (int i = 0; i < n_chains; ++i) {
+      if (!models[i]) { set_error("batch_create: null model %d", i); return PQMC_ERR_ARG; }
+      for (size_t k = 0; k < rep.size() && cls[i] < 0; ++k)
+        if (same_geometry(models[i], models[rep[k]])) cls[i] = (int)k;
+      if (cls[i] < 0) {
+        cls[i] = (int)rep.size();
+        rep.push_back(i);
+      }
+    }
+    if (rep.size() > 1) return create_uneven(models, n_chains, cls, (int)rep.size(), out);
   }
   pqmc_batch* b = new pqmc_batch();
   b->precision = precision;
@@ -1523,7 +1701,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     PQMC_CUDA(cudaMemcpy(b->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
     b->rb = rb;
     b->nrb = nrb;
-#define PQMC_SMEM(DM, R) PQMC_CUDA(cudaFuncSetAttribute(k_bscan<DM, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need))
+#define PQMC_SMEM(DM, R) PQMC_CUDA(raise_dyn_smem(k_bscan<DM, R>, (int)need))
     PQMC_SMEM(1, 1); PQMC_SMEM(2, 1); PQMC_SMEM(3, 1); PQMC_SMEM(4, 1);
     PQMC_SMEM(1, 2); PQMC_SMEM(2, 2); PQMC_SMEM(3, 2); PQMC_SMEM(4, 2);
 #undef PQMC_SMEM
@@ -1535,7 +1713,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     const size_t ib = um_chain_bytes(c0->ns) * (size_t)n_chains;
     PQMC_CUDA(cudaMalloc((void**)&b->d_img, ib));
     PQMC_CUDA(cudaMemset(b->d_img, 0, ib));
-    PQMC_CUDA(cudaFuncSetAttribute(k_bflush_um, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * UM_IMG));
+    PQMC_CUDA(raise_dyn_smem(k_bflush_um, 6 * UM_IMG));
   }
   b->h_desc.resize(n_chains);
   for (int i = 0; i < n_chains; ++i) {
@@ -1602,12 +1780,18 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
 
 int pqmc_batch_destroy(pqmc_batch* b) {
   if (!b) return PQMC_OK;
+  if (!b->parts.empty() || !b->part_of.empty()) {
+    for (auto* p : b->parts) pqmc_batch_destroy(p);   // the chains belong to the classes
+    b->parts.clear();
+    b->chains.clear();
+  }
   if (b->stream) cudaStreamSynchronize(b->stream);
   for (auto& m : b->marks) {
     cudaEventDestroy(m.a);
     cudaEventDestroy(m.b);
   }
   for (auto e : b->ev_pool) cudaEventDestroy(e);
+  drop_graphs(b);
   for (auto* c : b->chains) pqmc_destroy(c);
   for (auto* p : b->panels)
     if (p) cudaFree(p);
@@ -1633,18 +1817,49 @@ int pqmc_batch_destroy(pqmc_batch* b) {
 
 int pqmc_batch_set_flush(pqmc_batch* b, int mode) {
   if (!b || (mode != 0 && mode != 1)) { set_error("batch_set_flush: mode 0 (mma.sync) or 1 (tcgen05)"); return PQMC_ERR_ARG; }
+  for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_flush(p, mode));
   b->flush_mode = mode;
+  return PQMC_OK;
+}
+
+int pqmc_batch_set_graphs(pqmc_batch* b, int enable) {
+  if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  if (enable && b->precision != PQMC_PREC_MIXED) {
+    set_error("batch_set_graphs: slice graphs belong to mixed-precision batches");
+    return PQMC_ERR_ARG;
+  }
+  for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_graphs(p, enable));
+  PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  b->graphs = enable != 0;
+  if (!b->graphs) drop_graphs(b);
+  return PQMC_OK;
+}
+
+int pqmc_batch_graph_count(pqmc_batch* b, int* n) {
+  if (!b || !n) { set_error("batch_graph_count: null argument"); return PQMC_ERR_ARG; }
+  int total = (int)b->gcache.size();
+  for (auto* p : b->parts) {
+    int k = 0;
+    PQMC_TRY(pqmc_batch_graph_count(p, &k));
+    total += k;
+  }
+  *n = total;
   return PQMC_OK;
 }
 
 int pqmc_batch_set_delay(pqmc_batch* b, int kd) {
   if (!b || kd < 1 || kd > SCAN_KSTAGE) { set_error("batch_set_delay: depth must be in 1..%d", SCAN_KSTAGE); return PQMC_ERR_ARG; }
+  for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_delay(p, kd));
   b->kd = kd;
   return PQMC_OK;
 }
 
 int pqmc_batch_init(pqmc_batch* b) {
   if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  if (!b->parts.empty()) {
+    for (auto* p : b->parts) PQMC_TRY(pqmc_batch_init(p));
+    return PQMC_OK;
+  }
   for (auto* c : b->chains) PQMC_TRY(launch_init_expkv(c, 0, c->ntime));
   for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
   pqmc_chain* c0 = b->chains[0];
@@ -1659,6 +1874,7 @@ int pqmc_batch_init(pqmc_batch* b) {
 
 int pqmc_batch_set_timing(pqmc_batch* b, int enable) {
   if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_timing(p, enable));
   PQMC_CUDA(cudaStreamSynchronize(b->stream));
   PQMC_TRY(phase_resolve(b));
   b->timing = enable != 0;
@@ -1677,6 +1893,16 @@ int pqmc_batch_get_timing(pqmc_batch* b, double* ms, long long* launches) {
     ms[k] = b->phase_ms[k];
     launches[k] = b->phase_n[k];
   }
+  // an uneven batch: the sum over its classes (which overlap on the device)
+  for (auto* p : b->parts) {
+    double pm[PQMC_N_PHASES];
+    long long pn[PQMC_N_PHASES];
+    PQMC_TRY(pqmc_batch_get_timing(p, pm, pn));
+    for (int k = 0; k < PQMC_N_PHASES; ++k) {
+      ms[k] += pm[k];
+      launches[k] += pn[k];
+    }
+  }
   return PQMC_OK;
 }
 
@@ -1687,6 +1913,26 @@ int pqmc_batch_info(pqmc_batch* b, int* info) {
   info[2] = b->kd;
   info[3] = b->flush_mode;
   info[4] = b->precision;
+  return PQMC_OK;
+}
+
+int pqmc_batch_classes(pqmc_batch* b, int* n) {
+  if (!b || !n) { set_error("batch_classes: null argument"); return PQMC_ERR_ARG; }
+  *n = b->parts.empty() ? 1 : (int)b->parts.size();
+  return PQMC_OK;
+}
+
+int pqmc_batch_class_info(pqmc_batch* b, int k, int* info) {
+  if (!b || !info) { set_error("batch_class_info: null argument"); return PQMC_ERR_ARG; }
+  const int n = b->parts.empty() ? 1 : (int)b->parts.size();
+  if (k < 0 || k >= n) { set_error("batch_class_info: class %d of %d", k, n); return PQMC_ERR_ARG; }
+  pqmc_batch* p = b->parts.empty() ? b : b->parts[k];
+  info[0] = (int)p->chains.size();
+  info[1] = p->chains[0]->ns;
+  info[2] = p->chains[0]->ntime;
+  info[3] = p->kd;
+  info[4] = p->flush_mode;
+  info[5] = p->n_groups;
   return PQMC_OK;
 }
 
@@ -1703,6 +1949,23 @@ int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, con
     return PQMC_ERR_ARG;
   }
   if (b->precision != PQMC_PREC_MIXED) { set_error("batch_autotune: mixed batches only"); return PQMC_ERR_ARG; }
+  if (!b->parts.empty()) {
+    // every class tunes its own depth; ms_out sums the classes' ms per slice
+    std::vector<double> part_ms(n_candidates);
+    if (ms_out)
+      for (int i = 0; i < n_candidates; ++i) ms_out[i] = 0.0;
+    for (size_t k = 0; k < b->parts.size(); ++k) {
+      int bk = 0;
+      PQMC_TRY(pqmc_batch_autotune(b->parts[k], loop, first_tc, n_slices, candidates, n_candidates, &bk,
+                                   part_ms.data()));
+      if (k == 0) *best = bk;
+      if (ms_out)
+        for (int i = 0; i < n_candidates; ++i) ms_out[i] += part_ms[i];
+    }
+    b->kd = *best;
+    b->flush_mode = b->parts[0]->flush_mode;
+    return PQMC_OK;
+  }
   pqmc_chain* c0 = b->chains[0];
   const int nt = c0->ntime;
   cudaEvent_t e0, e1;
@@ -1712,6 +1975,10 @@ int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, con
   int best_kd = b->kd;
   int lp = loop, tc = first_tc;
   int st = PQMC_OK;
+  // candidates are timed with plain launches (a first capture would bias
+  // the comparison); the graphs of the chosen depth are captured afterwards
+  const bool graphs = b->graphs;
+  b->graphs = false;
   for (int i = 0; i < n_candidates && st == PQMC_OK; ++i) {
     const int kd = candidates[i];
     if (kd < 1 || kd > SCAN_KSTAGE) { st = PQMC_ERR_ARG; set_error("batch_autotune: depth %d out of range", kd); break; }
@@ -1731,6 +1998,7 @@ int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, con
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  b->graphs = graphs;
   if (st != PQMC_OK) return st;
   b->kd = best_kd;
   b->flush_mode = best_kd <= UM_KP ? 1 : 0;
@@ -1740,6 +2008,11 @@ int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, con
 
 int pqmc_batch_set_measure(pqmc_batch* b, int warmup, int meas_interval, int meas_number) {
   if (!b || meas_interval < 1 || meas_number < 0) { set_error("batch_set_measure: bad arguments"); return PQMC_ERR_ARG; }
+  if (!b->parts.empty()) {
+    for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_measure(p, warmup, meas_interval, meas_number));
+    b->meas_on = 1;
+    return PQMC_OK;
+  }
   pqmc_chain* c0 = b->chains[0];
   if (c0->ntime / 2 - meas_number < 1 || c0->ntime / 2 + meas_number > c0->ntime - 1) {
     set_error("measurement window ntime/2 +- %d leaves 1..ntime-1", meas_number);
@@ -1760,6 +2033,7 @@ int pqmc_batch_records(pqmc_batch* b, int i, double* out, int cap, int* n) {
     set_error("batch_records: bad arguments");
     return PQMC_ERR_ARG;
   }
+  if (!b->parts.empty()) return pqmc_batch_records(b->parts[b->part_of[i]], b->index_in_part[i], out, cap, n);
   if (i >= (int)b->records.size()) { *n = 0; return PQMC_OK; }
   pqmc_chain* c = b->chains[i];
   const size_t w = 2 * (size_t)(PQMC_N_SCALAR + 2 * PQMC_N_FIELD * c->n_cell);
@@ -1777,19 +2051,10 @@ int pqmc_batch_chain(pqmc_batch* b, int i, pqmc_chain** chain) {
   return PQMC_OK;
 }
 
-int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices) {
-  if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
-  for (auto* c : b->chains)
-    if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
+// ---- a mixed sweep in three parts, so that the classes of an uneven batch
+// can interleave their slices on their own streams -------------------------
+static int mixed_begin(pqmc_batch* b, int first_tc, int n_slices) {
   pqmc_chain* c0 = b->chains[0];
-  if (first_tc < 1 || n_slices < 0) { set_error("batch_sweep_slices: bad slice range"); return PQMC_ERR_ARG; }
-  if (b->precision == PQMC_PREC_FP64) {
-    for (auto* c : b->chains) {
-      const int n = std::min(n_slices, c->ntime - first_tc + 1);
-      if (n > 0) PQMC_TRY(pqmc_sweep_slices(c, loop, first_tc, n));
-    }
-    return PQMC_OK;
-  }
   if (first_tc + n_slices - 1 > c0->ntime) {
     set_error("batch_sweep_slices: slices %d..%d outside 1..%d", first_tc, first_tc + n_slices - 1, c0->ntime);
     return PQMC_ERR_ARG;
@@ -1801,42 +2066,38 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
   const dim3 cgrid((unsigned)std::min<long>((ng2 + 255) / 256, 64), (unsigned)b->chains.size());
   k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 1, ng2, 0);
   PQMC_LAUNCHED();
-  // fork: the other group's stream starts after the work queued so far
+  // fork: the other groups' streams start after the work queued so far
+  return groups_fork(b);
+}
+
+// slice tc of sweep `loop` for every group, the recompute that closes a
+// block of ngroup slices, and the measurement window
+static int mixed_slice(pqmc_batch* b, int loop, int tc) {
+  pqmc_chain* c0 = b->chains[0];
   const int NG = b->n_groups;
-  PQMC_TRY(groups_fork(b));
   const bool forward = (loop % 2) == 0;
-  const bool upd = c0->M.local_update != 0;
-  for (int tc = first_tc; tc < first_tc + n_slices; ++tc) {
-    int time;
-    if (!forward) {
-      time = c0->ntime - tc + 1;
-      for (int pf = c0->n_pf - 1; pf >= 0; --pf) {
-        for (int g = 0; g < NG; ++g) PQMC_TRY(bwrap(b, g, pf, time, false));
-        b->parity ^= 1;
-        if (upd && c0->h_pf_v_exist[pf])
-          for (int g = 0; g < NG; ++g) PQMC_TRY(bupdate(b, g, pf, time));
-      }
-    } else {
-      time = tc;
-      for (int pf = 0; pf < c0->n_pf; ++pf) {
-        if (upd && c0->h_pf_v_exist[pf])
-          for (int g = 0; g < NG; ++g) PQMC_TRY(bupdate(b, g, pf, time));
-        for (int g = 0; g < NG; ++g) PQMC_TRY(bwrap(b, g, pf, time, true));
-        b->parity ^= 1;
-      }
-    }
-    if (tc % c0->ngroup == 0) {
-      for (int g = 0; g < NG; ++g) PQMC_TRY(bscratch(b, g, forward ? time + 1 : time, forward));
-      b->parity ^= 1;
-    }
-    const int half = c0->ntime / 2;
-    if (b->meas_on && loop > b->meas_warmup && ((loop - b->meas_warmup) % b->meas_interval) == 0 &&
-        time >= half - b->meas_number && time <= half + b->meas_number)
-      PQMC_TRY(batch_measure(b, time, forward));
+  const int time = forward ? tc : c0->ntime - tc + 1;
+  for (int g = 0; g < NG; ++g) PQMC_TRY(group_slice(b, g, forward, time, b->parity));
+  b->parity ^= (c0->n_pf & 1);
+  if (tc % c0->ngroup == 0) {
+    for (int g = 0; g < NG; ++g) PQMC_TRY(bscratch(b, g, forward ? time + 1 : time, forward, b->parity));
+    b->parity ^= 1;
   }
-  // join, then G back to FP64 in the current buffer of every chain
+  const int half = c0->ntime / 2;
+  if (b->meas_on && loop > b->meas_warmup && ((loop - b->meas_warmup) % b->meas_interval) == 0 &&
+      time >= half - b->meas_number && time <= half + b->meas_number)
+    PQMC_TRY(batch_measure(b, time, forward));
+  return PQMC_OK;
+}
+
+// join, then G back to FP64 in the current buffer of every chain; returns
+// after the batch's work is done
+static int mixed_end(pqmc_batch* b) {
+  pqmc_chain* c0 = b->chains[0];
   PQMC_TRY(groups_join(b));
   PQMC_TRY(batch_sync_parity(b));
+  const long ng2 = (long)c0->ns * c0->ns;
+  const dim3 cgrid((unsigned)std::min<long>((ng2 + 255) / 256, 64), (unsigned)b->chains.size());
   k_gconv<<<cgrid, 256, 0, b->stream>>>(b->d_desc, 0, ng2, 0);
   PQMC_LAUNCHED();
   int err = 0;
@@ -1850,13 +2111,70 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
   return PQMC_OK;
 }
 
+// the classes of an uneven batch advance together: class k runs n[k] slices
+// from first_tc, its slices spread evenly over the call so that every class
+// keeps work queued until the end
+static int classes_run(pqmc_batch* b, int loop, int first_tc, const std::vector<int>& n) {
+  const size_t P = b->parts.size();
+  PQMC_CUDA(cudaEventRecord(b->ev_fork, b->stream));
+  int S = 0;
+  for (size_t k = 0; k < P; ++k) {
+    if (n[k] <= 0) continue;
+    PQMC_CUDA(cudaStreamWaitEvent(b->parts[k]->stream, b->ev_fork, 0));
+    PQMC_TRY(mixed_begin(b->parts[k], first_tc, n[k]));
+    S = std::max(S, n[k]);
+  }
+  std::vector<int> done(P, 0);
+  for (int step = 1; step <= S; ++step)
+    for (size_t k = 0; k < P; ++k) {
+      const int target = (int)(((long)step * n[k] + S - 1) / S);
+      while (done[k] < target) PQMC_TRY(mixed_slice(b->parts[k], loop, first_tc + done[k]++));
+    }
+  int st = PQMC_OK;
+  for (size_t k = 0; k < P; ++k) {
+    if (n[k] <= 0) continue;
+    const int sk = mixed_end(b->parts[k]);
+    if (st == PQMC_OK) st = sk;
+  }
+  return st;
+}
+
+int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices) {
+  if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  for (auto* c : b->chains)
+    if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
+  if (first_tc < 1 || n_slices < 0) { set_error("batch_sweep_slices: bad slice range"); return PQMC_ERR_ARG; }
+  if (b->precision == PQMC_PREC_FP64) {
+    for (auto* c : b->chains) {
+      const int n = std::min(n_slices, c->ntime - first_tc + 1);
+      if (n > 0) PQMC_TRY(pqmc_sweep_slices(c, loop, first_tc, n));
+    }
+    return PQMC_OK;
+  }
+  if (!b->parts.empty()) {
+    // uneven batch: each class takes the slices that exist in its sweep
+    std::vector<int> n(b->parts.size());
+    for (size_t k = 0; k < n.size(); ++k) n[k] = std::min(n_slices, b->parts[k]->chains[0]->ntime - first_tc + 1);
+    return classes_run(b, loop, first_tc, n);
+  }
+  PQMC_TRY(mixed_begin(b, first_tc, n_slices));
+  for (int tc = first_tc; tc < first_tc + n_slices; ++tc) PQMC_TRY(mixed_slice(b, loop, tc));
+  return mixed_end(b);
+}
+
 int pqmc_batch_sweep(pqmc_batch* b, int loop) {
   if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
+  for (auto* c : b->chains)
+    if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
   if (b->precision == PQMC_PREC_FP64) {
-    for (auto* c : b->chains)
-      if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
     for (auto* c : b->chains) PQMC_TRY(pqmc_sweep(c, loop, 1, 1 << 30, 1, 0, nullptr, 0, nullptr));
     return PQMC_OK;
+  }
+  if (!b->parts.empty()) {
+    // one whole sweep of every chain, each class over its own ntime slices
+    std::vector<int> n(b->parts.size());
+    for (size_t k = 0; k < n.size(); ++k) n[k] = b->parts[k]->chains[0]->ntime;
+    return classes_run(b, loop, 1, n);
   }
   return pqmc_batch_sweep_slices(b, loop, 1, b->chains[0]->ntime);
 }

@@ -670,6 +670,11 @@ int pqmc_create(const pqmc_model* model, pqmc_chain** out) {
     delete c;
     return st;
   }
+  c->hmodel = *model;
+  c->hmodel.pf_dim = c->hmodel.pf_npla = c->hmodel.pf_k_exist = c->hmodel.pf_v_exist = nullptr;
+  c->hmodel.pf_k_coe = c->hmodel.pf_v_coe = c->hmodel.pf_kmat = c->hmodel.pf_vmat = nullptr;
+  c->hmodel.pla_site_list = c->hmodel.bf_list = c->hmodel.boundary_crossing = nullptr;
+  c->hmodel.bc_phases = nullptr;
   *out = c;
   return PQMC_OK;
 }
@@ -763,6 +768,24 @@ int pqmc_get_state(pqmc_chain* c, pqmc_state* out) {
   out->negative_accept = h.neg_acc;
   for (int k = 0; k < 5; ++k) out->rng[k] = h.rng[k];
   out->reserved = 0;
+  return PQMC_OK;
+}
+
+int pqmc_set_state(pqmc_chain* c, const pqmc_state* st) {
+  CHK_CHAIN(c);
+  if (!st) { set_error("null state"); return PQMC_ERR_ARG; }
+  DevScalars h;
+  PQMC_CUDA(cudaMemcpyAsync(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  h.err_fast_max = st->err_fast_max;
+  h.err_fast = st->err_fast;
+  h.err_g = st->err_g;
+  h.err_g_rel_max = st->err_g_rel_max;
+  h.pos_acc = st->positive_accept;
+  h.neg_acc = st->negative_accept;
+  for (int k = 0; k < 5; ++k) h.rng[k] = st->rng[k];
+  PQMC_CUDA(cudaMemcpyAsync(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  PQMC_CUDA(cudaStreamSynchronize(c->stream));
   return PQMC_OK;
 }
 

@@ -106,6 +106,13 @@ struct pqmc_chain {
   cplx h_bc[2];
   double hop = 1.0, ep = 1.0;
   cplx* m_gtmp = nullptr;           // g = I - g_h
+  // host copy of the model's scalars (table pointers cleared)
+  pqmc_model hmodel;
+  // global moves (pqmc_set_global)
+  bool have_global = false;
+  pqmc_global_params gp;
+  std::vector<double> g_rpos;
+  long long g_acc = 0, g_rej = 0;
 };
 
 namespace pqmc {

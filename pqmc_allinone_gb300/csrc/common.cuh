@@ -72,6 +72,17 @@ inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_
     }                                                                          \
   } while (0)
 
+// raise a kernel's dynamic shared-memory limit to at least `bytes`, never
+// lower it: batches of different sizes live side by side in one context
+template <typename F>
+inline cudaError_t raise_dyn_smem(F* fn, int bytes) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, (const void*)fn);
+  if (e != cudaSuccess) return e;
+  if (a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 #define PQMC_TRY(expr)                                                         \
   do {                                                                         \
     int s__ = (expr);                                                          \

@@ -411,8 +411,11 @@ int pqmc_sweep(pqmc_chain* c, int first_loop, int n_sweeps, int warmup, int meas
     return PQMC_ERR_ARG;
   }
   int nrec = 0;
-  for (int loop = first_loop; loop < first_loop + n_sweeps; ++loop)
+  for (int loop = first_loop; loop < first_loop + n_sweeps; ++loop) {
+    // global step before the sweep (Main_PQMC.f90:87-96), once enabled
+    if (c->have_global) PQMC_TRY(pqmc_global_step(c, loop, nullptr));
     PQMC_TRY(sweep_one(c, loop, warmup, meas_interval, meas_number, records, n_records_cap, &nrec));
+  }
   PQMC_CUDA(cudaStreamSynchronize(c->stream));
   if (n_records) *n_records = nrec;
   return PQMC_OK;

@@ -841,22 +841,22 @@ int BatchRecompute::setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s
       set_error("batch recompute: %zu bytes of shared memory needed for the propagation", smem);
       return PQMC_ERR_ARG;
     }
-    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    PQMC_CUDA(cudaFuncSetAttribute(k_bprop_df<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PQMC_CUDA(raise_dyn_smem(k_bprop_df<1>, (int)smem));
+    PQMC_CUDA(raise_dyn_smem(k_bprop_df<2>, (int)smem));
+    PQMC_CUDA(raise_dyn_smem(k_bprop_df<3>, (int)smem));
+    PQMC_CUDA(raise_dyn_smem(k_bprop_df<4>, (int)smem));
     const size_t tsm = sizeof(dfc) * TRI_WARPS * (size_t)ne;
     if (tsm + 1024 > (size_t)optin) {
       set_error("batch recompute: nelec %d too large for the triangular inverse", ne);
       return PQMC_ERR_ARG;
     }
-    PQMC_CUDA(cudaFuncSetAttribute(k_tri_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    PQMC_CUDA(raise_dyn_smem(k_tri_inv, (int)tsm));
     // the cluster Gauss-Jordan needs a quarter of the matrix per block in shared memory
     const size_t gsm = sizeof(dfc) * (size_t)((ne + GJ_CL - 1) / GJ_CL) * ne;
     gj_cluster = ne <= GJ_MAXN && gsm + 20480 <= (size_t)optin;
     if (gj_cluster) {
-      PQMC_CUDA(cudaFuncSetAttribute(k_gj_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
-      PQMC_CUDA(cudaFuncSetAttribute(k_chol_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
+      PQMC_CUDA(raise_dyn_smem(k_gj_cluster, (int)gsm));
+      PQMC_CUDA(raise_dyn_smem(k_chol_cluster, (int)gsm));
     }
   }
   return PQMC_OK;

@@ -31,7 +31,7 @@ import ctypes
 
 import numpy as np
 
-from .abi import MeasStruct, ModelStruct, PqmcError, PqmcState, check, load_library
+from .abi import MeasStruct, ModelStruct, PqmcError, PqmcState, check, global_struct, load_library
 from .model import Model, record_width
 
 _f64p = ctypes.POINTER(ctypes.c_double)
@@ -128,6 +128,34 @@ class PqmcChain:
         self._chk(self.lib.pqmc_get_state(self.h, ctypes.byref(s)), "pqmc_get_state")
         return s.as_dict()
 
+    # ---- global moves (update_global, mod_update.f90:250-467) -----------
+    def set_global(self, gp: dict):
+        """Global-move parameters (abi.global_params); pqmc_sweep then runs
+        the driver's global step before every qualifying sweep."""
+        s, keep = global_struct(gp)
+        self._gkeep = keep
+        self._chk(self.lib.pqmc_set_global(self.h, ctypes.byref(s)), "pqmc_set_global")
+
+    def update_global(self, kind: int) -> bool:
+        a = np.zeros(1, dtype=np.int32)
+        self._chk(self.lib.pqmc_update_global(self.h, kind, a.ctypes.data_as(_i32p)), "update_global")
+        return bool(a[0])
+
+    def global_step(self, loop: int) -> int:
+        a = np.zeros(1, dtype=np.int32)
+        self._chk(self.lib.pqmc_global_step(self.h, loop, a.ctypes.data_as(_i32p)), "pqmc_global_step")
+        return int(a[0])
+
+    def global_counters(self) -> tuple[int, int]:
+        a, r = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._chk(self.lib.pqmc_global_counters(self.h, ctypes.byref(a), ctypes.byref(r)), "pqmc_global_counters")
+        return int(a.value), int(r.value)
+
+    def set_state(self, st: dict):
+        """Restore rng, accept counters and error maxima (a checkpoint's state())."""
+        s = PqmcState.from_dict(st)
+        self._chk(self.lib.pqmc_set_state(self.h, ctypes.byref(s)), "pqmc_set_state")
+
     def qd(self, blk: int):
         q = np.zeros((self.m.ns, self.m.nelec), dtype=np.complex128, order="F")
         d = np.zeros(self.m.nelec, dtype=np.complex128)
@@ -209,6 +237,24 @@ class PqmcChain:
         self._chk(self.lib.pqmc_sweep(self.h, first_loop, n_sweeps, warmup, meas_interval, meas_number,
                                       recs.ctypes.data_as(_f64p), cap, ctypes.byref(n)), "sweep")
         return recs[: n.value]
+
+
+def global_generate(m: Model, gp: dict, kind: int, words, field):
+    """pqmc_global_generate: the field of a global move on the host (no GPU).
+    Returns (new field (n_bf, ntime), ph_ln_cw, t_first, t_last, rng words)."""
+    lib = load_library()
+    ms = ModelStruct(m)
+    s, keep = global_struct(gp)
+    f = np.array(field, dtype=np.float64, order="F", copy=True)
+    w = np.array([int(x) for x in words], dtype=np.int32)
+    ph = np.zeros(1)
+    t = np.zeros(2, dtype=np.int32)
+    check(lib, lib.pqmc_global_generate(ctypes.byref(ms.s), ctypes.byref(s), kind, w.ctypes.data_as(_i32p),
+                                        f.ctypes.data_as(_f64p), ph.ctypes.data_as(_f64p),
+                                        t[:1].ctypes.data_as(_i32p), t[1:].ctypes.data_as(_i32p)),
+          "pqmc_global_generate")
+    del keep
+    return f, float(ph[0]), int(t[0]), int(t[1]), [int(x) for x in w]
 
 
 def kernel_launches() -> int:
@@ -306,6 +352,28 @@ class PqmcBatch:
         check(self.lib, self.lib.pqmc_batch_records(self.h, i, out.ctypes.data_as(_f64p), cap,
                                                      n.ctypes.data_as(_i32p)), "pqmc_batch_records")
         return out[:n[0]].view(np.complex128)
+
+    def set_graphs(self, enable: bool):
+        """Replay each slice's family steps from a captured CUDA graph."""
+        check(self.lib, self.lib.pqmc_batch_set_graphs(self.h, 1 if enable else 0), "pqmc_batch_set_graphs")
+
+    def classes(self) -> list:
+        """Geometry classes of the batch: [{chains, ns, ntime, delay_depth, flush, groups}]."""
+        n = np.zeros(1, dtype=np.int32)
+        check(self.lib, self.lib.pqmc_batch_classes(self.h, n.ctypes.data_as(_i32p)), "pqmc_batch_classes")
+        out = []
+        for k in range(int(n[0])):
+            v = np.zeros(6, dtype=np.int32)
+            check(self.lib, self.lib.pqmc_batch_class_info(self.h, k, v.ctypes.data_as(_i32p)),
+                  "pqmc_batch_class_info")
+            out.append({"chains": int(v[0]), "ns": int(v[1]), "ntime": int(v[2]), "delay_depth": int(v[3]),
+                        "flush": "tcgen05" if v[4] == 1 else "mma.sync", "groups": int(v[5])})
+        return out
+
+    def graph_count(self) -> int:
+        n = np.zeros(1, dtype=np.int32)
+        check(self.lib, self.lib.pqmc_batch_graph_count(self.h, n.ctypes.data_as(_i32p)), "pqmc_batch_graph_count")
+        return int(n[0])
 
     def set_flush(self, mode: int):
         """1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush."""

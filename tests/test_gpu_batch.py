@@ -177,3 +177,68 @@ def test_mixed_observables_within_error_bars():
         assert z.size > 0 and z.max() < 5.0, z.max()
         # components without spread must agree outright
         assert np.allclose(a.mean(axis=0)[~ok], p.mean(axis=0)[~ok], rtol=1e-6, atol=1e-9)
+
+
+def _run_batch(ms, loops, graphs=False, chains_only=None):
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    if graphs:
+        b.set_graphs(True)
+    b.init()
+    for loop in loops:
+        b.sweep(loop)
+    out = [(c.field(), c.g(), c.state()) for c in b.chains]
+    n_graphs = b.graph_count()
+    classes = b.classes()
+    b.close()
+    return out, n_graphs, classes
+
+
+def test_slice_graphs_bit_identical():
+    """The family steps of a slice replayed from captured CUDA graphs give
+    the same chains, bit for bit, as the same launches issued one by one:
+    one graph per direction and G-buffer parity serves every slice."""
+    ms = []
+    for i in range(3):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=120 + i)
+        ms.append((m, f, seed_words(1200 + i)))
+    eager, n0, _ = _run_batch(ms, (1, 2), graphs=False)
+    graph, n1, _ = _run_batch(ms, (1, 2), graphs=True)
+    assert n0 == 0 and n1 == 4      # {backward, forward} x {parity 0, 1}
+    for (f0, g0, s0), (f1, g1, s1) in zip(eager, graph):
+        assert np.array_equal(f0, f1) and np.array_equal(g0, g1)
+        assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
+        assert s0["positive_accept"] > 0
+
+
+def test_uneven_batch_matches_its_classes():
+    """A mixed batch of chains of uneven L and Lt (C3-shaped, scaled down)
+    splits into geometry classes that interleave on their own streams; every
+    chain must come out bit-identical to the same chain advanced in a batch of
+    its class alone, and after the sweeps its G (the stabilised recompute at
+    the sweep boundary) must match the FP64 oracle on the chain's own field."""
+    from oracle.oracle import OracleChain
+    rng = np.random.default_rng(7)
+    geo = [(4, 20), (6, 40), (4, 40), (6, 20), (4, 20), (6, 40), (4, 40)]
+    ms = []
+    for i, (L, nt) in enumerate(geo):
+        lam = float(rng.uniform(0.5, 1.0))
+        m, f = epsocz_small(L=L, ntime=nt, ngroup=10, lam=lam, alpha=0.3, seed=1000 + i)
+        ms.append((m, f, seed_words(1000 + i)))
+    mixed, n_graphs, classes = _run_batch(ms, (1, 2), graphs=True)
+    assert len(classes) == 4 and sum(c["chains"] for c in classes) == len(geo)
+    assert sorted((c["ns"], c["ntime"]) for c in classes) == [(32, 20), (32, 40), (72, 20), (72, 40)]
+    assert n_graphs == 4 * 4
+    for key in sorted(set(geo)):
+        idx = [i for i, g in enumerate(geo) if g == key]
+        alone, _, _ = _run_batch([ms[i] for i in idx], (1, 2), graphs=False)
+        for i, (f1, g1, s1) in zip(idx, alone):
+            f0, g0, s0 = mixed[i]
+            assert np.array_equal(f0, f1) and np.array_equal(g0, g1), (key, i)
+            assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
+    for (m, _, w), (f, g, s) in zip(ms, mixed):
+        assert s["positive_accept"] > 0 and s["negative_accept"] > 0
+        o = OracleChain(m, field=f, seed_words=w, meas=False)
+        o.init_expkv()
+        o.init_g(1)
+        assert rel_fro(g, o.g()) < MIXED_RECOMPUTE_TOL

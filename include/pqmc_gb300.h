@@ -345,7 +345,9 @@ int pqmc_batch_set_delay(pqmc_batch* batch, int depth);
  * delays use 0), 0 = mma.sync split-BF16 tiles */
 int pqmc_batch_set_flush(pqmc_batch* batch, int mode);
 /* one sweep of every chain (Main_PQMC.f90:99-154); equal-time
- * measurements only after pqmc_batch_set_measure */
+ * measurements only after pqmc_batch_set_measure; chains with global moves
+ * enabled (pqmc_set_global on pqmc_batch_chain) take the driver's global
+ * step first (Main_PQMC.f90:87-96), one chain after another */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
 /* Equal-time measurement inside batched sweeps with the reference's window
  * and cadence (loop > warmup, mod(loop-warmup, meas_interval) == 0, time in
@@ -376,7 +378,7 @@ int pqmc_batch_init(pqmc_batch* batch);
 int pqmc_batch_stream(pqmc_batch* batch, void** stream);
 /* info[5] = {chains, chain groups (streams), delay depth, flush engine,
  * precision}; the groups default to one per 16 chains (at most 4) and can
- * be set with the environment variable PQMC_BATCH_GROUPS (1..4) at creation */
+ * be set with the environment variable PQMC_BATCH_GROUPS (1..8) at creation */
 int pqmc_batch_info(pqmc_batch* batch, int* info);
 /* Uneven batches (mixed precision): chains of different geometry (Ns, Lt,
  * families) are grouped into classes of equal geometry; each class runs

@@ -432,6 +432,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   }
   const int rb = d.rb, nrb = d.nrb;
   const int io = (ns <= SCAN_THREADS - 32) ? SCAN_THREADS - 32 : 0;
+  const bool row_warp = warp * 32 < ns;   // holds a row of G (every warp when RPT = 2)
   const ScanLayout L = scan_layout(npla, ns, ldp, qc, kd, 4 * nrb * rb * (int)sizeof(float4));
   float4* s_rows = reinterpret_cast<float4*>(s_dyn + L.rows);     // [dim][nrb*rb] rows of G at S
   float2* s_stage = reinterpret_cast<float2*>(s_dyn + L.stage);
@@ -562,7 +563,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       phase ^= 1u << st;
       const float2* cA = s_stage + (size_t)st * 2 * qc * ldp;
       const float2* cB = cA + (size_t)qc * ldp;
-      const int nq = min(qc, K - c * qc);
+      // warps without a row of G skip the column loop: the broadcast loads
+      // of the accepted sites' panel entries are its shared-memory bound
+      const int nq = row_warp ? min(qc, K - c * qc) : 0;
 #pragma unroll 2
       for (int qq = 0; qq < nq; ++qq) {
         float2 bs[dim], as[dim];
@@ -1202,7 +1205,7 @@ struct pqmc_batch {
   cudaStream_t stream = nullptr;   // the stream of group 0, the batch's public stream
   // chain groups: each group has its own stream and recompute workspace, so
   // one group's latency-bound scan overlaps the other's flush and recompute
-  static constexpr int MAX_GROUPS = 4;
+  static constexpr int MAX_GROUPS = 8;
   int n_groups = 1;
   int g_first[MAX_GROUPS] = {}, g_count[MAX_GROUPS] = {};
   cudaStream_t g_stream[MAX_GROUPS] = {};
@@ -1747,10 +1750,10 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
   PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
-  // two chain groups on two streams for mixed batches of 16 chains or more
-  // chain groups: PQMC_BATCH_GROUPS (1..4) when set, else 2 for 16 chains or more
+  // chain groups: PQMC_BATCH_GROUPS (1..8) when set, else one per 16 chains
+  // (at most 4)
   {
-    int ng = precision == PQMC_PREC_MIXED ? n_chains / 16 : 1;
+    int ng = precision == PQMC_PREC_MIXED ? std::min(n_chains / 16, 4) : 1;
     const char* env = getenv("PQMC_BATCH_GROUPS");
     if (env && precision == PQMC_PREC_MIXED) ng = atoi(env);
     ng = std::max(1, std::min(std::min(ng, (int)pqmc_batch::MAX_GROUPS), n_chains));
@@ -2166,6 +2169,10 @@ int pqmc_batch_sweep(pqmc_batch* b, int loop) {
   if (!b) { set_error("null batch"); return PQMC_ERR_ARG; }
   for (auto* c : b->chains)
     if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
+  // the driver's global step of every chain with global moves enabled
+  // (Main_PQMC.f90:87-96), chain after chain, before the batched sweep
+  for (auto* c : b->chains)
+    if (c->have_global) PQMC_TRY(pqmc_global_step(c, loop, nullptr));
   if (b->precision == PQMC_PREC_FP64) {
     for (auto* c : b->chains) PQMC_TRY(pqmc_sweep(c, loop, 1, 1 << 30, 1, 0, nullptr, 0, nullptr));
     return PQMC_OK;

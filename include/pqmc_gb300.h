@@ -322,9 +322,12 @@ int pqmc_set_field_device(pqmc_chain* chain, const double* boson_field_dev);
  * Green's-function trace formula Re Tr[E^-1 dE/dx G] per plaquette, by a
  * right-to-left pass that checkpoints the orthonormal left factor every
  * ngroup slices and a left-to-right pass that recomputes G from the
- * checkpoints and wraps it through each block.  Needs init_expkv/init_g
- * (with the current field) first; leaves G and the Q/D strings as they were
- * (the rank's fast-update state is not disturbed). */
+ * checkpoints and wraps it through each block.  Needs the expKV of the
+ * current field (pqmc_init_expkv) and the trial state; init_g_T0 is not
+ * needed.  Leaves G and the Q/D strings as they were (the rank's
+ * fast-update state is not disturbed); ln_cw is set to the value, as
+ * cal_new_weight_T0 sets it.  Calls on different chains may run from
+ * different host threads at the same time. */
 int pqmc_logweight_grad(pqmc_chain* chain, double* logw_out, double* grad_dev);
 
 /* ---- batched, mixed precision --------------------------------------- */

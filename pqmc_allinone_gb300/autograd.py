@@ -7,12 +7,28 @@ backward returns ``dW/dx`` from the hand-written adjoint
 (``pqmc_logweight_grad``: checkpointed left factors every ngroup slices and
 the Green's-function trace formula, csrc/adjoint.cu).  Each chain is a
 ``PqmcChain`` of matching model; its fast-update state is not disturbed.
+
+The chains are independent: each runs on its own CUDA stream, driven from
+its own host thread (the C-ABI allows one thread per chain handle), so the
+small per-chain kernels of different chains overlap on the GPU.  The
+thread count is ``PQMC_GRAD_THREADS`` (default: up to 8).
 """
 from __future__ import annotations
+
+import concurrent.futures as cf
+import os
 
 import torch
 
 from .engine import PqmcChain
+
+
+def _threads(n: int) -> int:
+    try:
+        t = int(os.environ.get("PQMC_GRAD_THREADS", "8"))
+    except ValueError:
+        t = 8
+    return max(1, min(n, t))
 
 
 class LogWeight(torch.autograd.Function):
@@ -28,12 +44,21 @@ class LogWeight(torch.autograd.Function):
         grads = torch.empty_like(xf)
         vals = torch.empty(B, dtype=torch.float64)
         torch.cuda.synchronize()
-        for b, ch in enumerate(chains):
+
+        def one(b: int) -> float:
+            ch = chains[b]
             ch.set_field_device(xf[b].data_ptr())
             ch.init_expkv()
-            ch.init_g(1)
-            w = ch.logweight_grad_device(grads[b].data_ptr())
-            vals[b] = w.real
+            return ch.logweight_grad_device(grads[b].data_ptr()).real
+
+        nt = _threads(B)
+        if nt == 1:
+            for b in range(B):
+                vals[b] = one(b)
+        else:
+            with cf.ThreadPoolExecutor(max_workers=nt) as ex:
+                for b, w in enumerate(ex.map(one, range(B))):
+                    vals[b] = w
         ctx.save_for_backward(grads.transpose(1, 2))
         return vals.to(x.device)
 

@@ -9,8 +9,9 @@
 // acts (the matrix the local update at (f,tau) sees), and c = ncopy (x2 under
 // TR_weight).
 //
-// Reverse sweep with checkpoints: a right-to-left pass (the value) stores the
-// orthonormal left factor every ngroup slices; a left-to-right pass recomputes
+// Reverse sweep with checkpoints: one right-to-left pass gives the value
+// (cal_new_weight_T0 from the trial state) and stores the orthonormal left
+// factor every ngroup slices; a left-to-right pass recomputes
 // G from the left checkpoint and the current right factor at each block start
 // and wraps it family by family through the block (the slices between
 // checkpoints are recomputed, not stored).
@@ -121,35 +122,38 @@ extern "C" int pqmc_set_field_device(pqmc_chain* c, const double* dfield) {
 // grad_dev: device, (n_bf, ntime) doubles (gradient of Re logw).
 extern "C" int pqmc_logweight_grad(pqmc_chain* c, double* logw_out, double* grad_dev) {
   if (!c || !grad_dev) { set_error("logweight_grad: null argument"); return PQMC_ERR_ARG; }
-  if (!c->have_g) { set_error("logweight_grad before init_g"); return PQMC_ERR_STATE; }
   const int ns = c->ns, ne = c->nelec, nt = c->ntime, ng = c->ngroup;
   cudaStream_t s = c->stream;
   const size_t qb = sizeof(cplx) * (size_t)ns * ne;
-  // checkpoints of the left factor at tau = 0, ng, 2ng, ... (adjoint layout X = L^H)
   const int nck = nt / ng + 1;
   cplx* ck = nullptr;
   PQMC_CUDA(cudaMallocAsync((void**)&ck, qb * nck, s));
-  // backward pass (right-to-left): X starts as Q(nblock) and absorbs B(nt) ... B(1)
-  PQMC_CUDA(cudaMemcpyAsync(c->xmat, c->q_string + (size_t)ns * ne * (c->nblock - 1), qb, cudaMemcpyDeviceToDevice, s));
-  int p = nt;
-  int slot = nt / ng;
-  if (nt % ng == 0) PQMC_CUDA(cudaMemcpyAsync(ck + (size_t)ns * ne * slot, c->xmat, qb, cudaMemcpyDeviceToDevice, s));
-  while (p >= 1) {
-    int lo = ((p - 1) / ng) * ng + 1;   // block of slices [lo, p]
-    PQMC_TRY(launch_propagate(c, c->xmat, ne, p, lo, false));
-    PQMC_TRY(house_qr(s, ns, ne, c->xmat, c->tau, c->dtmp));
-    slot = (lo - 1) / ng;
-    PQMC_CUDA(cudaMemcpyAsync(ck + (size_t)ns * ne * slot, c->xmat, qb, cudaMemcpyDeviceToDevice, s));
-    p = lo - 1;
+  // right-to-left pass: cal_new_weight_T0 with the orthonormal left factor
+  // checkpointed every ngroup slices (one propagation for value and
+  // checkpoints)
+  int st = do_new_weight_ck(c, ck);
+  int info = 0;
+  DevScalars h;
+  if (st == PQMC_OK && (cudaMemcpyAsync(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                        cudaStreamSynchronize(s) != cudaSuccess)) {
+    set_error("logweight_grad: reading the weight failed");
+    st = PQMC_ERR_CUDA;
   }
-  // value: the reference's own routine (LQ every ngroup from the top)
-  int st = pqmc_cal_new_weight(c, logw_out);
+  if (st == PQMC_OK) info = h.lu_info;
+  if (st == PQMC_OK && info != 0) {
+    set_error("logweight_grad: zero pivot %d", info);
+    st = PQMC_ERR_SINGULAR;
+  }
   if (st != PQMC_OK) {
     cudaFreeAsync(ck, s);
     return st;
   }
-  // forward pass: R starts as Q(1); at each block start G from the checkpoint
-  PQMC_CUDA(cudaMemcpyAsync(c->rmat, c->q_string, qb, cudaMemcpyDeviceToDevice, s));
+  if (logw_out) {
+    logw_out[0] = h.ln_cw.x;
+    logw_out[1] = h.ln_cw.y;
+  }
+  // forward pass: R starts as the trial state; at each block start G from the checkpoint
+  PQMC_CUDA(cudaMemcpyAsync(c->rmat, c->slater_q, qb, cudaMemcpyDeviceToDevice, s));
   const double scale = (double)c->M.ncopy * (c->M.tr_weight ? 2.0 : 1.0);
   cplx* gsave = c->g;   // keep the chain's G: compute into the pair (g, g_alt) then restore
   cplx* gsave_alt = c->g_alt;

@@ -447,6 +447,39 @@ int do_new_weight(pqmc_chain* c) {
   return PQMC_OK;
 }
 
+// cal_new_weight_T0 of the current field from the trial state alone (no
+// init_g_T0 needed), with the orthonormal left factor kept every ngroup
+// slices: ck[k] (Ns x nelec) is the factor at slice boundary k*ngroup, for
+// k = 0 .. ntime/ngroup (the adjoint's checkpoints).  Blocks are aligned to
+// multiples of ngroup from the bottom; the weight equals do_new_weight's up
+// to rounding.  Leaves G and the Q/D strings alone; ln_cw is set.
+int do_new_weight_ck(pqmc_chain* c, cplx* ck) {
+  const int ns = c->ns, ne = c->nelec, nt = c->ntime, ng = c->ngroup;
+  cudaStream_t s = c->stream;
+  const size_t qb = sizeof(cplx) * (size_t)ns * ne;
+  PQMC_CUDA(cudaMemcpyAsync(c->xmat, c->slater_q, qb, cudaMemcpyDeviceToDevice, s));
+  k_sumlog<<<1, 256, 0, s>>>(ne, c->slater_d, &c->sc->sumlogd, 0);
+  PQMC_LAUNCHED();
+  if (nt % ng == 0) PQMC_CUDA(cudaMemcpyAsync(ck + (size_t)ns * ne * (nt / ng), c->xmat, qb, cudaMemcpyDeviceToDevice, s));
+  for (int p = nt; p >= 1;) {
+    const int lo = ((p - 1) / ng) * ng + 1;   // slices [lo, p]
+    PQMC_TRY(launch_propagate(c, c->xmat, ne, p, lo, false));
+    PQMC_TRY(house_qr(s, ns, ne, c->xmat, c->tau, c->dtmp));
+    k_sumlog<<<1, 256, 0, s>>>(ne, c->dtmp, &c->sc->sumlogd, 1);
+    PQMC_LAUNCHED();
+    PQMC_CUDA(cudaMemcpyAsync(ck + (size_t)ns * ne * ((lo - 1) / ng), c->xmat, qb, cudaMemcpyDeviceToDevice, s));
+    p = lo - 1;
+  }
+  k_sumlog<<<1, 256, 0, s>>>(ne, c->slater_d, &c->sc->sumlogd, 1);
+  PQMC_LAUNCHED();
+  PQMC_TRY(zgemm(s, 'C', 'N', ne, ne, ns, mk(1.0), c->xmat, ns, c->slater_q, ns, mk(0.0), c->pbp, ne));
+  PQMC_TRY(lu_factor(s, ne, c->pbp, c->ipiv, &c->sc->lu_info, c->lcol));
+  PQMC_TRY(lu_logdet(s, ne, c->pbp, c->ipiv, &c->sc->logdet));
+  k_finish_weight<<<1, 1, 0, s>>>(c->sc, c->M.tr_weight, c->M.ncopy, 0);
+  PQMC_LAUNCHED();
+  return PQMC_OK;
+}
+
 // ---------------------------------------------------------------------------
 template <typename T>
 static int dalloc(T** p, size_t n) {

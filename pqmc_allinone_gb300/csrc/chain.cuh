@@ -126,6 +126,7 @@ int launch_propagate(pqmc_chain* c, cplx* X, int n, int t_from, int t_to, bool f
 int do_init_g(pqmc_chain* c, int start_time);
 int do_g_scratch(pqmc_chain* c, int time, bool forward, int loop);
 int do_new_weight(pqmc_chain* c);
+int do_new_weight_ck(pqmc_chain* c, cplx* ck);
 int block_log(pqmc_chain* c, int blk1);
 int do_measure(pqmc_chain* c, int time);
 int do_finish_record(pqmc_chain* c, int meas_number);

@@ -612,6 +612,20 @@ def run_uneven(args, world, rank, local):
         plain = {"value": C / est, "unit": "chain-sweeps/s", "sample_s_per_sweep_at_lt200": secs,
                  "method": "one plain FP64 chain per L at Lt=200 timed over one sweep; the batch's "
                            "sum of per-chain sweep times scaled by Lt (chains one after another)"}
+        # the FP64 batch (single-chain kernels, chains driven concurrently
+        # from host threads) on the first 24 chains of the mix, one sweep
+        sub = ms[:24]
+        fb = PqmcBatch([m for m, _, _ in sub], [f for _, f, _ in sub], [w for _, _, w in sub], precision=0)
+        fb.init()
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        fb.sweep(1)
+        torch.cuda.synchronize()
+        tb = time.perf_counter() - ta
+        fb.close()
+        plain["fp64_batch_sample"] = {"chains": len(sub), "seconds": tb, "value": len(sub) / tb,
+                                      "unit": "chain-sweeps/s",
+                                      "note": "PQMC_PREC_FP64 batch of the first 24 chains, one sweep, wall time"}
     if rank != 0:
         return
     Ls = [int(m.lat.dlength[0]) for m, _, _ in ms]

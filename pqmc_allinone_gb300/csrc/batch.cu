@@ -22,7 +22,11 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <atomic>
+#include <functional>
 #include <deque>
+#include <string>
+#include <thread>
 #include <vector>
 #include "chain.cuh"
 #include "linalg.cuh"
@@ -1541,6 +1545,38 @@ static int batch_measure(pqmc_batch* b, int time, bool forward) {
   return groups_fork(b);
 }
 
+// An FP64 batch runs the single-chain path of every chain; the chains are
+// independent (own buffers, own stream), so worker threads drive them
+// concurrently and their kernels overlap on the device.  The first failure
+// is reported with its message on the calling thread.
+static int fp64_each(pqmc_batch* b, const std::function<int(pqmc_chain*)>& fn) {
+  const int n = (int)b->chains.size();
+  int nw = 8;
+  if (const char* env = getenv("PQMC_BATCH_THREADS")) nw = atoi(env);
+  nw = std::max(1, std::min(nw, n));
+  if (nw == 1) {
+    for (auto* c : b->chains) PQMC_TRY(fn(c));
+    return PQMC_OK;
+  }
+  std::atomic<int> next{0}, status{PQMC_OK};
+  std::string msg;
+  std::atomic_flag have_msg = ATOMIC_FLAG_INIT;
+  auto work = [&]() {
+    for (int i = next++; i < n && status.load() == PQMC_OK; i = next++) {
+      const int st = fn(b->chains[i]);
+      if (st != PQMC_OK) {
+        int ok = PQMC_OK;
+        if (status.compare_exchange_strong(ok, st) && !have_msg.test_and_set()) msg = pqmc_last_error();
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nw; ++t) pool.emplace_back(work);
+  for (auto& t : pool) t.join();
+  if (status.load() != PQMC_OK) set_error("%s", msg.c_str());
+  return status.load();
+}
+
 // geometry of a mixed batch: chains of one class share every launch shape
 static bool same_geometry(const pqmc_model* a, const pqmc_model* b) {
   if (a->ns != b->ns || a->nelec != b->nelec || a->ntime != b->ntime || a->ngroup != b->ngroup ||
@@ -1866,10 +1902,8 @@ int pqmc_batch_init(pqmc_batch* b) {
   for (auto* c : b->chains) PQMC_TRY(launch_init_expkv(c, 0, c->ntime));
   for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
   pqmc_chain* c0 = b->chains[0];
-  if (b->precision == PQMC_PREC_FP64 || c0->ntime % c0->ngroup != 0) {
-    for (auto* c : b->chains) PQMC_TRY(pqmc_init_g(c, 1));
-    return PQMC_OK;
-  }
+  if (b->precision == PQMC_PREC_FP64 || c0->ntime % c0->ngroup != 0)
+    return fp64_each(b, [](pqmc_chain* c) { return pqmc_init_g(c, 1); });
   for (int g = 0; g < b->n_groups; ++g) PQMC_TRY(b->rec[g].init_g());
   for (auto* c : b->chains) c->have_g = true;
   return batch_refresh(b);
@@ -2147,13 +2181,11 @@ int pqmc_batch_sweep_slices(pqmc_batch* b, int loop, int first_tc, int n_slices)
   for (auto* c : b->chains)
     if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
   if (first_tc < 1 || n_slices < 0) { set_error("batch_sweep_slices: bad slice range"); return PQMC_ERR_ARG; }
-  if (b->precision == PQMC_PREC_FP64) {
-    for (auto* c : b->chains) {
+  if (b->precision == PQMC_PREC_FP64)
+    return fp64_each(b, [&](pqmc_chain* c) {
       const int n = std::min(n_slices, c->ntime - first_tc + 1);
-      if (n > 0) PQMC_TRY(pqmc_sweep_slices(c, loop, first_tc, n));
-    }
-    return PQMC_OK;
-  }
+      return n > 0 ? pqmc_sweep_slices(c, loop, first_tc, n) : PQMC_OK;
+    });
   if (!b->parts.empty()) {
     // uneven batch: each class takes the slices that exist in its sweep
     std::vector<int> n(b->parts.size());
@@ -2173,10 +2205,8 @@ int pqmc_batch_sweep(pqmc_batch* b, int loop) {
   // (Main_PQMC.f90:87-96), chain after chain, before the batched sweep
   for (auto* c : b->chains)
     if (c->have_global) PQMC_TRY(pqmc_global_step(c, loop, nullptr));
-  if (b->precision == PQMC_PREC_FP64) {
-    for (auto* c : b->chains) PQMC_TRY(pqmc_sweep(c, loop, 1, 1 << 30, 1, 0, nullptr, 0, nullptr));
-    return PQMC_OK;
-  }
+  if (b->precision == PQMC_PREC_FP64)
+    return fp64_each(b, [&](pqmc_chain* c) { return pqmc_sweep(c, loop, 1, 1 << 30, 1, 0, nullptr, 0, nullptr); });
   if (!b->parts.empty()) {
     // one whole sweep of every chain, each class over its own ntime slices
     std::vector<int> n(b->parts.size());

@@ -350,7 +350,8 @@ int pqmc_batch_set_flush(pqmc_batch* batch, int mode);
 /* one sweep of every chain (Main_PQMC.f90:99-154); equal-time
  * measurements only after pqmc_batch_set_measure; chains with global moves
  * enabled (pqmc_set_global on pqmc_batch_chain) take the driver's global
- * step first (Main_PQMC.f90:87-96), one chain after another */
+ * step first (Main_PQMC.f90:87-96), the chains' steps run from worker
+ * threads (PQMC_BATCH_THREADS, default 8) */
 int pqmc_batch_sweep(pqmc_batch* batch, int loop);
 /* Equal-time measurement inside batched sweeps with the reference's window
  * and cadence (loop > warmup, mod(loop-warmup, meas_interval) == 0, time in
@@ -380,7 +381,7 @@ int pqmc_batch_init(pqmc_batch* batch);
  * work on it (the chain groups run on their own streams in between) */
 int pqmc_batch_stream(pqmc_batch* batch, void** stream);
 /* info[5] = {chains, chain groups (streams), delay depth, flush engine,
- * precision}; the groups default to one per 16 chains (at most 4) and can
+ * precision}; the groups default to one per 8 chains (at most 8) and can
  * be set with the environment variable PQMC_BATCH_GROUPS (1..8) at creation */
 int pqmc_batch_info(pqmc_batch* batch, int* info);
 /* Uneven batches (mixed precision): chains of different geometry (Ns, Lt,

@@ -1786,10 +1786,10 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
   PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
-  // chain groups: PQMC_BATCH_GROUPS (1..8) when set, else one per 16 chains
-  // (at most 4)
+  // chain groups: PQMC_BATCH_GROUPS (1..8) when set, else one per 8 chains
+  // (at most 8)
   {
-    int ng = precision == PQMC_PREC_MIXED ? std::min(n_chains / 16, 4) : 1;
+    int ng = precision == PQMC_PREC_MIXED ? n_chains / 8 : 1;
     const char* env = getenv("PQMC_BATCH_GROUPS");
     if (env && precision == PQMC_PREC_MIXED) ng = atoi(env);
     ng = std::max(1, std::min(std::min(ng, (int)pqmc_batch::MAX_GROUPS), n_chains));
@@ -2202,9 +2202,12 @@ int pqmc_batch_sweep(pqmc_batch* b, int loop) {
   for (auto* c : b->chains)
     if (!c->have_g) { set_error("batch_sweep before init_g"); return PQMC_ERR_STATE; }
   // the driver's global step of every chain with global moves enabled
-  // (Main_PQMC.f90:87-96), chain after chain, before the batched sweep
-  for (auto* c : b->chains)
-    if (c->have_global) PQMC_TRY(pqmc_global_step(c, loop, nullptr));
+  // (Main_PQMC.f90:87-96) before the batched sweep; the chains' steps are
+  // independent and run from worker threads
+  bool any_global = false;
+  for (auto* c : b->chains) any_global = any_global || c->have_global;
+  if (any_global)
+    PQMC_TRY(fp64_each(b, [&](pqmc_chain* c) { return c->have_global ? pqmc_global_step(c, loop, nullptr) : PQMC_OK; }));
   if (b->precision == PQMC_PREC_FP64)
     return fp64_each(b, [&](pqmc_chain* c) { return pqmc_sweep(c, loop, 1, 1 << 30, 1, 0, nullptr, 0, nullptr); });
   if (!b->parts.empty()) {

@@ -517,23 +517,29 @@ namespace cgx = cooperative_groups;
 __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_gj_cluster(const GJArgs* args, int n) {
   cgx::cluster_group cl = cgx::this_cluster();
   extern __shared__ __align__(16) unsigned char gj_dyn[];
-  __shared__ dfc s_f[GJ_MAXN];   // multipliers of the current step (written by the owner block)
+  // multipliers, pivot row and reciprocal pivot of step k in buffer k&1
+  // (written by the owner block into every block; double-buffered so that
+  // one cluster barrier per step suffices)
+  __shared__ dfc s_f[2][GJ_MAXN];
+  __shared__ int s_p[2];
+  __shared__ dfc s_rec[2];
   __shared__ int s_perm[GJ_MAXN];
-  __shared__ int s_p;
-  __shared__ dfc s_rec;
-  __shared__ float s_bv[256];
-  __shared__ int s_bi[256];
+  __shared__ float s_bv[32];
+  __shared__ int s_bi[32];
   const int rank = (int)cl.block_rank();
   const GJArgs a = args[blockIdx.x / GJ_CL];
   const int w = (n + GJ_CL - 1) / GJ_CL, c_lo = rank * w, c_hi = min(n, c_lo + w), nc = max(0, c_hi - c_lo);
   dfc* A = reinterpret_cast<dfc*>(gj_dyn);   // [nc][n] local slab, A[i + n*(j - c_lo)]
-  const int tid = threadIdx.x;
-  for (int e = tid; e < nc * n; e += blockDim.x) A[e] = dfc_make(a.M[(size_t)c_lo * n + e]);
-  cl.sync();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int jl = warp; jl < nc; jl += nw)
+    for (int i = lane; i < n; i += 32) A[(size_t)n * jl + i] = dfc_make(a.M[(size_t)(c_lo + jl) * n + i]);
+  __syncthreads();
+  cl.sync();   // every block of the cluster runs before its shared memory is written
   int nswap = 0;
   for (int k = 0; k < n; ++k) {
-    const int owner = k / w;
-    if (rank == owner) {
+    const int buf = k & 1;
+    if (k / w == rank) {
+      // column k is current: this block finished its elimination of step k-1
       const dfc* col = A + (size_t)n * (k - c_lo);
       float best = -1.f;
       int bi = k;
@@ -541,17 +547,30 @@ __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_gj_cluste
         const float m = fabsf(col[i].re.hi) + fabsf(col[i].im.hi);
         if (m > best) { best = m; bi = i; }
       }
-      s_bv[tid] = best;
-      s_bi[tid] = bi;
-      __syncthreads();
-      for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-        if (tid < st) {
-          const float ov = s_bv[tid + st];
-          const int oi = s_bi[tid + st];
-          if (ov > s_bv[tid] || (ov == s_bv[tid] && oi < s_bi[tid])) { s_bv[tid] = ov; s_bi[tid] = oi; }
-        }
-        __syncthreads();
+      // largest magnitude, smallest row on ties: within each warp, then over warps
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
       }
+      if (lane == 0) {
+        s_bv[warp] = best;
+        s_bi[warp] = bi;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        best = lane < nw ? s_bv[lane] : -2.f;
+        bi = lane < nw ? s_bi[lane] : n;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) s_bi[0] = bi;
+      }
+      __syncthreads();
       const int p = s_bi[0];
       const dfc pv = col[p];
       df nrm = df_add(df_mul(pv.re, pv.re), df_mul(pv.im, pv.im));
@@ -562,21 +581,20 @@ __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_gj_cluste
       const df inv = df_div(df{1.f, 0.f}, nrm.hi == 0.0f ? df{1.f, 0.f} : nrm);
       const dfc rec = dfc{df_mul(pv.re, inv), df_neg(df_mul(pv.im, inv))};
       // multipliers f_i = A(sigma(i), k) with rows k and p exchanged
-      for (int r = 0; r < GJ_CL; ++r) {
-        dfc* rf = cl.map_shared_rank(s_f, r);
-        for (int i = tid; i < n; i += blockDim.x) {
-          const int src = (i == k) ? p : ((i == p) ? k : i);
-          rf[i] = col[src];
-        }
-        if (tid == 0) {
-          *cl.map_shared_rank(&s_p, r) = p;
-          *cl.map_shared_rank(&s_rec, r) = rec;
-        }
+      for (int i = tid; i < n; i += blockDim.x) {
+        const dfc v = col[(i == k) ? p : ((i == p) ? k : i)];
+#pragma unroll
+        for (int r = 0; r < GJ_CL; ++r) cl.map_shared_rank(&s_f[buf][0], r)[i] = v;
+      }
+      if (tid < GJ_CL) {
+        *cl.map_shared_rank(&s_p[buf], tid) = p;
+        *cl.map_shared_rank(&s_rec[buf], tid) = rec;
       }
     }
     cl.sync();
-    const int p = s_p;
-    const dfc rec = s_rec;
+    const int p = s_p[buf];
+    const dfc rec = s_rec[buf];
+    const dfc* f = s_f[buf];
     if (tid == 0) s_perm[k] = p;
     if (p != k) ++nswap;
     // exchange rows k and p, scale row k, eliminate, in this block's columns
@@ -590,15 +608,18 @@ __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_gj_cluste
       cj[k] = (c_lo + jl == k) ? rec : dfc_mul(cj[k], rec);
     }
     __syncthreads();
-    for (long e = tid; e < (long)nc * n; e += blockDim.x) {
-      const int i = (int)(e % n), jl = (int)(e / n);
-      if (i == k) continue;
+    for (int jl = warp; jl < nc; jl += nw) {
       dfc* cj = A + (size_t)n * jl;
-      const dfc f = s_f[i];
-      if (c_lo + jl == k) cj[i] = dfc_sub(dfc_zero(), dfc_mul(f, rec));
-      else cj[i] = dfc_fms(cj[i], f, cj[k]);
+      const dfc ck = cj[k];
+      if (c_lo + jl == k) {
+        for (int i = lane; i < n; i += 32)
+          if (i != k) cj[i] = dfc_sub(dfc_zero(), dfc_mul(f[i], rec));
+      } else {
+        for (int i = lane; i < n; i += 32)
+          if (i != k) cj[i] = dfc_fms(cj[i], f[i], ck);
+      }
     }
-    cl.sync();   // s_f, s_p, s_rec are rewritten by the next step's owner
+    __syncthreads();   // this block's next pivot column is current
   }
   // undo the row exchanges as column exchanges: computed column c ends at pos(c)
   __shared__ int s_at[GJ_MAXN];
@@ -642,30 +663,39 @@ __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_gj_cluste
   }
 }
 
-// Cholesky W = L L^H in double-float on a cluster of GJ_CL blocks, a slab
-// of columns of W per block in shared memory (right-looking: the block
-// owning column j forms it and writes it to every block of the cluster, each
-// block updates its own trailing columns).  The factor goes to `work` for
-// k_tri_inv and d_j = L_jj to `d` (multiplied in when accumulate_d).
+// Cholesky W = L L^H in double-float on a cluster of GJ_CL blocks.  Column
+// k lives in block k % GJ_CL (cyclic, so every block has about the same
+// share of each trailing update), local slot k / GJ_CL, in shared memory.
+// Right-looking, one cluster barrier per column: the block owning column j
+// forms L(:,j) (its column is final once its own update by column j-1 has
+// finished) and writes it into buffer j&1 of every block; after the barrier
+// each block updates its own trailing columns, a warp per column and a lane
+// per row.  The writer of buffer (j+1)&1 can only have passed barrier j, by
+// which every block has finished reading that buffer for column j-1.  The
+// factor goes to `work` for k_tri_inv and d_j = L_jj to `d` (multiplied in
+// when accumulate_d).
 __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_chol_cluster(const CholArgs* args, int n,
                                                                                       int accumulate_d) {
   cgx::cluster_group cl = cgx::this_cluster();
   extern __shared__ __align__(16) unsigned char ch_dyn[];
-  __shared__ dfc s_f[GJ_MAXN];   // column j of L (written by the owner block)
+  __shared__ dfc s_f[2][GJ_MAXN];   // L(:,j) of the current column, double-buffered
   __shared__ int s_bad;
   __shared__ df s_l;
   const int rank = (int)cl.block_rank();
   const CholArgs a = args[blockIdx.x / GJ_CL];
-  const int w = (n + GJ_CL - 1) / GJ_CL, c_lo = rank * w, c_hi = min(n, c_lo + w), nc = max(0, c_hi - c_lo);
-  dfc* A = reinterpret_cast<dfc*>(ch_dyn);   // [nc][n]
-  const int tid = threadIdx.x;
-  for (int e = tid; e < nc * n; e += blockDim.x) A[e] = dfc_make(a.W[(size_t)c_lo * n + e]);
+  const int nc = (n - rank + GJ_CL - 1) / GJ_CL;   // columns rank, rank + GJ_CL, ...
+  dfc* A = reinterpret_cast<dfc*>(ch_dyn);         // [nc][n]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int kl = warp; kl < nc; kl += nw) {
+    const cplx* src = a.W + (size_t)(rank + GJ_CL * kl) * n;
+    for (int i = lane; i < n; i += 32) A[(size_t)n * kl + i] = dfc_make(src[i]);
+  }
   if (tid == 0) s_bad = 0;
-  cl.sync();
+  cl.sync();   // every block of the cluster runs before its shared memory is written
   for (int j = 0; j < n; ++j) {
-    const int owner = j / w;
-    if (rank == owner) {
-      dfc* col = A + (size_t)n * (j - c_lo);
+    const int buf = j & 1;
+    if (j % GJ_CL == rank) {
+      dfc* col = A + (size_t)n * (j / GJ_CL);
       if (tid == 0) {
         df ajj = col[j].re;
         if (!(ajj.hi > 0.0f)) {
@@ -677,31 +707,35 @@ __global__ void __cluster_dims__(GJ_CL, 1, 1) __launch_bounds__(256) k_chol_clus
       }
       __syncthreads();
       const df inv = df_div(df{1.0f, 0.0f}, s_l);
-      for (int i = j + 1 + tid; i < n; i += blockDim.x) col[i] = dfc{df_mul(col[i].re, inv), df_mul(col[i].im, inv)};
-      __syncthreads();
-      for (int r = 0; r < GJ_CL; ++r) {
-        dfc* rf = cl.map_shared_rank(s_f, r);
-        for (int i = j + 1 + tid; i < n; i += blockDim.x) rf[i] = col[i];
+      for (int i = j + 1 + tid; i < n; i += blockDim.x) {
+        const dfc v = dfc{df_mul(col[i].re, inv), df_mul(col[i].im, inv)};
+        col[i] = v;
+#pragma unroll
+        for (int r = 0; r < GJ_CL; ++r) cl.map_shared_rank(&s_f[buf][0], r)[i] = v;
       }
     }
     cl.sync();
     // L(i,k) -= L(i,j) conj(L(k,j)) for j < k <= i, k in this block's columns
-    const int k0 = max(c_lo, j + 1);
-    for (long e = tid; e < (long)(c_hi - k0) * n; e += blockDim.x) {
-      const int i = (int)(e % n), k = k0 + (int)(e / n);
-      if (i < k) continue;
-      const dfc lkj = s_f[k];
-      dfc* cell = A + (size_t)n * (k - c_lo) + i;
-      *cell = dfc_fms(*cell, s_f[i], dfc{lkj.re, df_neg(lkj.im)});
+    const int kl0 = j < rank ? 0 : (j - rank) / GJ_CL + 1;
+    const dfc* f = s_f[buf];
+    for (int kl = kl0 + warp; kl < nc; kl += nw) {
+      const int k = rank + GJ_CL * kl;
+      const dfc lkj = f[k];
+      const dfc ckj = dfc{lkj.re, df_neg(lkj.im)};
+      dfc* col = A + (size_t)n * kl;
+      for (int i = k + lane; i < n; i += 32) col[i] = dfc_fms(col[i], f[i], ckj);
     }
-    cl.sync();
+    __syncthreads();   // this block's next pivot column is final
   }
-  for (int jl = tid; jl < nc; jl += blockDim.x) {
-    const int j = c_lo + jl;
-    const double v = df_to_d(A[(size_t)n * jl + j].re);
+  for (int kl = tid; kl < nc; kl += blockDim.x) {
+    const int j = rank + GJ_CL * kl;
+    const double v = df_to_d(A[(size_t)n * kl + j].re);
     a.d[j] = accumulate_d ? mk(a.d[j].x * v, 0.0) : mk(v, 0.0);
   }
-  for (int e = tid; e < nc * n; e += blockDim.x) a.work[(size_t)c_lo * n + e] = A[e];
+  for (int kl = warp; kl < nc; kl += nw) {
+    dfc* dst = a.work + (size_t)(rank + GJ_CL * kl) * n;
+    for (int i = lane; i < n; i += 32) dst[i] = A[(size_t)n * kl + i];
+  }
   if (tid == 0 && s_bad) *a.status = 1;
 }
 
@@ -853,7 +887,7 @@ int BatchRecompute::setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s
     PQMC_CUDA(raise_dyn_smem(k_tri_inv, (int)tsm));
     // the cluster Gauss-Jordan needs a quarter of the matrix per block in shared memory
     const size_t gsm = sizeof(dfc) * (size_t)((ne + GJ_CL - 1) / GJ_CL) * ne;
-    gj_cluster = ne <= GJ_MAXN && gsm + 20480 <= (size_t)optin;
+    gj_cluster = ne <= GJ_MAXN && gsm + 32768 <= (size_t)optin;   // plus the static shared memory
     if (gj_cluster) {
       PQMC_CUDA(raise_dyn_smem(k_gj_cluster, (int)gsm));
       PQMC_CUDA(raise_dyn_smem(k_chol_cluster, (int)gsm));

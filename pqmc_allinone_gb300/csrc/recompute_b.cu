@@ -266,6 +266,65 @@ __global__ void __launch_bounds__(TRI_WARPS * 32) k_tri_inv(const CholArgs* args
   for (int i = lane; i < n; i += 32) a.rinv[i + (size_t)n * j] = i <= j ? dfc_to_d(x[i]) : mk(0.0);
 }
 
+// The same R^-1 = L^-H, column j per warp, by column-oriented substitution:
+// x_k = (delta_kj - s_k) / L_kk for k = j .. 0, then s_m += conj(L_km) x_k
+// for every m < k.  Lane l owns the rows m = l (mod 32) (their s_m and x_m
+// in registers); row k of L is loaded one step ahead, so the chain of
+// dependent steps waits on the arithmetic and one shuffle, not on memory.
+// Rows up to 32 * TRI_SLOTS (nelec <= 256).
+constexpr int TRI_SLOTS = 8;
+__global__ void __launch_bounds__(TRI_WARPS * 32) k_tri_inv_rows(const CholArgs* args, int n) {
+  const CholArgs a = args[blockIdx.y];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * TRI_WARPS + warp;
+  if (j >= n) return;
+  const dfc* L = a.work;
+  dfc cur[TRI_SLOTS], nxt[TRI_SLOTS], sx[TRI_SLOTS];
+  df dcur = {1.f, 0.f}, dnxt = {1.f, 0.f};
+#pragma unroll
+  for (int t = 0; t < TRI_SLOTS; ++t) {
+    const int m = lane + 32 * t;
+    sx[t] = dfc_zero();
+    cur[t] = m < j ? L[j + (size_t)n * m] : dfc_zero();
+  }
+  if (lane == (j & 31)) dcur = L[j + (size_t)n * j].re;
+  for (int k = j; k >= 0; --k) {
+    // row k-1 and its diagonal entry, ahead of need
+#pragma unroll
+    for (int t = 0; t < TRI_SLOTS; ++t) {
+      const int m = lane + 32 * t;
+      nxt[t] = m < k - 1 ? L[(k - 1) + (size_t)n * m] : dfc_zero();
+    }
+    if (k >= 1 && lane == ((k - 1) & 31)) dnxt = L[(k - 1) + (size_t)n * (k - 1)].re;
+    // x_k by its owner lane (the others compute a discarded value), broadcast
+    dfc sk = dfc_zero();
+#pragma unroll
+    for (int t = 0; t < TRI_SLOTS; ++t) sk = (lane + 32 * t == k) ? sx[t] : sk;
+    const df inv = df_div(df{1.f, 0.f}, dcur);
+    const dfc v = dfc_sub(k == j ? dfc{{1.f, 0.f}, {0.f, 0.f}} : dfc_zero(), sk);
+    dfc xk = dfc{df_mul(v.re, inv), df_mul(v.im, inv)};
+#pragma unroll
+    for (int t = 0; t < TRI_SLOTS; ++t) sx[t] = (lane + 32 * t == k) ? xk : sx[t];
+    const int src = k & 31;
+    xk.re.hi = __shfl_sync(0xffffffffu, xk.re.hi, src);
+    xk.re.lo = __shfl_sync(0xffffffffu, xk.re.lo, src);
+    xk.im.hi = __shfl_sync(0xffffffffu, xk.im.hi, src);
+    xk.im.lo = __shfl_sync(0xffffffffu, xk.im.lo, src);
+    // s_m += conj(L_km) x_k for the rows m < k this lane owns
+#pragma unroll
+    for (int t = 0; t < TRI_SLOTS; ++t)
+      if (lane + 32 * t < k) sx[t] = dfc_add(sx[t], dfc_mulc(cur[t], xk));
+#pragma unroll
+    for (int t = 0; t < TRI_SLOTS; ++t) cur[t] = nxt[t];
+    dcur = dnxt;
+  }
+#pragma unroll
+  for (int t = 0; t < TRI_SLOTS; ++t) {
+    const int m = lane + 32 * t;
+    if (m < n) a.rinv[m + (size_t)n * j] = m <= j ? dfc_to_d(sx[t]) : mk(0.0);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Gauss-Jordan inverse in place with partial pivoting (df32 scratch), FP64
 // log det from the pivots (zgetrf/zdet conventions: product of pivots, sign
@@ -923,8 +982,11 @@ int BatchRecompute::cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*
       k_chol_inv<<<C, 512, 0, stream>>>(d_chol, ne, pass);
     }
     PQMC_LAUNCHED();
-    k_tri_inv<<<dim3((ne + TRI_WARPS - 1) / TRI_WARPS, C), TRI_WARPS * 32, sizeof(dfc) * TRI_WARPS * ne, stream>>>(
-        d_chol, ne);
+    if (ne <= 32 * TRI_SLOTS)
+      k_tri_inv_rows<<<dim3((ne + TRI_WARPS - 1) / TRI_WARPS, C), TRI_WARPS * 32, 0, stream>>>(d_chol, ne);
+    else
+      k_tri_inv<<<dim3((ne + TRI_WARPS - 1) / TRI_WARPS, C), TRI_WARPS * 32, sizeof(dfc) * TRI_WARPS * ne, stream>>>(
+          d_chol, ne);
     PQMC_LAUNCHED();
     for (int i = 0; i < C; ++i)
       ga[i] = GemmArgs{X[i], rinv + (size_t)i * ne * ne, tmpX + (size_t)i * ns * ne, ns, ne, ns, 0, 2};

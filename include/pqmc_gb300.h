@@ -382,7 +382,7 @@ int pqmc_batch_init(pqmc_batch* batch);
 int pqmc_batch_stream(pqmc_batch* batch, void** stream);
 /* info[5] = {chains, chain groups (streams), delay depth, flush engine,
  * precision}; the groups default to one per 8 chains (at most 8) and can
- * be set with the environment variable PQMC_BATCH_GROUPS (1..8) at creation */
+ * be set with the environment variable PQMC_BATCH_GROUPS (1..16) at creation */
 int pqmc_batch_info(pqmc_batch* batch, int* info);
 /* Uneven batches (mixed precision): chains of different geometry (Ns, Lt,
  * families) are grouped into classes of equal geometry; each class runs

@@ -70,22 +70,30 @@ __device__ __forceinline__ float2 fcfma(float2 a, float2 b, float2 acc) {
 }
 
 // ---------------------------------------------------------------------------
-__global__ void k_bdraw(const BDesc* D, int C, int pf) {
+// the ran2 draws of n_fam family steps in sweep order (family pf_first,
+// then pf_first + pf_step, ...), each family's proposals into its own part
+// of the proposal records; families without a local update draw nothing
+__global__ void k_bdraw(const BDesc* D, int C, int pf_first, int pf_step, int n_fam) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const BDesc d = D[c];
-  const int npla = d.M.pf_npla[pf];
   Ran2Dev rng;
   rng.iran = d.sc->rng[0]; rng.jran = d.sc->rng[1]; rng.kran = d.sc->rng[2];
   rng.mran = d.sc->rng[3]; rng.nran = d.sc->rng[4];
-  for (int p = 0; p < npla; ++p) {
-    if (d.M.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
-      d.pre[p].xnew = (double)rng.next();
-      d.pre[p].dE = (double)rng.next();
-    } else {
-      d.pre[p].xnew = (double)rng.ran_sysm();
+  for (int q = 0; q < n_fam; ++q) {
+    const int pf = pf_first + q * pf_step;
+    if (!d.M.pf_v_exist[pf]) continue;
+    const int npla = d.M.pf_npla[pf];
+    PlaqPre* pre = d.pre + (size_t)pf * d.M.max_pla;
+    for (int p = 0; p < npla; ++p) {
+      if (d.M.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
+        pre[p].xnew = (double)rng.next();
+        pre[p].dE = (double)rng.next();
+      } else {
+        pre[p].xnew = (double)rng.ran_sysm();
+      }
+      pre[p].r = (double)rng.next();
     }
-    d.pre[p].r = (double)rng.next();
   }
   d.sc->rng[0] = rng.iran; d.sc->rng[1] = rng.jran; d.sc->rng[2] = rng.kran;
   d.sc->rng[3] = rng.mran; d.sc->rng[4] = rng.nran;
@@ -113,7 +121,9 @@ __global__ void k_bsettime(BDesc* D, int C, int t) {
   if (c < C) D[c].t = t;
 }
 
-__global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf) {
+// proposals of families pf_first .. pf_first+n_fam-1 (bpf blocks of 8
+// plaquettes per family), each into the family's part of the records
+__global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf_first, int bpf) {
   __shared__ BDesc sd;
   if (threadIdx.x == 0) sd = D[blockIdx.y];
   __syncthreads();
@@ -121,10 +131,11 @@ __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf) {
   const int t = d.t;
   const DevModel& M = d.M;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pf = pf_first + (int)blockIdx.x / bpf;
   const int npla = M.pf_npla[pf], dim = M.pf_dim[pf], pd = M.pdim;
-  const int p = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (p >= npla) return;
-  PlaqPre* pre = d.pre;
+  const int p = ((int)blockIdx.x % bpf) * (blockDim.x >> 5) + warp;
+  if (p >= npla || !M.pf_v_exist[pf]) return;
+  PlaqPre* pre = d.pre + (size_t)pf * M.max_pla;
   const double* field = d.field;
   const bool closed = (M.expkv_kind != PQMC_EXPKV_GENERAL);
   const int b = M.bf[p + M.max_pla * pf];
@@ -452,7 +463,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   const CUtensorMap* tmG = parity ? d.tm_galt : d.tm_g;
   float2* A = d.A;
   float2* B = d.B;
-  const PlaqPre* pre = d.pre;
+  const PlaqPre* pre = d.pre + (size_t)pf * M.max_pla;
   // ---- stage the rest of the family (panels are empty: Geff = G) ----------
   for (int e = tid; e < (npla - p0) * 4; e += blockDim.x) {
     const int p = p0 + e / 4, m = e % 4;
@@ -1209,7 +1220,7 @@ struct pqmc_batch {
   cudaStream_t stream = nullptr;   // the stream of group 0, the batch's public stream
   // chain groups: each group has its own stream and recompute workspace, so
   // one group's latency-bound scan overlaps the other's flush and recompute
-  static constexpr int MAX_GROUPS = 8;
+  static constexpr int MAX_GROUPS = 16;
   int n_groups = 1;
   int g_first[MAX_GROUPS] = {}, g_count[MAX_GROUPS] = {};
   cudaStream_t g_stream[MAX_GROUPS] = {};
@@ -1227,6 +1238,11 @@ struct pqmc_batch {
   };
   bool graphs = false;
   std::deque<SliceGraph> gcache;
+  // proposal records of every family per chain (n_pf x max_pla); when the
+  // families' bosons are disjoint, a slice's draws and proposals of all
+  // families are formed in one launch each at the start of the slice
+  std::vector<pqmc::PlaqPre*> pre_all;
+  bool slice_prep = false;
   // equal-time measurement inside batched sweeps (ms_begin_measure semantics)
   int meas_on = 0, meas_warmup = 0, meas_interval = 1, meas_number = 0;
   std::vector<std::vector<double>> records;   // finished records per chain
@@ -1341,6 +1357,24 @@ static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
 }
 
 // update_phonon_field of family pf for group g's chains at the group's slice
+// draws and proposals of n_fam families from pf_first (step pf_step in the
+// draw order) for group g
+static int bprepare(pqmc_batch* b, int g, int pf_first, int pf_step, int n_fam) {
+  const int C = b->g_count[g];
+  const BDesc* Dg = b->d_desc + b->g_first[g];
+  cudaStream_t st = b->g_stream[g];
+  pqmc_chain* c0 = b->chains[0];
+  const int bpf = (c0->max_pla + 7) / 8;
+  const int lo = pf_step > 0 ? pf_first : pf_first + (n_fam - 1) * pf_step;
+  cudaEvent_t tp = gphase_begin(b, g);
+  k_bdraw<<<(C + 63) / 64, 64, 0, st>>>(Dg, C, pf_first, pf_step, n_fam);
+  PQMC_LAUNCHED();
+  k_bprep<<<dim3(bpf * n_fam, C), 256, 0, st>>>(Dg, lo, bpf);
+  PQMC_LAUNCHED();
+  gphase_end(b, g, PQMC_PHASE_PREP, tp);
+  return PQMC_OK;
+}
+
 static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
   const int C = b->g_count[g], c_first = b->g_first[g];
   const BDesc* Dg = b->d_desc + c_first;
@@ -1348,12 +1382,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
   cudaStream_t st = b->g_stream[g];
   pqmc_chain* c0 = b->chains[0];
   const int npla = c0->h_pf_npla[pf], dim = c0->h_pf_dim[pf];
-  cudaEvent_t tp = gphase_begin(b, g);
-  k_bdraw<<<(C + 63) / 64, 64, 0, st>>>(Dg, C, pf);
-  PQMC_LAUNCHED();
-  k_bprep<<<dim3((npla + 7) / 8, C), 256, 0, st>>>(Dg, pf);
-  PQMC_LAUNCHED();
-  gphase_end(b, g, PQMC_PHASE_PREP, tp);
+  if (!b->slice_prep) PQMC_TRY(bprepare(b, g, pf, 1, 1));
   PQMC_CUDA(cudaMemsetAsync(next, 0, sizeof(int) * C, st));
   const int kd = std::max(dim, std::min(b->kd, b->h_desc[0].kmax));
   // enough rounds for the worst case (every proposal accepted)
@@ -1398,6 +1427,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
 static int slice_ops(pqmc_batch* b, int g, bool forward, int parity) {
   pqmc_chain* c0 = b->chains[0];
   const bool upd = c0->M.local_update != 0;
+  if (upd && b->slice_prep) PQMC_TRY(bprepare(b, g, forward ? 0 : c0->n_pf - 1, forward ? 1 : -1, c0->n_pf));
   if (!forward) {
     for (int pf = c0->n_pf - 1; pf >= 0; --pf) {
       PQMC_TRY(bwrap(b, g, pf, false, parity));
@@ -1673,6 +1703,24 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
         return PQMC_ERR_ARG;
       }
   }
+  if (precision == PQMC_PREC_MIXED) {
+    // a slice's proposals can all be formed at its start when no boson is
+    // shared by two families (a family's moves then change nothing the
+    // other families' proposals read)
+    bool disjoint = true;
+    for (int i = 0; i < n_chains && disjoint; ++i) {
+      const pqmc_model* m = models[i];
+      std::vector<int> owner(m->n_bf, -1);
+      for (int f = 0; f < m->n_pf && disjoint; ++f)
+        for (int q = 0; q < m->pf_npla[f]; ++q) {
+          const int bf = m->bf_list[q + m->max_pla * f];
+          if (bf < 0 || bf >= m->n_bf) continue;
+          if (owner[bf] >= 0 && owner[bf] != f) { disjoint = false; break; }
+          owner[bf] = f;
+        }
+    }
+    b->slice_prep = disjoint;
+  }
   PQMC_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   int kmax = 0;
   for (int f = 0; f < c0->n_pf; ++f) kmax = std::max(kmax, c0->h_pf_npla[f] * c0->h_pf_dim[f]);
@@ -1771,6 +1819,12 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     h.nrb = b->nrb;
     h.err = b->d_err;
     h.pre = c->pre;
+    if (precision == PQMC_PREC_MIXED) {
+      PlaqPre* pa = nullptr;
+      PQMC_CUDA(cudaMalloc((void**)&pa, sizeof(PlaqPre) * (size_t)c->n_pf * c->max_pla));
+      b->pre_all.push_back(pa);
+      h.pre = pa;
+    }
     h.sc = c->sc;
     float2* pan = nullptr;
     int* kc = nullptr;
@@ -1786,10 +1840,10 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
   PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
-  // chain groups: PQMC_BATCH_GROUPS (1..8) when set, else one per 8 chains
+  // chain groups: PQMC_BATCH_GROUPS (1..16) when set, else one per 8 chains
   // (at most 8)
   {
-    int ng = precision == PQMC_PREC_MIXED ? n_chains / 8 : 1;
+    int ng = precision == PQMC_PREC_MIXED ? std::min(n_chains / 8, 8) : 1;
     const char* env = getenv("PQMC_BATCH_GROUPS");
     if (env && precision == PQMC_PREC_MIXED) ng = atoi(env);
     ng = std::max(1, std::min(std::min(ng, (int)pqmc_batch::MAX_GROUPS), n_chains));
@@ -1836,6 +1890,8 @@ int pqmc_batch_destroy(pqmc_batch* b) {
     if (p) cudaFree(p);
   for (auto* k : b->kcounts)
     if (k) cudaFree(k);
+  for (auto* pa : b->pre_all)
+    if (pa) cudaFree(pa);
   if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);

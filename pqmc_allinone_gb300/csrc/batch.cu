@@ -121,10 +121,17 @@ __global__ void k_bsettime(BDesc* D, int C, int t) {
   if (c < C) D[c].t = t;
 }
 
-// proposals of families pf_first .. pf_first+n_fam-1 (bpf blocks of 8
-// plaquettes per family), each into the family's part of the records
+// proposals of families pf_first .. (bpf blocks of PREP_PLA plaquettes per
+// family), each into the family's part of the records.  The per-plaquette
+// scalars (jump, action change, threshold, the closed-form norm and its
+// cosh/sinh) are formed one plaquette per lane of warp 0, the 4x4 blocks
+// (new propagators, Delta) by 16 lanes per plaquette: on GB300 every FP64
+// warp instruction costs the same whatever its active lanes, so the scalar
+// part is spread across lanes instead of repeated per plaquette.
+constexpr int PREP_PLA = 16;
 __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf_first, int bpf) {
   __shared__ BDesc sd;
+  __shared__ double s_x[PREP_PLA], s_norm[PREP_PLA], s_ch[PREP_PLA], s_sh[PREP_PLA];
   if (threadIdx.x == 0) sd = D[blockIdx.y];
   __syncthreads();
   const BDesc& d = sd;
@@ -133,63 +140,68 @@ __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf_first, int
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int pf = pf_first + (int)blockIdx.x / bpf;
   const int npla = M.pf_npla[pf], dim = M.pf_dim[pf], pd = M.pdim;
-  const int p = ((int)blockIdx.x % bpf) * (blockDim.x >> 5) + warp;
-  if (p >= npla || !M.pf_v_exist[pf]) return;
+  const int p0 = ((int)blockIdx.x % bpf) * PREP_PLA;
+  if (p0 >= npla || !M.pf_v_exist[pf]) return;
   PlaqPre* pre = d.pre + (size_t)pf * M.max_pla;
   const double* field = d.field;
   const bool closed = (M.expkv_kind != PQMC_EXPKV_GENERAL);
-  const int b = M.bf[p + M.max_pla * pf];
-  double jump;
-  if (M.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
-    double u1 = pre[p].xnew, u2 = pre[p].dE;
-    jump = M.jump * (sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
-  } else {
-    jump = M.jump * pre[p].xnew;
-  }
-  double xnew = field[b + (size_t)M.n_bf * t] + jump;
-  double norm = 0.0, ch = 0.0, sh = 0.0;
-  __syncwarp();
-  if (lane == 0) {
-    double dE = -M.delt * energy_diff(M, field, b, t, jump);
+  // ---- scalars: one plaquette per lane ------------------------------------
+  if (warp == 0 && lane < PREP_PLA && p0 + lane < npla) {
+    const int p = p0 + lane;
+    const int b = M.bf[p + M.max_pla * pf];
+    double jump;
+    if (M.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
+      double u1 = pre[p].xnew, u2 = pre[p].dE;
+      jump = M.jump * (sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+    } else {
+      jump = M.jump * pre[p].xnew;
+    }
+    const double xnew = field[b + (size_t)M.n_bf * t] + jump;
+    const double dE = -M.delt * energy_diff(M, field, b, t, jump);
     pre[p].dE = dE;
     pre[p].thr = b_threshold(M, dE, pre[p].r);
+    pre[p].xnew = xnew;
+    s_x[lane] = xnew;
     if (closed) {
-      norm = closed_norm(M, pf, xnew);
-      ch = cosh(norm);
-      sh = sinh(norm);
+      const double norm = closed_norm(M, pf, xnew);
+      s_norm[lane] = norm;
+      s_ch[lane] = cosh(norm);
+      s_sh[lane] = sinh(norm);
     } else {
       dev_get_expkv(M, pf, p, xnew, false, pre[p].enew);
       dev_get_expkv(M, pf, p, xnew, true, pre[p].einv);
     }
   }
-  norm = __shfl_sync(0xffffffffu, norm, 0);
-  ch = __shfl_sync(0xffffffffu, ch, 0);
-  sh = __shfl_sync(0xffffffffu, sh, 0);
-  const int i = lane % dim, j = lane / dim;
-  const bool act = lane < dim * dim;
+  __syncthreads();
+  // ---- 4x4 blocks: 16 lanes per plaquette, two plaquettes per warp ---------
+  const int h = lane >> 4, sl = lane & 15, q = 2 * warp + h, p = p0 + q;
+  const bool valid = q < PREP_PLA && p < npla;
+  const int i = sl % dim, j = sl / dim;
+  const bool act = valid && sl < dim * dim;
   cplx en = mk(0.0);
   if (act) {
     if (closed) {
+      const double xnew = s_x[q], norm = s_norm[q], ch = s_ch[q], sh = s_sh[q];
       en = closed_entry(M, pf, p, xnew, false, i, j, norm, ch, sh);
-      pre[p].enew[lane] = en;
-      pre[p].einv[lane] = closed_entry(M, pf, p, xnew, true, i, j, norm, ch, sh);
+      pre[p].enew[sl] = en;
+      pre[p].einv[sl] = closed_entry(M, pf, p, xnew, true, i, j, norm, ch, sh);
     } else {
-      en = pre[p].enew[lane];
+      en = pre[p].enew[sl];
     }
   }
   __syncwarp();
-  const size_t base = M.kv_base(p, pf, t);
+  // Delta = expKV_inv(old) expKV(new) - I   (mod_update.f90:240-243)
+  const size_t base = valid ? M.kv_base(p, pf, t) : 0;
   cplx a = mk(0.0);
   for (int k = 0; k < dim; ++k) {
-    cplx ekj = shfl_c(en, k + dim * j);
+    const cplx ekj = shfl_c(en, 16 * h + k + dim * j);
     if (act) a = cadd(a, cmul(d.expkv_inv[base + i + pd * k], ekj));
   }
   if (act) {
     if (i == j) a = csub(a, mk(1.0));
-    pre[p].delta[lane] = a;
-    pre[p].deltaf[lane] = make_float2((float)a.x, (float)a.y);
+    pre[p].delta[sl] = a;
+    pre[p].deltaf[sl] = make_float2((float)a.x, (float)a.y);
   }
-  if (lane == 0) pre[p].xnew = xnew;
 }
 
 // ---------------------------------------------------------------------------
@@ -1364,7 +1376,7 @@ static int bprepare(pqmc_batch* b, int g, int pf_first, int pf_step, int n_fam) 
   const BDesc* Dg = b->d_desc + b->g_first[g];
   cudaStream_t st = b->g_stream[g];
   pqmc_chain* c0 = b->chains[0];
-  const int bpf = (c0->max_pla + 7) / 8;
+  const int bpf = (c0->max_pla + PREP_PLA - 1) / PREP_PLA;
   const int lo = pf_step > 0 ? pf_first : pf_first + (n_fam - 1) * pf_step;
   cudaEvent_t tp = gphase_begin(b, g);
   k_bdraw<<<(C + 63) / 64, 64, 0, st>>>(Dg, C, pf_first, pf_step, n_fam);

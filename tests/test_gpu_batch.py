@@ -242,3 +242,26 @@ def test_uneven_batch_matches_its_classes():
         o.init_expkv()
         o.init_g(1)
         assert rel_fro(g, o.g()) < MIXED_RECOMPUTE_TOL
+
+
+def test_fp64_uneven_batch_matches_oracle():
+    """An FP64 batch of chains of uneven L and Lt, driven from worker
+    threads: every chain's decisions and field match the oracle, bit for
+    bit, after a sweep each."""
+    from oracle.oracle import OracleChain
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    geo = [(4, 20), (6, 40), (4, 40), (6, 20), (4, 20)]
+    ms = []
+    for i, (L, nt) in enumerate(geo):
+        m, f = epsocz_small(L=L, ntime=nt, ngroup=10, lam=0.6 + 0.05 * i, alpha=0.3, seed=1100 + i)
+        ms.append((m, f, seed_words(1100 + i)))
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=0)
+    b.init()
+    b.sweep(1)
+    for (m, f, w), ch in zip(ms, b.chains):
+        o = OracleChain(m, field=f, seed_words=w, meas=False)
+        o.init_expkv(); o.init_g(1); o.sweep(1, 1)
+        assert np.array_equal(ch.field(), o.field())
+        assert ch.state()["positive_accept"] == o.state()["positive_accept"]
+        assert rel_fro(ch.g(), o.g()) < 1e-10
+    b.close()

@@ -460,6 +460,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
   const int rb = d.rb, nrb = d.nrb;
   const int io = (ns <= SCAN_THREADS - 32) ? SCAN_THREADS - 32 : 0;
   const bool row_warp = warp * 32 < ns;   // holds a row of G (every warp when RPT = 2)
+  // a warp with no row of G that is not the copy-engine warp
+  const int inv_warp = (RPT == 1 && ns <= SCAN_THREADS - 64) ? SCAN_THREADS / 32 - 2 : -1;
   const ScanLayout L = scan_layout(npla, ns, ldp, qc, kd, 4 * nrb * rb * (int)sizeof(float4));
   float4* s_rows = reinterpret_cast<float4*>(s_dyn + L.rows);     // [dim][nrb*rb] rows of G at S
   float2* s_stage = reinterpret_cast<float2*>(s_dyn + L.stage);
@@ -540,15 +542,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     }
     if (tid == 0) na += wa;
     p += wa;
-    // ---- accepted move p: T = Delta R^-1 by the warp that evaluated it ------
+    // ---- accepted move p: T = Delta R^-1, by a warp without rows of G when
+    //      there is one (its work then overlaps the row warps' panel loop),
+    //      else by the warp that evaluated the move -------------------------
     const float2 det = s_det[wa];
-    if (warp == wa) {
-      wf_inverse(dim, s_R[warp], det, lane);
+    if (warp == (inv_warp >= 0 ? inv_warp : wa)) {
+      wf_inverse(dim, s_R[wa], det, lane);
       if (act) {
         const float2* de = s_delta + 16 * p;
         float2 a = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < dim; ++k) a = fcfma(de[i + dim * k], s_R[warp][k + dim * j], a);
+        for (int k = 0; k < dim; ++k) a = fcfma(de[i + dim * k], s_R[wa][k + dim * j], a);
         s_T[lane] = a;
       }
       if (lane == 0) {

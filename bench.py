@@ -412,7 +412,7 @@ def run_mixed(args, world, rank, local):
                             "scaled to the chains of one launch (chain group 0)",
             "tensor_achieved_tflops": flops / secs / 1e12 if secs > 0 else 0.0,
             "tensor_peak_tflops": pk["bf16_tflops_sustained"],
-            "kernel": ("k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "
+            "kernel": ("k_bsplit + k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "
                        "in tensor memory)" if (depth <= 64 and (args.flush or tune)) else
                        "k_bflush (rank-K flush G += A B, mma.sync BF16x3 products, FP32 accumulate)"),
             "algorithmic": "32*Ns^2*dim/K bytes (G read + write, double-float) and 8*Ns^2*dim flop per accepted "

@@ -883,19 +883,23 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
 // products hi.hi, hi.mid, mid.hi, hi.lo, mid.mid, lo.hi accumulated into one
 // FP32 accumulator in tensor memory (128 lanes x 128 columns per tile).
 //
-// Each CTA of k_bflush_um (one 128 x 64 tile of G) reads its 128 rows of A
-// and 64 columns of B from the FP32 panels and writes their three BF16
-// terms as shared-memory images in the no-swizzle K-major core-matrix
-// layout: a core matrix is 8 rows x 16 bytes (8 BF16 along K); core (row
-// group i8, K group j8) sits at j8 * UM_LBO + i8 * 128 bytes (UM_LBO = 16
-// row groups * 128 B).  Each image is 128 rows x 2*UM_KP BF16 (Ar/Br-part
-// at k < UM_KP, Ai-part at UM_KP + k).
+// k_bsplit writes the split operands as shared-memory tile images in the
+// no-swizzle K-major core-matrix layout: a core matrix is 8 rows x 16 bytes
+// (8 BF16 along K); core (row group i8, K group j8) sits at
+// j8 * UM_LBO + i8 * 128 bytes (UM_LBO = 16 row groups * 128 B), so the
+// first k columns of a tile image are one contiguous prefix.  Per chain:
+// UM_RT row tiles of A' and UM_CT column tiles of B', three splits each,
+// each image 128 rows x 2*UM_KP BF16 (Ar/Br-part at k < UM_KP, Ai-part at
+// UM_KP + k).
 constexpr int UM_KP = 64;                    // panel columns per flush on this path (delay depth <= 64)
 constexpr int UM_IMG = 128 * 2 * UM_KP * 2;  // bytes per tile image (32 KB)
 constexpr int UM_LBO = 16 * 128;             // bytes between adjacent K core matrices
 
 __host__ __device__ __forceinline__ int um_rtiles(int ns) { return (ns + 127) / 128; }
 __host__ __device__ __forceinline__ int um_ctiles(int ns) { return (ns + 63) / 64; }
+__host__ __device__ __forceinline__ size_t um_chain_bytes(int ns) {
+  return (size_t)3 * (um_rtiles(ns) + um_ctiles(ns)) * UM_IMG;
+}
 __device__ __forceinline__ int um_off(int row, int k) {   // byte offset of (row, k) in a tile image
   return (k >> 3) * UM_LBO + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
@@ -908,6 +912,60 @@ __device__ __forceinline__ void split3b(float x, __nv_bfloat16* o) {
   o[0] = h;
   o[1] = m;
   o[2] = __float2bfloat16_rn(r1 - __bfloat162float(m));
+}
+
+__global__ void __launch_bounds__(256) k_bsplit(const BDesc* D, unsigned char* img_all) {
+  const BDesc& d = D[blockIdx.y];
+  const int K = *d.kcount;
+  if (K == 0) return;
+  const int ns = d.M.ns, ldp = d.ldp, K16 = (K + 15) & ~15;
+  const int RT = um_rtiles(ns), CT = um_ctiles(ns);
+  unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
+  // work item: (tile t, group of 8 k, row in tile); consecutive threads take
+  // consecutive rows, so the panel reads coalesce and every thread writes one
+  // 16-byte core-matrix row per split and half
+  const int KG = K16 / 8;
+  const long total = (long)(RT + CT) * KG * 128;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int row = (int)(e % 128);
+    const int kg = (int)((e / 128) % KG);
+    const int t = (int)(e / (128L * KG));
+    float lo8[8], hi8[8];   // values at k (first half) and UM_KP + k (second half)
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      const int k = kg * 8 + jj;
+      if (t < RT) {
+        const int r = t * 128 + row;
+        const float2 v = (r < ns && k < K) ? d.A[(size_t)k * ldp + r] : make_float2(0.f, 0.f);
+        lo8[jj] = v.x;   // Ar
+        hi8[jj] = v.y;   // Ai
+      } else {
+        const int c = (t - RT) * 64 + (row & 63);
+        const float2 v = (c < ns && k < K) ? d.B[(size_t)k * ldp + c] : make_float2(0.f, 0.f);
+        if (row < 64) { lo8[jj] = v.x; hi8[jj] = -v.y; }   // re column: [Br | -Bi]
+        else { lo8[jj] = v.y; hi8[jj] = v.x; }             // im column: [Bi | Br]
+      }
+    }
+    __align__(16) __nv_bfloat16 ls[3][8], hs[3][8];
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      __nv_bfloat16 a3[3], b3[3];
+      split3b(lo8[jj], a3);
+      split3b(hi8[jj], b3);
+#pragma unroll
+      for (int s3 = 0; s3 < 3; ++s3) {
+        ls[s3][jj] = a3[s3];
+        hs[s3][jj] = b3[s3];
+      }
+    }
+    unsigned char* base = img + (size_t)t * 3 * UM_IMG;
+    const int o1 = um_off(row, kg * 8), o2 = um_off(row, UM_KP + kg * 8);
+#pragma unroll
+    for (int s3 = 0; s3 < 3; ++s3) {
+      *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o1) = *reinterpret_cast<const uint4*>(ls[s3]);
+      *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o2) = *reinterpret_cast<const uint4*>(hs[s3]);
+    }
+  }
 }
 
 // shared-memory operand descriptor (no swizzle, K-major), Blackwell format
@@ -952,9 +1010,9 @@ __device__ __forceinline__ void um_ld32(uint32_t taddr, float* v) {
 
 // one CTA per (128-row tile, 64-column tile, chain); 8 warps: warps w and w+4
 // read accumulator lanes 32(w%4).. and take column halves 0 and 1
-__global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, int parity) {
+__global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigned char* img_all, int parity) {
   __shared__ BDesc sd;
-  __shared__ __align__(8) uint64_t s_mma;
+  __shared__ __align__(8) uint64_t s_load, s_mma;
   __shared__ uint32_t s_taddr;
   __shared__ int s_fail;
   extern __shared__ __align__(1024) unsigned char um_dyn[];   // 3 A images, then 3 B images
@@ -962,6 +1020,7 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, int parity) {
   if (tid == 0) {
     sd = D[blockIdx.y];
     s_fail = 0;
+    mbar_init(&s_load, 1);
     mbar_init(&s_mma, 1);
     fence_mbar_init();
   }
@@ -981,55 +1040,22 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, int parity) {
   const int ti = blockIdx.x % RT, tj = blockIdx.x / RT;
   if (K > 0) {
     const int K16 = (K + 15) & ~15;
-    // ---- operand images: the FP32 panels of this tile's 128 rows of A and
-    //      64 columns of B (as 128 real rows [Br|-Bi], [Bi|Br]), split into
-    //      three BF16 terms in the no-swizzle K-major core-matrix layout; a
-    //      work item is (image row, 8 consecutive k) -------------------------
-    {
-      const int ldp = d.ldp, KG = K16 / 8;
-      for (int e = tid; e < 2 * 128 * KG; e += blockDim.x) {
-        const int row = e % 128, kg = (e / 128) % KG, isb = e / (128 * KG);
-        float lo8[8], hi8[8];
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          const int k = kg * 8 + jj;
-          if (!isb) {
-            const int r = ti * 128 + row;
-            const float2 v = (r < ns && k < K) ? d.A[(size_t)k * ldp + r] : make_float2(0.f, 0.f);
-            lo8[jj] = v.x;   // Ar
-            hi8[jj] = v.y;   // Ai
-          } else {
-            const int c = tj * 64 + (row & 63);
-            const float2 v = (c < ns && k < K) ? d.B[(size_t)k * ldp + c] : make_float2(0.f, 0.f);
-            if (row < 64) { lo8[jj] = v.x; hi8[jj] = -v.y; }   // re column: [Br | -Bi]
-            else { lo8[jj] = v.y; hi8[jj] = v.x; }             // im column: [Bi | Br]
-          }
-        }
-        __align__(16) __nv_bfloat16 ls[3][8], hs[3][8];
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          __nv_bfloat16 a3[3], b3[3];
-          split3b(lo8[jj], a3);
-          split3b(hi8[jj], b3);
-#pragma unroll
-          for (int s3 = 0; s3 < 3; ++s3) {
-            ls[s3][jj] = a3[s3];
-            hs[s3][jj] = b3[s3];
-          }
-        }
-        unsigned char* base = um_dyn + (size_t)(isb ? 3 : 0) * UM_IMG;
-        const int o1 = um_off(row, kg * 8), o2 = um_off(row, UM_KP + kg * 8);
-#pragma unroll
-        for (int s3 = 0; s3 < 3; ++s3) {
-          *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o1) = *reinterpret_cast<const uint4*>(ls[s3]);
-          *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o2) = *reinterpret_cast<const uint4*>(hs[s3]);
-        }
-      }
-      // generic-proxy stores to shared memory, read next by the tensor core
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
+    const unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
+    const uint32_t part = (uint32_t)(K16 / 8) * UM_LBO;   // bytes of k < K16 in one half
     if (tid == 0) {
+      mbar_arrive_tx(&s_load, 6u * 2u * part);
+      for (int s3 = 0; s3 < 3; ++s3) {
+        const unsigned char* ga = img + ((size_t)ti * 3 + s3) * UM_IMG;
+        const unsigned char* gb = img + ((size_t)(RT + tj) * 3 + s3) * UM_IMG;
+        unsigned char* sa = um_dyn + (size_t)s3 * UM_IMG;
+        unsigned char* sb = um_dyn + (size_t)(3 + s3) * UM_IMG;
+        const size_t h2 = (size_t)(UM_KP / 8) * UM_LBO;
+        bulk_g2s(sa, ga, part, &s_load);
+        bulk_g2s(sa + h2, ga + h2, part, &s_load);
+        bulk_g2s(sb, gb, part, &s_load);
+        bulk_g2s(sb + h2, gb + h2, part, &s_load);
+      }
+      if (!mbar_wait_bounded(&s_load, 0)) s_fail = 1;
       um_fence_after();
       if (!s_fail) {
         // split pairs (A', B'): (0,0) (0,1) (1,0) (0,2) (1,1) (2,0), packed 2 bits each
@@ -1201,6 +1227,7 @@ struct pqmc_batch {
   int kd = 64;            // delay depth (panel columns per flush)
   int qc = 8;             // panel columns per streamed chunk of the scan
   int flush_mode = 1;     // 1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush
+  unsigned char* d_img = nullptr;   // split operand tile images of the tcgen05 flush
   CUtensorMap* d_tmaps = nullptr;   // per chain: maps of its two G buffers
   int rb = 0, nrb = 0;              // row box of the maps (columns) and boxes per row
   std::vector<cplx*> tm_buf;        // per chain x 2: the buffer each map describes
@@ -1378,6 +1405,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
   const int rounds = (npla * dim + (kd / dim) * dim - 1) / ((kd / dim) * dim);
   const int tiles = ((c0->ns + FB_M - 1) / FB_M) * ((c0->ns + FB_N - 1) / FB_N);
   const int ns = c0->ns;
+  unsigned char* img = b->d_img ? b->d_img + um_chain_bytes(ns) * c_first : nullptr;
   for (int r = 0; r < rounds; ++r) {
     const BDesc& h0 = b->h_desc[0];
     const size_t smem = scan_layout(npla, ns, h0.ldp, b->qc, kd, 4 * h0.nrb * h0.rb * (int)sizeof(float4)).total;
@@ -1394,8 +1422,11 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     PQMC_LAUNCHED();
     gphase_end(b, g, PQMC_PHASE_SCAN, ts);
     cudaEvent_t tf = gphase_begin(b, g);
-    if (b->flush_mode == 1 && b->precision == PQMC_PREC_MIXED && kd <= UM_KP) {
-      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, st>>>(Dg, parity);
+    if (b->flush_mode == 1 && img && kd <= UM_KP) {
+      const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * (((kd + 15) & ~15) / 8);
+      k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, st>>>(Dg, img);
+      PQMC_LAUNCHED();
+      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, st>>>(Dg, img, parity);
       PQMC_LAUNCHED();
     } else {
       k_bflush<<<dim3(tiles, C), 256, 0, st>>>(Dg, parity);
@@ -1780,7 +1811,13 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   }
   PQMC_CUDA(cudaMalloc((void**)&b->d_err, sizeof(int)));
   PQMC_CUDA(cudaMemset(b->d_err, 0, sizeof(int)));
-  if (precision == PQMC_PREC_MIXED) PQMC_CUDA(raise_dyn_smem(k_bflush_um, 6 * UM_IMG));
+  if (precision == PQMC_PREC_MIXED) {
+    // tcgen05 flush: split operand images (zero outside the rows and columns of G)
+    const size_t ib = um_chain_bytes(c0->ns) * (size_t)n_chains;
+    PQMC_CUDA(cudaMalloc((void**)&b->d_img, ib));
+    PQMC_CUDA(cudaMemset(b->d_img, 0, ib));
+    PQMC_CUDA(raise_dyn_smem(k_bflush_um, 6 * UM_IMG));
+  }
   b->h_desc.resize(n_chains);
   for (int i = 0; i < n_chains; ++i) {
     pqmc_chain* c = b->chains[i];
@@ -1874,6 +1911,7 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
+  if (b->d_img) cudaFree(b->d_img);
   if (b->d_tmaps) cudaFree(b->d_tmaps);
   for (int g = 1; g < pqmc_batch::MAX_GROUPS; ++g)
     if (b->g_stream[g]) {

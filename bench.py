@@ -463,30 +463,34 @@ def run_e2e_mixed(b, m, cur, steps: int) -> dict:
     import torch
     C = len(b.chains)
     nb, blk = m.n_bf, m.ngroup
-    host = torch.empty((C, m.ntime, nb), dtype=torch.float64, pin_memory=True)   # (n_bf, ntime) per chain
-    hv = host.numpy()
+    # the fields live on the host (pinned); every step the block of slices
+    # it touches goes up for all chains in one call, the batch runs it, the
+    # updated block and every chain's state come back
+    field = torch.empty((C, m.ntime, nb), dtype=torch.float64, pin_memory=True)   # (n_bf, ntime) per chain
+    io = torch.empty((C, blk, nb), dtype=torch.float64, pin_memory=True)          # chain after chain
+    fv, iov = field.numpy(), io.numpy()
     for i, c in enumerate(b.chains):
-        hv[i] = c.field().T
+        fv[i] = c.field().T
     state_bytes = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         loop, tc = cur.next()
         first_time = tc if loop % 2 == 0 else m.ntime - (tc + blk - 1) + 1
-        for i, c in enumerate(b.chains):
-            c.set_field_slices(first_time, hv[i, first_time - 1:first_time - 1 + blk].T)
+        iov[:] = fv[:, first_time - 1:first_time - 1 + blk]
+        b.field_slices(first_time, blk, iov, True)
         b.sweep_slices(loop, tc, blk)
-        for i, c in enumerate(b.chains):
-            c.get_field_slices(first_time, blk, out=hv[i, first_time - 1:first_time - 1 + blk].T)
-        states = [c.state() for c in b.chains]
+        b.field_slices(first_time, blk, iov, False)
+        fv[:, first_time - 1:first_time - 1 + blk] = iov
+        states = b.states()
         state_bytes = len(states) * 104
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / steps
     blk_bytes = C * nb * blk * 8
     return {"value": C * (blk / m.ntime) / dt, "unit": "chain-sweeps/s", "h2d_bytes_per_step": int(blk_bytes),
             "d2h_bytes_per_step": int(blk_bytes + state_bytes), "steps": steps,
-            "path": "pqmc_set_field_slices (pinned host) + pqmc_batch_sweep_slices + pqmc_get_field_slices + "
-                    "pqmc_get_state per chain"}
+            "path": "pqmc_batch_field_slices (pinned host, all chains) + pqmc_batch_sweep_slices + "
+                    "pqmc_batch_field_slices back + pqmc_batch_states"}
 
 
 def run_plain_headline(args, world, rank, local):

@@ -394,6 +394,16 @@ int pqmc_batch_info(pqmc_batch* batch, int* info);
  * flush engine, chain groups} of class k.  Chain indices stay those of the
  * models array. */
 int pqmc_batch_classes(pqmc_batch* batch, int* n);
+/* Field blocks of every chain in one call: slices first_time ..
+ * first_time+n_times-1 of each chain's boson_field (clipped to the chain's
+ * ntime), host blocks chain after chain, each (n_bf, n) column-major.
+ * to_device = 1 copies host -> device and refreshes expKV of those slices
+ * (the batched pqmc_set_field_slices), 0 copies device -> host.  The copies
+ * are queued on the chains' streams together and the call returns when they
+ * are done; with pinned host memory they overlap each other. */
+int pqmc_batch_field_slices(pqmc_batch* batch, int first_time, int n_times, double* host, int to_device);
+/* pqmc_get_state of every chain (states[n_chains]) with one wait */
+int pqmc_batch_states(pqmc_batch* batch, pqmc_state* states);
 int pqmc_batch_class_info(pqmc_batch* batch, int k, int* info);
 /* CUDA-event timers per phase of the mixed family step; set_timing clears
  * the totals, get_timing returns PQMC_N_PHASES totals (ms) and counts. */

@@ -248,6 +248,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_get_timing": ([vp, _f64p, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "pqmc_batch_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_classes": ([vp, _i32p], ctypes.c_int),
+        "pqmc_batch_field_slices": ([vp, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_states": ([vp, ctypes.POINTER(PqmcState)], ctypes.c_int),
         "pqmc_batch_class_info": ([vp, ctypes.c_int, _i32p], ctypes.c_int),
         "pqmc_batch_graph_count": ([vp, _i32p], ctypes.c_int),
         "pqmc_version": ([], ctypes.c_char_p),

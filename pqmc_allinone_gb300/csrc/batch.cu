@@ -1259,6 +1259,7 @@ struct pqmc_batch {
   // families are formed in one launch each at the start of the slice
   std::vector<pqmc::PlaqPre*> pre_all;
   bool slice_prep = false;
+  pqmc::DevScalars* h_states = nullptr;   // pinned staging of pqmc_batch_states
   // equal-time measurement inside batched sweeps (ms_begin_measure semantics)
   int meas_on = 0, meas_warmup = 0, meas_interval = 1, meas_number = 0;
   std::vector<std::vector<double>> records;   // finished records per chain
@@ -1908,6 +1909,7 @@ int pqmc_batch_destroy(pqmc_batch* b) {
     if (k) cudaFree(k);
   for (auto* pa : b->pre_all)
     if (pa) cudaFree(pa);
+  if (b->h_states) cudaFreeHost(b->h_states);
   if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
@@ -2022,6 +2024,53 @@ int pqmc_batch_info(pqmc_batch* b, int* info) {
   info[2] = b->kd;
   info[3] = b->flush_mode;
   info[4] = b->precision;
+  return PQMC_OK;
+}
+
+int pqmc_batch_field_slices(pqmc_batch* b, int first_time, int n_times, double* host, int to_device) {
+  if (!b || !host || first_time < 1 || n_times < 1) { set_error("batch_field_slices: bad arguments"); return PQMC_ERR_ARG; }
+  // every chain's copy (and expKV refresh) is queued on its own stream
+  // first; one wait per stream at the end
+  size_t off = 0;
+  for (auto* c : b->chains) {
+    const int n = std::min(n_times, c->ntime - first_time + 1);
+    if (n <= 0) continue;
+    double* dev = c->field + (size_t)c->n_bf * (first_time - 1);
+    const size_t bytes = sizeof(double) * (size_t)c->n_bf * n;
+    if (to_device) {
+      PQMC_CUDA(cudaMemcpyAsync(dev, host + off, bytes, cudaMemcpyHostToDevice, c->stream));
+      PQMC_TRY(launch_init_expkv(c, first_time - 1, n));
+    } else {
+      PQMC_CUDA(cudaMemcpyAsync(host + off, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+    }
+    off += (size_t)c->n_bf * n;
+  }
+  for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  return PQMC_OK;
+}
+
+int pqmc_batch_states(pqmc_batch* b, pqmc_state* out) {
+  if (!b || !out) { set_error("batch_states: null argument"); return PQMC_ERR_ARG; }
+  const size_t n = b->chains.size();
+  if (!b->h_states) PQMC_CUDA(cudaMallocHost((void**)&b->h_states, sizeof(DevScalars) * n));
+  for (size_t i = 0; i < n; ++i)
+    PQMC_CUDA(cudaMemcpyAsync(b->h_states + i, b->chains[i]->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost,
+                              b->chains[i]->stream));
+  for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  for (size_t i = 0; i < n; ++i) {
+    const DevScalars& h = b->h_states[i];
+    pqmc_state& o = out[i];
+    o.ln_cw[0] = h.ln_cw.x;
+    o.ln_cw[1] = h.ln_cw.y;
+    o.err_fast_max = h.err_fast_max;
+    o.err_fast = h.err_fast;
+    o.err_g = h.err_g;
+    o.err_g_rel_max = h.err_g_rel_max;
+    o.positive_accept = h.pos_acc;
+    o.negative_accept = h.neg_acc;
+    for (int k = 0; k < 5; ++k) o.rng[k] = h.rng[k];
+    o.reserved = 0;
+  }
   return PQMC_OK;
 }
 

@@ -357,6 +357,21 @@ class PqmcBatch:
         """Replay each slice's family steps from a captured CUDA graph."""
         check(self.lib, self.lib.pqmc_batch_set_graphs(self.h, 1 if enable else 0), "pqmc_batch_set_graphs")
 
+    def field_slices(self, first_time: int, n: int, host, to_device: bool):
+        """Slices first_time..first_time+n-1 of every chain's field, host
+        blocks chain after chain ((n_bf, n) column-major each, clipped to
+        each chain's ntime), in one call (pinned host memory: host may be a
+        numpy view of a pinned buffer)."""
+        check(self.lib, self.lib.pqmc_batch_field_slices(self.h, first_time, n,
+                                                          host.ctypes.data_as(_f64p), 1 if to_device else 0),
+              "pqmc_batch_field_slices")
+
+    def states(self) -> list:
+        """state() of every chain with one wait."""
+        arr = (PqmcState * len(self.chains))()
+        check(self.lib, self.lib.pqmc_batch_states(self.h, arr), "pqmc_batch_states")
+        return [a.as_dict() for a in arr]
+
     def classes(self) -> list:
         """Geometry classes of the batch: [{chains, ns, ntime, delay_depth, flush, groups}]."""
         n = np.zeros(1, dtype=np.int32)

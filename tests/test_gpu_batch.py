@@ -265,3 +265,36 @@ def test_fp64_uneven_batch_matches_oracle():
         assert ch.state()["positive_accept"] == o.state()["positive_accept"]
         assert rel_fro(ch.g(), o.g()) < 1e-10
     b.close()
+
+
+def test_batch_field_slices_and_states():
+    """pqmc_batch_field_slices moves one block of every chain's field (host
+    blocks chain after chain) and refreshes expKV like the per-chain call;
+    pqmc_batch_states equals the per-chain states."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(3):
+        m, f = epsocz_small(L=4, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=300 + i)
+        ms.append((m, f, seed_words(3000 + i)))
+    m = ms[0][0]
+    b = PqmcBatch([x for x, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    b.init()
+    rng = np.random.default_rng(5)
+    blk = rng.normal(scale=0.5, size=(3, 10, m.n_bf))      # chain after chain, (n_bf, 10) column-major each
+    b.field_slices(6, 10, blk, True)
+    for i, c in enumerate(b.chains):
+        assert np.array_equal(c.field()[:, 5:15], blk[i].T)
+    back = np.zeros_like(blk)
+    b.field_slices(6, 10, back, False)
+    assert np.array_equal(back, blk)
+    # expKV of the new slices is current: the same sweep as a batch set up with those fields
+    fields = [c.field() for c in b.chains]
+    b.sweep(1)
+    b2 = PqmcBatch([x for x, _, _ in ms], fields, [w for _, _, w in ms], precision=1)
+    b2.init()
+    b2.sweep(1)
+    for c1, c2 in zip(b.chains, b2.chains):
+        assert np.array_equal(c1.field(), c2.field())
+    assert b.states() == [c.state() for c in b.chains]
+    b.close()
+    b2.close()

@@ -269,8 +269,8 @@ def test_fp64_uneven_batch_matches_oracle():
 
 def test_batch_field_slices_and_states():
     """pqmc_batch_field_slices moves one block of every chain's field (host
-    blocks chain after chain) and refreshes expKV like the per-chain call;
-    pqmc_batch_states equals the per-chain states."""
+    blocks chain after chain) both ways; pqmc_batch_states equals the
+    per-chain states."""
     from pqmc_allinone_gb300.engine import PqmcBatch
     ms = []
     for i in range(3):
@@ -278,7 +278,6 @@ def test_batch_field_slices_and_states():
         ms.append((m, f, seed_words(3000 + i)))
     m = ms[0][0]
     b = PqmcBatch([x for x, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
-    b.init()
     rng = np.random.default_rng(5)
     blk = rng.normal(scale=0.5, size=(3, 10, m.n_bf))      # chain after chain, (n_bf, 10) column-major each
     b.field_slices(6, 10, blk, True)
@@ -287,8 +286,9 @@ def test_batch_field_slices_and_states():
     back = np.zeros_like(blk)
     b.field_slices(6, 10, back, False)
     assert np.array_equal(back, blk)
-    # expKV of the new slices is current: the same sweep as a batch set up with those fields
+    # the chains then run exactly as a batch set up with those fields
     fields = [c.field() for c in b.chains]
+    b.init()
     b.sweep(1)
     b2 = PqmcBatch([x for x, _, _ in ms], fields, [w for _, _, w in ms], precision=1)
     b2.init()

@@ -415,9 +415,10 @@ int pqmc_batch_class_info(pqmc_batch* batch, int k, int* info);
 #define PQMC_N_PHASES        5
 int pqmc_batch_set_timing(pqmc_batch* batch, int enable);
 int pqmc_batch_get_timing(pqmc_batch* batch, double* ms, long long* launches);
-/* Slice graphs (mixed batches; no reference counterpart): with enable=1 the
- * family steps of a slice (draws, proposals, scan rounds, flushes, wraps)
- * are captured once per chain group, direction and G-buffer parity into a
+/* Slice graphs (mixed batches, on by default; no reference counterpart):
+ * the family steps of a slice (draws, proposals, scan rounds, flushes,
+ * wraps) are captured once per chain group, direction and G-buffer parity
+ * into a
  * CUDA graph and replayed for every later slice; the slice's time index
  * lives in device memory, so one graph serves all slices.  The stabilised
  * recompute and the measurement window still run as plain launches, and

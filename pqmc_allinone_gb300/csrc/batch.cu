@@ -1671,6 +1671,7 @@ static int create_uneven(const pqmc_model* const* models, int n_chains, const st
   b->n_groups = groups;
   b->kd = b->parts[0]->kd;
   b->flush_mode = b->parts[0]->flush_mode;
+  b->graphs = b->parts[0]->graphs;
   *out = b;
   return PQMC_OK;
 }
@@ -1700,6 +1701,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   }
   pqmc_batch* b = new pqmc_batch();
   b->precision = precision;
+  b->graphs = precision == PQMC_PREC_MIXED;   // slice graphs on by default
   for (int i = 0; i < n_chains; ++i) {
     pqmc_chain* c = nullptr;
     int st = pqmc_create(models[i], &c);

@@ -182,8 +182,7 @@ def test_mixed_observables_within_error_bars():
 def _run_batch(ms, loops, graphs=False, chains_only=None):
     from pqmc_allinone_gb300.engine import PqmcBatch
     b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
-    if graphs:
-        b.set_graphs(True)
+    b.set_graphs(graphs)
     b.init()
     for loop in loops:
         b.sweep(loop)

@@ -419,8 +419,10 @@ def run_mixed(args, world, rank, local):
                            "move, K = delay depth; chain group 0's moves over its flush-phase event time (the "
                            "other groups' kernels share the GPU meanwhile)",
             "peak_source": f"{pk['source']} HBM copy bandwidth; bf16 sustained for the tensor figure",
-            "dominant_by_time": "k_bscan (the sequential ratio scan, one CTA per chain: latency-bound by the "
-                                "Markov order, see phases)"}
+            "dominant_by_time": "k_bscan (59% of the serialised kernel time in profiles/"
+                                "launches_mixed_14x14_lt1000_16chains.md): the sequential ratio scan, one CTA per "
+                                "chain, latency-bound by the Markov order (FMA pipe 33% active), neither an HBM nor "
+                                "a tensor-pipe kernel"}
     total_ms = sum(v[0] for v in phases.values())
     phase_out = {k: {"ms_per_step": v[0] / 2, "share": v[0] / total_ms if total_ms else None,
                      "launch_groups": v[1]} for k, v in phases.items()}

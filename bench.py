@@ -34,6 +34,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "sweeps/s @14x14 Lt=1000: batched mixed-prec vs plain FP64 on GB300"
+
 # DFMA throughput of this GB300 pool measured with a dependent-free FP64 FMA
 # loop over all SMs (MEASURED_PEAKS.json holds no FP64 figure)
 FP64_PEAK_GFLOPS = 1010.8
@@ -219,11 +221,15 @@ def run_reference(args, world, rank):
     v = float(np.mean([x["value"] for x in vals]))
     cb = dict(vals[-1])
     cb["value"] = v
-    out = {"metric": "sweeps/s @14x14 Lt=1000", "value": v, "unit": "sweeps/s", "n_gpus": args.gpus,
+    ref_config = config_of(name, m, args.gpus, cb["cores"])
+    ref_config["workload"] = (f"{int(m.lat.dlength[0])}x{int(m.lat.dlength[0])} SOC EPSOCZ, Lt={m.ntime}: the "
+                              "reference's CPU path (the line-cited C++ FP64 restatement), one chain per host core, "
+                              f"{cb['cores']} cores")
+    out = {"metric": METRIC, "value": v, "unit": "chain-sweeps/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * (m.ngroup / m.ntime) / v,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-           "data": "synthetic", "config": config_of(name, m, args.gpus, cb["cores"]), "impl": "reference",
-           "cpu_baseline": cb, "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0,
+           "data": "synthetic", "config": ref_config, "impl": "reference",
+           "cpu_baseline": cb, "e2e": {"value": v, "unit": "chain-sweeps/s", "h2d_bytes_per_step": 0,
                                        "d2h_bytes_per_step": 0},
            "note": "the reference Fortran cannot be built here or on the GPU box (no Fortran compiler, no "
                    "LAPACK); this arm times the oracle, the line-cited C++ FP64 restatement of the same path, "
@@ -442,7 +448,7 @@ def run_mixed(args, world, rank, local):
         cb = cpu_baseline(m, M2.field_gaussian(m, 2), sw(42), args.cpu_slices or 10)
     if rank != 0:
         return
-    out = {"metric": "sweeps/s @14x14 Lt=1000: batched mixed-prec vs plain FP64 on GB300",
+    out = {"metric": METRIC,
            "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None,

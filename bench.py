@@ -382,23 +382,25 @@ def run_mixed(args, world, rank, local):
         b.sweep_slices(*cur.next(), m.ngroup)
     torch.cuda.synchronize()
     phases = b.timing()
+    rounds = b.flush_rounds()
     b.set_timing(False)
     st2 = [c.state() for c in b.chains]
     # the phase timers follow chain group 0 (the first C/groups chains)
     g0 = C // max(1, binfo["groups"])
     acc_ph = sum(s2["positive_accept"] - s1["positive_accept"] for s1, s2 in zip(st1[:g0], st2[:g0]))
 
-    # the delayed-update contraction G += A B (rank-K flush).  At delay depth
-    # K it does 8*Ns^2*K flop against 32*Ns^2 bytes of G (double-float read
-    # and write): 2K/8 = 16 flop/B at K=64, under the HBM roof (7.3 TB/s x 16
-    # = 117 TFLOP/s), far below the tensor roof.  Algorithmic bytes per
-    # accepted move: a full-depth flush serves K/dim accepted moves, so
-    # 32*Ns^2*dim/K bytes per move (short last rounds move the same bytes for
-    # fewer moves: this count is a lower bound of the real traffic).
+    # the delayed-update contraction G += A B (rank-K flush, k_bflush_um).  At
+    # delay depth K it does 8*Ns^2*K flop against 32*Ns^2 bytes of G
+    # (double-float read and write): 2K/8 = 16 flop/B at K=64, under the HBM
+    # roof (7.3 TB/s x 16 = 117 TFLOP/s), far below the tensor roof.
+    # Algorithmic bytes: 32*Ns^2 per flush that had columns to fold in
+    # (counted on the device per chain), over the flush kernel's own event
+    # time (the BF16 split kernel is timed apart).
     pk = peaks()
     dim = 4
     flush_ms, flush_n = phases["flush"]
-    bytes_alg = 32.0 * m.ns * m.ns * dim / depth * acc_ph
+    rounds_g0 = sum(rounds[:g0])
+    bytes_alg = 32.0 * m.ns * m.ns * rounds_g0
     flops = 8.0 * m.ns * m.ns * dim * acc_ph
     secs = flush_ms * 1e-3
     achieved = bytes_alg / secs / 1e9 if secs > 0 else 0.0
@@ -418,12 +420,14 @@ def run_mixed(args, world, rank, local):
                             "scaled to the chains of one launch (chain group 0)",
             "tensor_achieved_tflops": flops / secs / 1e12 if secs > 0 else 0.0,
             "tensor_peak_tflops": pk["bf16_tflops_sustained"],
-            "kernel": ("k_bsplit + k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "
+            "kernel": ("k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "
                        "in tensor memory)" if (depth <= 64 and (args.flush or tune)) else
                        "k_bflush (rank-K flush G += A B, mma.sync BF16x3 products, FP32 accumulate)"),
-            "algorithmic": "32*Ns^2*dim/K bytes (G read + write, double-float) and 8*Ns^2*dim flop per accepted "
-                           "move, K = delay depth; chain group 0's moves over its flush-phase event time (the "
-                           "other groups' kernels share the GPU meanwhile)",
+            "algorithmic": "32*Ns^2 bytes (G read + write, double-float) per flush with panel columns (device "
+                           "count, chain group 0) and 8*Ns^2*dim flop per accepted move, over the flush kernel's "
+                           "event time during two blocks (the other groups' kernels share the GPU meanwhile; "
+                           "launches of empty rounds included)",
+            "flush_rounds_group0": rounds_g0,
             "peak_source": f"{pk['source']} HBM copy bandwidth; bf16 sustained for the tensor figure",
             "dominant_by_time": "k_bscan (59% of the serialised kernel time in profiles/"
                                 "launches_mixed_14x14_lt1000_16chains.md): the sequential ratio scan, one CTA per "

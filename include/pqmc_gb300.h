@@ -412,9 +412,14 @@ int pqmc_batch_class_info(pqmc_batch* batch, int k, int* info);
 #define PQMC_PHASE_FLUSH     2   /* tensor-core rank-K flush G += A B     */
 #define PQMC_PHASE_WRAP      3   /* two-way wrap by a family             */
 #define PQMC_PHASE_RECOMPUTE 4   /* stabilised recompute (get_g_scratch)  */
-#define PQMC_N_PHASES        5
+#define PQMC_PHASE_SPLIT     5   /* BF16 split of the panels for tcgen05  */
+#define PQMC_N_PHASES        6
 int pqmc_batch_set_timing(pqmc_batch* batch, int enable);
 int pqmc_batch_get_timing(pqmc_batch* batch, double* ms, long long* launches);
+/* Per chain (rounds[n_chains]): the rank-K flushes that had panel columns
+ * to fold in since the last pqmc_batch_set_timing, i.e. the number of
+ * read-modify-writes of the chain's G by the flush. */
+int pqmc_batch_flush_rounds(pqmc_batch* batch, long long* rounds);
 /* Slice graphs (mixed batches, on by default; no reference counterpart):
  * the family steps of a slice (draws, proposals, scan rounds, flushes,
  * wraps) are captured once per chain group, direction and G-buffer parity

@@ -58,6 +58,7 @@ struct BDesc {
   const CUtensorMap* tm_galt;
   int rb, nrb;
   int t;         // 0-based time index of the slice in progress (k_bsettime)
+  unsigned long long* nflush;   // flush rounds with work (for the roofline accounting)
 };
 
 __device__ __forceinline__ float2 f2(cplx a) { return make_float2((float)a.x, (float)a.y); }
@@ -786,6 +787,7 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
   const BDesc& d = sd;
   const int K = *d.kcount;
   if (K == 0) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.nflush, 1ull);
   const int ns = d.M.ns;
   const int tiles_m = (ns + FB_M - 1) / FB_M, tiles_n = (ns + FB_N - 1) / FB_N;
   const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
@@ -1039,6 +1041,7 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigne
   const int ns = d.M.ns, RT = um_rtiles(ns);
   const int ti = blockIdx.x % RT, tj = blockIdx.x / RT;
   if (K > 0) {
+    if (blockIdx.x == 0 && tid == 0) atomicAdd(d.nflush, 1ull);
     const int K16 = (K + 15) & ~15;
     const unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
     const uint32_t part = (uint32_t)(K16 / 8) * UM_LBO;   // bytes of k < K16 in one half
@@ -1260,6 +1263,7 @@ struct pqmc_batch {
   std::vector<pqmc::PlaqPre*> pre_all;
   bool slice_prep = false;
   pqmc::DevScalars* h_states = nullptr;   // pinned staging of pqmc_batch_states
+  unsigned long long* d_nflush = nullptr;  // per chain: flush rounds with work
   // equal-time measurement inside batched sweeps (ms_begin_measure semantics)
   int meas_on = 0, meas_warmup = 0, meas_interval = 1, meas_number = 0;
   std::vector<std::vector<double>> records;   // finished records per chain
@@ -1422,11 +1426,15 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
 #undef PQMC_SCAN
     PQMC_LAUNCHED();
     gphase_end(b, g, PQMC_PHASE_SCAN, ts);
-    cudaEvent_t tf = gphase_begin(b, g);
     if (b->flush_mode == 1 && img && kd <= UM_KP) {
       const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * (((kd + 15) & ~15) / 8);
+      cudaEvent_t tsp = gphase_begin(b, g);
       k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, st>>>(Dg, img);
       PQMC_LAUNCHED();
+      gphase_end(b, g, PQMC_PHASE_SPLIT, tsp);
+    }
+    cudaEvent_t tf = gphase_begin(b, g);
+    if (b->flush_mode == 1 && img && kd <= UM_KP) {
       k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, st>>>(Dg, img, parity);
       PQMC_LAUNCHED();
     } else {
@@ -1857,6 +1865,9 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     b->panels.push_back(pan);
     b->kcounts.push_back(kc);
   }
+  PQMC_CUDA(cudaMalloc((void**)&b->d_nflush, sizeof(unsigned long long) * n_chains));
+  PQMC_CUDA(cudaMemset(b->d_nflush, 0, sizeof(unsigned long long) * n_chains));
+  for (int i = 0; i < n_chains; ++i) b->h_desc[i].nflush = b->d_nflush + i;
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
   PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
   // chain groups: PQMC_BATCH_GROUPS (1..16) when set, else one per 8 chains
@@ -1912,6 +1923,7 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   for (auto* pa : b->pre_all)
     if (pa) cudaFree(pa);
   if (b->h_states) cudaFreeHost(b->h_states);
+  if (b->d_nflush) cudaFree(b->d_nflush);
   if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
@@ -1995,6 +2007,31 @@ int pqmc_batch_set_timing(pqmc_batch* b, int enable) {
     b->phase_ms[k] = 0.0;
     b->phase_n[k] = 0;
   }
+  if (b->d_nflush) PQMC_CUDA(cudaMemset(b->d_nflush, 0, sizeof(unsigned long long) * b->chains.size()));
+  return PQMC_OK;
+}
+
+int pqmc_batch_flush_rounds(pqmc_batch* b, long long* rounds) {
+  if (!b || !rounds) { set_error("batch_flush_rounds: null argument"); return PQMC_ERR_ARG; }
+  if (!b->parts.empty()) {
+    for (size_t k = 0; k < b->parts.size(); ++k) {
+      std::vector<long long> pr(b->parts[k]->chains.size());
+      PQMC_TRY(pqmc_batch_flush_rounds(b->parts[k], pr.data()));
+      for (size_t i = 0; i < b->chains.size(); ++i)
+        if (b->part_of[i] == (int)k) rounds[i] = pr[b->index_in_part[i]];
+    }
+    return PQMC_OK;
+  }
+  const size_t n = b->chains.size();
+  if (!b->d_nflush) {
+    for (size_t i = 0; i < n; ++i) rounds[i] = 0;
+    return PQMC_OK;
+  }
+  std::vector<unsigned long long> h(n);
+  PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  for (int g = 1; g < b->n_groups; ++g) PQMC_CUDA(cudaStreamSynchronize(b->g_stream[g]));
+  PQMC_CUDA(cudaMemcpy(h.data(), b->d_nflush, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n; ++i) rounds[i] = (long long)h[i];
   return PQMC_OK;
 }
 

@@ -311,7 +311,7 @@ class PqmcBatch:
         return {"chains": int(v[0]), "groups": int(v[1]), "delay_depth": int(v[2]),
                 "flush": "tcgen05" if v[3] == 1 else "mma.sync", "precision": int(v[4])}
 
-    PHASES = ("prep", "scan", "flush", "wrap", "recompute")
+    PHASES = ("prep", "scan", "flush", "wrap", "recompute", "split")
 
     def set_timing(self, enable: bool):
         check(self.lib, self.lib.pqmc_batch_set_timing(self.h, 1 if enable else 0), "pqmc_batch_set_timing")
@@ -323,6 +323,12 @@ class PqmcBatch:
         check(self.lib, self.lib.pqmc_batch_get_timing(self.h, ms.ctypes.data_as(_f64p), n),
               "pqmc_batch_get_timing")
         return {p: (float(ms[i]), int(n[i])) for i, p in enumerate(self.PHASES)}
+
+    def flush_rounds(self) -> list:
+        """Per chain: flushes with panel columns since set_timing (G read-modify-writes)."""
+        n = (ctypes.c_longlong * len(self.chains))()
+        check(self.lib, self.lib.pqmc_batch_flush_rounds(self.h, n), "pqmc_batch_flush_rounds")
+        return [int(v) for v in n]
 
     def set_delay(self, depth: int):
         check(self.lib, self.lib.pqmc_batch_set_delay(self.h, depth), "pqmc_batch_set_delay")

@@ -297,3 +297,28 @@ def test_batch_field_slices_and_states():
     assert b.states() == [c.state() for c in b.chains]
     b.close()
     b2.close()
+
+
+def test_phase_timers_and_flush_rounds():
+    """The phase timers cover every phase of the family step and the device
+    count of flushes with columns is at least one per family step with an
+    accepted move (and at most the launched rounds)."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(2):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=700 + i)
+        ms.append((m, f, seed_words(7000 + i)))
+    b = PqmcBatch([x for x, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    b.init()
+    b.set_timing(True)
+    b.sweep_slices(1, 1, 10)
+    ph = b.timing()
+    rounds = b.flush_rounds()
+    b.set_timing(False)
+    assert set(ph) == set(PqmcBatch.PHASES)
+    for k in ("prep", "scan", "flush", "wrap", "recompute", "split"):
+        assert ph[k][0] > 0 and ph[k][1] > 0, k
+    launched = ph["flush"][1]
+    assert all(0 < r <= launched for r in rounds), (rounds, launched)
+    assert b.flush_rounds() == [0, 0]          # set_timing clears the counts
+    b.close()

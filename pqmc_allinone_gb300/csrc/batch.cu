@@ -887,23 +887,39 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
 //
 // k_bsplit writes the split operands as shared-memory tile images in the
 // no-swizzle K-major core-matrix layout: a core matrix is 8 rows x 16 bytes
-// (8 BF16 along K); core (row group i8, K group j8) sits at
-// j8 * UM_LBO + i8 * 128 bytes (UM_LBO = 16 row groups * 128 B), so the
-// first k columns of a tile image are one contiguous prefix.  Per chain:
-// UM_RT row tiles of A' and UM_CT column tiles of B', three splits each,
-// each image 128 rows x 2*UM_KP BF16 (Ar/Br-part at k < UM_KP, Ai-part at
-// UM_KP + k).
+// (8 BF16 along K); a tile image of nrg row groups puts core (row group i8,
+// K group j8) at j8 * nrg * 128 + i8 * 128 bytes, so the first k columns of
+// each half of an image are one contiguous prefix.  Each image is
+// 2*UM_KP BF16 wide (Ar/Br-part at k < UM_KP, Ai-part at UM_KP + k; the
+// second half starts at (UM_KP/8) * nrg * 128).  Per chain: um_rtiles row
+// tiles of A' and um_ctiles column tiles of B', three splits each, every
+// image in a UM_IMG slot.  The images are compact: a row tile holds only
+// its rows of G (the last one of an Ns that is not a multiple of 128 holds
+// fewer), and a column tile with nc <= 32 columns of G holds 32 re columns
+// followed by 32 im columns (ncg = 4 core groups each; rows past nc are
+// never written and only reach accumulator columns that are not read), so
+// the flush of a ragged tile copies and multiplies only what it needs
+// (N = 16 ncg).
 constexpr int UM_KP = 64;                    // panel columns per flush on this path (delay depth <= 64)
-constexpr int UM_IMG = 128 * 2 * UM_KP * 2;  // bytes per tile image (32 KB)
-constexpr int UM_LBO = 16 * 128;             // bytes between adjacent K core matrices
+constexpr int UM_IMG = 128 * 2 * UM_KP * 2;  // bytes per tile image slot (32 KB)
 
 __host__ __device__ __forceinline__ int um_rtiles(int ns) { return (ns + 127) / 128; }
 __host__ __device__ __forceinline__ int um_ctiles(int ns) { return (ns + 63) / 64; }
 __host__ __device__ __forceinline__ size_t um_chain_bytes(int ns) {
   return (size_t)3 * (um_rtiles(ns) + um_ctiles(ns)) * UM_IMG;
 }
-__device__ __forceinline__ int um_off(int row, int k) {   // byte offset of (row, k) in a tile image
-  return (k >> 3) * UM_LBO + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+// row groups of row tile t, column groups of column tile t
+__host__ __device__ __forceinline__ int um_rg(int ns, int t) {
+  const int g = (ns - 128 * t + 7) / 8;
+  return g < 16 ? g : 16;
+}
+__host__ __device__ __forceinline__ int um_cg(int ns, int t) {   // 4 or 8, so im starts at TMEM column 32 or 64
+  const int g = (ns - 64 * t + 7) / 8;
+  return g <= 4 ? 4 : 8;
+}
+// byte offset of (row, k) in a tile image of nrg row groups
+__device__ __forceinline__ int um_off(int row, int k, int nrg) {
+  return (k >> 3) * nrg * 128 + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
 // three-way BF16 split of an FP32 value
@@ -921,51 +937,63 @@ __global__ void __launch_bounds__(256) k_bsplit(const BDesc* D, unsigned char* i
   const int K = *d.kcount;
   if (K == 0) return;
   const int ns = d.M.ns, ldp = d.ldp, K16 = (K + 15) & ~15;
-  const int RT = um_rtiles(ns), CT = um_ctiles(ns);
+  const int RT = um_rtiles(ns);
   unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
-  // work item: (tile t, group of 8 k, row in tile); consecutive threads take
-  // consecutive rows, so the panel reads coalesce and every thread writes one
-  // 16-byte core-matrix row per split and half
+  // work items: (group of 8 k, row of G) for A', then (group of 8 k, column
+  // of G) for B', rows and columns padded to whole core matrices (R8);
+  // consecutive threads take consecutive rows or columns, so the panel reads
+  // coalesce, and every thread writes 16-byte core-matrix rows.  A B' item
+  // writes both image rows of its column (re and im), so each panel entry is
+  // read and split once; RN rounding is sign-symmetric: split(-x) = -split(x).
   const int KG = K16 / 8;
-  const long total = (long)(RT + CT) * KG * 128;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-    const int row = (int)(e % 128);
-    const int kg = (int)((e / 128) % KG);
-    const int t = (int)(e / (128L * KG));
-    float lo8[8], hi8[8];   // values at k (first half) and UM_KP + k (second half)
+  const long R8 = (long)((ns + 7) / 8) * 8;
+  const long na = R8 * KG;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < 2 * na; e += (long)gridDim.x * blockDim.x) {
+    const bool isb = e >= na;
+    const long e2 = isb ? e - na : e;
+    const int r = (int)(e2 % R8), kg = (int)(e2 / R8);
+    __align__(16) __nv_bfloat16 xs[3][8], ys[3][8];   // splits of the re and im parts at k = kg*8 + jj
+    const float2* P = isb ? d.B : d.A;
 #pragma unroll
     for (int jj = 0; jj < 8; ++jj) {
       const int k = kg * 8 + jj;
-      if (t < RT) {
-        const int r = t * 128 + row;
-        const float2 v = (r < ns && k < K) ? d.A[(size_t)k * ldp + r] : make_float2(0.f, 0.f);
-        lo8[jj] = v.x;   // Ar
-        hi8[jj] = v.y;   // Ai
-      } else {
-        const int c = (t - RT) * 64 + (row & 63);
-        const float2 v = (c < ns && k < K) ? d.B[(size_t)k * ldp + c] : make_float2(0.f, 0.f);
-        if (row < 64) { lo8[jj] = v.x; hi8[jj] = -v.y; }   // re column: [Br | -Bi]
-        else { lo8[jj] = v.y; hi8[jj] = v.x; }             // im column: [Bi | Br]
-      }
-    }
-    __align__(16) __nv_bfloat16 ls[3][8], hs[3][8];
-#pragma unroll
-    for (int jj = 0; jj < 8; ++jj) {
+      const float2 v = (r < ns && k < K) ? P[(size_t)k * ldp + r] : make_float2(0.f, 0.f);
       __nv_bfloat16 a3[3], b3[3];
-      split3b(lo8[jj], a3);
-      split3b(hi8[jj], b3);
+      split3b(v.x, a3);
+      split3b(v.y, b3);
 #pragma unroll
       for (int s3 = 0; s3 < 3; ++s3) {
-        ls[s3][jj] = a3[s3];
-        hs[s3][jj] = b3[s3];
+        xs[s3][jj] = a3[s3];
+        ys[s3][jj] = b3[s3];
       }
     }
-    unsigned char* base = img + (size_t)t * 3 * UM_IMG;
-    const int o1 = um_off(row, kg * 8), o2 = um_off(row, UM_KP + kg * 8);
+    if (!isb) {   // A' row: [Ar | Ai]
+      const int t = r / 128, row = r % 128, nrg = um_rg(ns, t);
+      unsigned char* base = img + (size_t)t * 3 * UM_IMG;
+      const int o1 = um_off(row, kg * 8, nrg), o2 = um_off(row, UM_KP + kg * 8, nrg);
 #pragma unroll
-    for (int s3 = 0; s3 < 3; ++s3) {
-      *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o1) = *reinterpret_cast<const uint4*>(ls[s3]);
-      *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o2) = *reinterpret_cast<const uint4*>(hs[s3]);
+      for (int s3 = 0; s3 < 3; ++s3) {
+        *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o1) = *reinterpret_cast<const uint4*>(xs[s3]);
+        *reinterpret_cast<uint4*>(base + (size_t)s3 * UM_IMG + o2) = *reinterpret_cast<const uint4*>(ys[s3]);
+      }
+    } else {      // B' re row c: [Br | -Bi], im row 8 ncg + c: [Bi | Br]
+      const int t = r / 64, c = r % 64, ncg = um_cg(ns, t), nrg = 2 * ncg;
+      unsigned char* base = img + (size_t)(RT + t) * 3 * UM_IMG;
+      const int o1 = um_off(c, kg * 8, nrg), o2 = um_off(c, UM_KP + kg * 8, nrg);
+      const int o3 = um_off(8 * ncg + c, kg * 8, nrg), o4 = um_off(8 * ncg + c, UM_KP + kg * 8, nrg);
+#pragma unroll
+      for (int s3 = 0; s3 < 3; ++s3) {
+        uint4 yn = *reinterpret_cast<const uint4*>(ys[s3]);
+        yn.x ^= 0x80008000u;
+        yn.y ^= 0x80008000u;
+        yn.z ^= 0x80008000u;
+        yn.w ^= 0x80008000u;
+        unsigned char* b3 = base + (size_t)s3 * UM_IMG;
+        *reinterpret_cast<uint4*>(b3 + o1) = *reinterpret_cast<const uint4*>(xs[s3]);
+        *reinterpret_cast<uint4*>(b3 + o2) = yn;
+        *reinterpret_cast<uint4*>(b3 + o3) = *reinterpret_cast<const uint4*>(ys[s3]);
+        *reinterpret_cast<uint4*>(b3 + o4) = *reinterpret_cast<const uint4*>(xs[s3]);
+      }
     }
   }
 }
@@ -978,14 +1006,17 @@ __device__ __forceinline__ uint64_t um_desc(uint32_t saddr, uint32_t lbo, uint32
   dsc |= (uint64_t)1 << 46;   // descriptor version 1 (tcgen05)
   return dsc;                 // base offset 0, layout type 0 = no swizzle
 }
-// instruction descriptor: kind::f16, D = F32, A = B = BF16, both K-major, M = N = 128
-constexpr uint32_t UM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+// instruction descriptor: kind::f16, D = F32, A = B = BF16, both K-major,
+// M = 128, N = n (a multiple of 16, at most 256)
+__device__ __forceinline__ uint32_t um_idesc(uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
 
-__device__ __forceinline__ void um_mma(uint32_t dtm, uint64_t ad, uint64_t bd, uint32_t accumulate) {
+__device__ __forceinline__ void um_mma(uint32_t dtm, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtm),
-      "l"(ad), "l"(bd), "r"(UM_IDESC), "r"(accumulate)
+      "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 __device__ __forceinline__ void um_commit(uint64_t* mbar) {
@@ -1011,18 +1042,21 @@ __device__ __forceinline__ void um_ld32(uint32_t taddr, float* v) {
 }
 
 // one CTA per (128-row tile, 64-column tile, chain); 8 warps: warps w and w+4
-// read accumulator lanes 32(w%4).. and take column halves 0 and 1
+// read accumulator lanes 32(w%4).. and take column halves 0 and 1.  Thread 0
+// issues the copies of the three splits on three barriers and starts the
+// products of a split pair as soon as both of its images have landed.
 __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigned char* img_all, int parity) {
   __shared__ BDesc sd;
-  __shared__ __align__(8) uint64_t s_load, s_mma;
+  __shared__ __align__(8) uint64_t s_load[3], s_mma;
   __shared__ uint32_t s_taddr;
-  __shared__ int s_fail;
+  __shared__ int s_fail, s_commit;
   extern __shared__ __align__(1024) unsigned char um_dyn[];   // 3 A images, then 3 B images
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     sd = D[blockIdx.y];
     s_fail = 0;
-    mbar_init(&s_load, 1);
+    s_commit = 0;
+    for (int s3 = 0; s3 < 3; ++s3) mbar_init(&s_load[s3], 1);
     mbar_init(&s_mma, 1);
     fence_mbar_init();
   }
@@ -1040,74 +1074,86 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigne
   const int K = *d.kcount;
   const int ns = d.M.ns, RT = um_rtiles(ns);
   const int ti = blockIdx.x % RT, tj = blockIdx.x / RT;
+  const int nrg_a = um_rg(ns, ti), ncg = um_cg(ns, tj), nrg_b = 2 * ncg;
   if (K > 0) {
     if (blockIdx.x == 0 && tid == 0) atomicAdd(d.nflush, 1ull);
     const int K16 = (K + 15) & ~15;
     const unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
-    const uint32_t part = (uint32_t)(K16 / 8) * UM_LBO;   // bytes of k < K16 in one half
+    const uint32_t ka = (uint32_t)nrg_a * 128, kb = (uint32_t)nrg_b * 128;   // bytes per K group
+    const uint32_t part_a = (uint32_t)(K16 / 8) * ka, part_b = (uint32_t)(K16 / 8) * kb;   // k < K16 of one half
+    const uint32_t h2a = (uint32_t)(UM_KP / 8) * ka, h2b = (uint32_t)(UM_KP / 8) * kb;
     if (tid == 0) {
-      mbar_arrive_tx(&s_load, 6u * 2u * part);
       for (int s3 = 0; s3 < 3; ++s3) {
         const unsigned char* ga = img + ((size_t)ti * 3 + s3) * UM_IMG;
         const unsigned char* gb = img + ((size_t)(RT + tj) * 3 + s3) * UM_IMG;
         unsigned char* sa = um_dyn + (size_t)s3 * UM_IMG;
         unsigned char* sb = um_dyn + (size_t)(3 + s3) * UM_IMG;
-        const size_t h2 = (size_t)(UM_KP / 8) * UM_LBO;
-        bulk_g2s(sa, ga, part, &s_load);
-        bulk_g2s(sa + h2, ga + h2, part, &s_load);
-        bulk_g2s(sb, gb, part, &s_load);
-        bulk_g2s(sb + h2, gb + h2, part, &s_load);
+        mbar_arrive_tx(&s_load[s3], 2u * (part_a + part_b));
+        bulk_g2s(sa, ga, part_a, &s_load[s3]);
+        bulk_g2s(sa + h2a, ga + h2a, part_a, &s_load[s3]);
+        bulk_g2s(sb, gb, part_b, &s_load[s3]);
+        bulk_g2s(sb + h2b, gb + h2b, part_b, &s_load[s3]);
       }
-      if (!mbar_wait_bounded(&s_load, 0)) s_fail = 1;
-      um_fence_after();
-      if (!s_fail) {
-        // split pairs (A', B'): (0,0) (0,1) (1,0) (0,2) (1,1) (2,0), packed 2 bits each
-        constexpr uint32_t PA = 0u | (0u << 2) | (1u << 4) | (0u << 6) | (1u << 8) | (2u << 10);
-        constexpr uint32_t PB = 0u | (1u << 2) | (0u << 4) | (2u << 6) | (1u << 8) | (0u << 10);
-        const uint32_t base = smem_addr(um_dyn);
-        uint32_t acc = 0;
-        for (int pr = 0; pr < 6; ++pr) {
-          const uint32_t sa = (PA >> (2 * pr)) & 3u, sb = (PB >> (2 * pr)) & 3u;
-          for (int half = 0; half < 2; ++half)
-            for (int kk = 0; kk < K16 / 16; ++kk) {
-              const uint32_t off = (uint32_t)half * (UM_KP / 8) * UM_LBO + (uint32_t)kk * 2 * UM_LBO;
-              const uint64_t ad = um_desc(base + sa * UM_IMG + off, UM_LBO, 128);
-              const uint64_t bd = um_desc(base + (3 + sb) * UM_IMG + off, UM_LBO, 128);
-              um_mma(taddr, ad, bd, acc);
-              acc = 1;
-            }
+      // split pairs (A', B'): (0,0) (0,1) (1,0) (0,2) (1,1) (2,0), packed 2 bits each
+      constexpr uint32_t PA = 0u | (0u << 2) | (1u << 4) | (0u << 6) | (1u << 8) | (2u << 10);
+      constexpr uint32_t PB = 0u | (1u << 2) | (0u << 4) | (2u << 6) | (1u << 8) | (0u << 10);
+      const uint32_t base = smem_addr(um_dyn), idesc = um_idesc(16u * (uint32_t)ncg);
+      uint32_t acc = 0;
+      int landed = 0;   // splits whose images are in shared memory
+      for (int pr = 0; pr < 6 && !s_fail; ++pr) {
+        const uint32_t sa = (PA >> (2 * pr)) & 3u, sb = (PB >> (2 * pr)) & 3u;
+        const int need = (int)(sa > sb ? sa : sb);
+        while (landed <= need && !s_fail) {
+          if (!mbar_wait_bounded(&s_load[landed], 0)) s_fail = 1;
+          ++landed;
         }
+        if (s_fail) break;
+        um_fence_after();
+        for (int half = 0; half < 2; ++half)
+          for (int kk = 0; kk < K16 / 16; ++kk) {
+            const uint64_t ad = um_desc(base + sa * UM_IMG + half * h2a + kk * 2 * ka, ka, 128);
+            const uint64_t bd = um_desc(base + (3 + sb) * UM_IMG + half * h2b + kk * 2 * kb, kb, 128);
+            um_mma(taddr, ad, bd, idesc, acc);
+            acc = 1;
+          }
+      }
+      if (acc) {   // track every issued product, so TMEM is not freed under it
         um_commit(&s_mma);
+        s_commit = 1;
       }
     }
+    // epilogue: accumulator lanes (rows) 32(w%4)..+31, columns of half w/4
+    // (re at TMEM column c, im at 8 ncg + c).  The thread's 32 G entries are
+    // read while the images load and the MMAs run (the tile belongs to this
+    // CTA alone), so the epilogue only waits for the accumulator.
+    float4* G = reinterpret_cast<float4*>(parity ? d.g_alt : d.g);
+    const int q = warp & 3, half = warp >> 2;
+    const int r = ti * 128 + q * 32 + lane;
+    const int col0 = tj * 64 + half * 32;
+    const int ncol = min(32, ns - col0);
+    float4 gv[32];
+    if (r < ns) {
+#pragma unroll
+      for (int c = 0; c < 32; ++c)
+        if (c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c)];
+    }
     __syncthreads();
-    if (!s_fail) {
+    if (s_commit) {
       if (!mbar_wait_bounded(&s_mma, 0)) s_fail = 1;   // every thread observes the commit
       um_fence_after();
     }
     __syncthreads();
     if (!s_fail) {
-      // epilogue: accumulator lanes (rows) 32(w%4)..+31, columns of half w/4;
-      // the 32 G entries of the thread are loaded before any is written
-      float4* G = reinterpret_cast<float4*>(parity ? d.g_alt : d.g);
-      const int q = warp & 3, half = warp >> 2;
-      const int r = ti * 128 + q * 32 + lane;
-      const int col0 = tj * 64 + half * 32;
-      const int ncol = min(32, ns - col0);
-      float4 gv[32];
-      if (r < ns) {
+      if (ncol > 0) {   // warp-uniform
+        float re[32], im[32];
+        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+        um_ld32(taddr + lane_base + half * 32, re);
+        um_ld32(taddr + lane_base + 8 * ncg + half * 32, im);
+        if (r < ns) {
 #pragma unroll
-        for (int c = 0; c < 32; ++c)
-          if (c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c)];
-      }
-      float re[32], im[32];
-      const uint32_t lane_base = (uint32_t)(q * 32) << 16;
-      um_ld32(taddr + lane_base + half * 32, re);
-      um_ld32(taddr + lane_base + 64 + half * 32, im);
-      if (r < ns) {
-#pragma unroll
-        for (int c = 0; c < 32; ++c)
-          if (c < ncol) G[r + (size_t)ns * (col0 + c)] = dg_addf(gv[c], make_float2(re[c], im[c]));
+          for (int c = 0; c < 32; ++c)
+            if (c < ncol) G[r + (size_t)ns * (col0 + c)] = dg_addf(gv[c], make_float2(re[c], im[c]));
+        }
       }
     } else if (tid == 0) {
       atomicExch(d.err, PQMC_ERR_TIMEOUT);
@@ -1427,7 +1473,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     PQMC_LAUNCHED();
     gphase_end(b, g, PQMC_PHASE_SCAN, ts);
     if (b->flush_mode == 1 && img && kd <= UM_KP) {
-      const long items = (long)(um_rtiles(ns) + um_ctiles(ns)) * 128 * (((kd + 15) & ~15) / 8);
+      const long items = 2L * ((ns + 7) / 8 * 8) * (((kd + 15) & ~15) / 8);
       cudaEvent_t tsp = gphase_begin(b, g);
       k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, st>>>(Dg, img);
       PQMC_LAUNCHED();

@@ -1166,24 +1166,31 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigne
 
 // ---------------------------------------------------------------------------
 // Two-way wrap with an FP32 correction on the FP64 G (left: A=expKV, B=expKV_inv).
-// One thread per (row item, column item) block of the family's cover; items
-// are the family's plaquettes (DIM sites) and uncovered singletons, so every
-// block is at most DIM x DIM and lives in registers.
+// Items are the family's plaquettes (DIM sites) and uncovered singletons, so
+// every block of G between a row item and a column item is at most DIM x DIM
+// and lives in registers.  A CTA takes WRAP_R row items x WRAP_C column items,
+// one pair per thread, and first forms (A - I) of its row items and (B - I)
+// of its column items once, in FP64 rounded to FP32, into shared memory
+// (entry-major, so the threads of a warp read consecutive words).
+constexpr int WRAP_R = 32, WRAP_C = 4;
 template <int DIM>
-__global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int left, int n_items, int parity,
+__global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int left, int n_items, int parity,
                                                const int* __restrict__ wpla, const int* __restrict__ wsites,
                                                const int* __restrict__ wdim) {
   __shared__ BDesc sd;
-  if (threadIdx.x == 0) sd = D[blockIdx.y];
+  __shared__ float2 s_am[DIM * DIM][WRAP_R];   // (A - I)(a, b) of row item lr at [a + DIM b][lr]
+  __shared__ float2 s_bm[DIM * DIM][WRAP_C];
+  if (threadIdx.x == 0) sd = D[blockIdx.z];
   __syncthreads();
   const BDesc& d = sd;
-  const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (pair >= (long)n_items * n_items) return;
   const DevModel& M = d.M;
   const int t = d.t;
-  const int ir = (int)(pair % n_items), ic = (int)(pair / n_items);
   const int ns = M.ns, pd = M.pdim;
-  const int dr = wdim[ir], dc = wdim[ic];
+  const int ir0 = blockIdx.x * WRAP_R, ic0 = blockIdx.y * WRAP_C;
+  const int lr = threadIdx.x % WRAP_R, lc = threadIdx.x / WRAP_R;
+  const int ir = ir0 + lr, ic = ic0 + lc;
+  const bool live = ir < n_items && ic < n_items;
+  const int dr = live ? wdim[ir] : 0, dc = live ? wdim[ic] : 0;
   const float4* gin = reinterpret_cast<const float4*>(parity ? d.g_alt : d.g);   // double-float G
   float4* gout = reinterpret_cast<float4*>(parity ? d.g : d.g_alt);
   int Sr[DIM], Sc[DIM];
@@ -1192,28 +1199,36 @@ __global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int left,
     Sr[k] = k < dr ? wsites[4 * ir + k] : 0;
     Sc[k] = k < dc ? wsites[4 * ic + k] : 0;
   }
+  // the block of G, loaded first so that the loads are in flight while the
+  // CTA forms its (A - I) and (B - I); its FP32 rounding dg_f2 is formed
+  // where it is used (fewer registers)
   float4 gd[DIM][DIM];
-  float2 gf[DIM][DIM], am[DIM][DIM], bm[DIM][DIM];
 #pragma unroll
   for (int b = 0; b < DIM; ++b)
 #pragma unroll
-    for (int a = 0; a < DIM; ++a) {
+    for (int a = 0; a < DIM; ++a)
       gd[a][b] = (a < dr && b < dc) ? gin[Sr[a] + (size_t)ns * Sc[b]] : make_float4(0.f, 0.f, 0.f, 0.f);
-      gf[a][b] = dg_f2(gd[a][b]);
+  // A - I and B - I formed in FP64 and rounded once; zero for singletons.
+  // Consecutive threads take consecutive items of one entry.
+  for (int e = threadIdx.x; e < (WRAP_R + WRAP_C) * DIM * DIM; e += blockDim.x) {
+    const bool isc = e >= WRAP_R * DIM * DIM;
+    const int e2 = isc ? e - WRAP_R * DIM * DIM : e;
+    const int nl = isc ? WRAP_C : WRAP_R;
+    const int il = e2 % nl, ent = e2 / nl, a = ent % DIM, b = ent / DIM;
+    const int item = (isc ? ic0 : ir0) + il;
+    float2 v = make_float2(0.f, 0.f);
+    if (item < n_items) {
+      const int p = wpla[item], dm = wdim[item];
+      if (p >= 0 && a < dm && b < dm) {
+        const cplx* X = (isc ? (left ? d.expkv_inv : d.expkv) : (left ? d.expkv : d.expkv_inv)) + M.kv_base(p, pf, t);
+        v = f2(csub(X[a + pd * b], mk(a == b ? 1.0 : 0.0)));
+      }
     }
-  const int pr = wpla[ir], pc = wpla[ic];
-  const cplx* Am = (pr >= 0) ? (left ? d.expkv : d.expkv_inv) + M.kv_base(pr, pf, t) : nullptr;
-  const cplx* Bm = (pc >= 0) ? (left ? d.expkv_inv : d.expkv) + M.kv_base(pc, pf, t) : nullptr;
-  // (A - I) and (B - I) in FP32; identity blocks for singletons
-#pragma unroll
-  for (int b = 0; b < DIM; ++b)
-#pragma unroll
-    for (int a = 0; a < DIM; ++a) {
-      // A - I and B - I formed in FP64 and rounded once
-      const double one = a == b ? 1.0 : 0.0;
-      am[a][b] = (Am && a < dr && b < dr) ? f2(csub(Am[a + pd * b], mk(one))) : make_float2(0.f, 0.f);
-      bm[a][b] = (Bm && a < dc && b < dc) ? f2(csub(Bm[a + pd * b], mk(one))) : make_float2(0.f, 0.f);
-    }
+    if (isc) s_bm[ent][il] = v;
+    else s_am[ent][il] = v;
+  }
+  __syncthreads();
+  if (!live) return;
   // corr = (A - I) (G B) + G (B - I) = (A - I) G + (A - I) G (B - I) + G (B - I)
   float2 gb[DIM][DIM];   // G (B - I)
 #pragma unroll
@@ -1222,7 +1237,7 @@ __global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int left,
     for (int a = 0; a < DIM; ++a) {
       float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) s = fa(s, fm(gf[a][k], bm[k][b]));
+      for (int k = 0; k < DIM; ++k) s = fa(s, fm(dg_f2(gd[a][k]), s_bm[k + DIM * b][lc]));
       gb[a][b] = s;
     }
 #pragma unroll
@@ -1231,7 +1246,7 @@ __global__ void __launch_bounds__(128) k_bwrap(const BDesc* D, int pf, int left,
     for (int a = 0; a < DIM; ++a) {
       float2 corr = gb[a][b];
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) corr = fa(corr, fm(am[a][k], fa(gf[k][b], gb[k][b])));
+      for (int k = 0; k < DIM; ++k) corr = fa(corr, fm(s_am[a + DIM * k][lr], fa(dg_f2(gd[k][b]), gb[k][b])));
       if (a < dr && b < dc) gout[Sr[a] + (size_t)ns * Sc[b]] = dg_addf(gd[a][b], corr);
     }
 }
@@ -1408,8 +1423,8 @@ static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
   const int C = b->g_count[g];
   const BDesc* D = b->d_desc + b->g_first[g];
   cudaStream_t st = b->g_stream[g];
-  long pairs = (long)w.n_items * w.n_items;
-  dim3 grid((unsigned)((pairs + 127) / 128), (unsigned)C);
+  const dim3 grid((unsigned)((w.n_items + WRAP_R - 1) / WRAP_R), (unsigned)((w.n_items + WRAP_C - 1) / WRAP_C),
+                  (unsigned)C);
   const int l = left ? 1 : 0;
   cudaEvent_t tw = gphase_begin(b, g);
   switch (c0->h_pf_dim[pf]) {

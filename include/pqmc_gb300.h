@@ -382,7 +382,10 @@ int pqmc_batch_init(pqmc_batch* batch);
 int pqmc_batch_stream(pqmc_batch* batch, void** stream);
 /* info[5] = {chains, chain groups (streams), delay depth, flush engine,
  * precision}; the groups default to one per 8 chains (at most 8) and can
- * be set with the environment variable PQMC_BATCH_GROUPS (1..16) at creation */
+ * be set with the environment variable PQMC_BATCH_GROUPS (1..16) at creation.
+ * A mixed batch wraps G with whole columns staged in shared memory where
+ * they fit; PQMC_WRAP_COLS=0 at creation keeps the per-block gather form
+ * (the same arithmetic, entry for entry). */
 int pqmc_batch_info(pqmc_batch* batch, int* info);
 /* Uneven batches (mixed precision): chains of different geometry (Ns, Lt,
  * families) are grouped into classes of equal geometry; each class runs

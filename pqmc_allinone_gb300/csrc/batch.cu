@@ -1251,6 +1251,170 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
     }
 }
 
+// Two-way wrap with whole columns of G staged in shared memory (used when
+// they fit).  The family's cover items partition the sites, so a CTA that
+// owns WRAPC_C column items owns every entry of their columns: it brings the
+// columns in with 1-D bulk copies, forms (A - I) of every row item and
+// (B - I) of its column items (FP64, rounded once), updates each block (row
+// item x column item) in place with the arithmetic of k_bwrap, entry for
+// entry, and writes the columns back with bulk stores.  Every entry of G is
+// read and written once, in whole columns.
+constexpr int WRAPC_C = 2;
+constexpr size_t WRAPC_MAX_SMEM = 200 * 1024;   // dynamic shared memory of k_bwrap_cols at most
+__host__ __device__ inline size_t wrapc_smem(int ns, int n_items, int dim) {
+  return (size_t)WRAPC_C * dim * ns * 16 + (size_t)dim * dim * (n_items + WRAPC_C) * 8 + (size_t)n_items * 6 * 4;
+}
+__device__ __forceinline__ void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_addr(ssrc)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit_wait_all() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+template <int DIM>
+__global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
+                                                    const int* __restrict__ wpla, const int* __restrict__ wsites,
+                                                    const int* __restrict__ wdim) {
+  __shared__ BDesc sd;
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ int s_fail;
+  extern __shared__ __align__(128) unsigned char wc_dyn[];
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    sd = D[blockIdx.y];
+    s_fail = 0;
+    mbar_init(&s_bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const BDesc& d = sd;
+  const DevModel& M = d.M;
+  const int t = d.t;
+  const int ns = M.ns, pd = M.pdim;
+  const int ic0 = blockIdx.x * WRAPC_C, ncl = min(WRAPC_C, n_items - ic0);
+  float4* s_col = reinterpret_cast<float4*>(wc_dyn);                              // [WRAPC_C * DIM][ns]
+  float2* s_am = reinterpret_cast<float2*>(s_col + (size_t)WRAPC_C * DIM * ns);   // [DIM * DIM][n_items]
+  float2* s_bm = s_am + (size_t)DIM * DIM * n_items;                              // [DIM * DIM][WRAPC_C]
+  int* s_pla = reinterpret_cast<int*>(s_bm + (size_t)DIM * DIM * WRAPC_C);        // cover items: plaquette,
+  int* s_dim = s_pla + n_items;                                                   // dimension and
+  int* s_site = s_dim + n_items;                                                  // sites (4 per item)
+  const float4* gin = reinterpret_cast<const float4*>(parity ? d.g_alt : d.g);   // double-float G
+  float4* gout = reinterpret_cast<float4*>(parity ? d.g : d.g_alt);
+  const uint32_t cbytes = (uint32_t)ns * 16u;   // one column of G
+  if (tid == 0) {
+    // the sites of the column items, all loads issued before any is used
+    int cdim[WRAPC_C], csite[WRAPC_C][DIM];
+#pragma unroll
+    for (int icl = 0; icl < WRAPC_C; ++icl) {
+      cdim[icl] = icl < ncl ? wdim[ic0 + icl] : 0;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) csite[icl][b] = icl < ncl ? wsites[4 * (ic0 + icl) + b] : 0;
+    }
+    uint32_t bytes = 0;
+#pragma unroll
+    for (int icl = 0; icl < WRAPC_C; ++icl) bytes += (uint32_t)cdim[icl] * cbytes;
+    mbar_arrive_tx(&s_bar, bytes);
+#pragma unroll
+    for (int icl = 0; icl < WRAPC_C; ++icl)
+#pragma unroll
+      for (int b = 0; b < DIM; ++b)
+        if (b < cdim[icl])
+          bulk_g2s(s_col + (size_t)(icl * DIM + b) * ns, gin + (size_t)ns * csite[icl][b], cbytes, &s_bar);
+  }
+  for (int e = tid; e < n_items; e += blockDim.x) {
+    s_pla[e] = wpla[e];
+    s_dim[e] = wdim[e];
+  }
+  for (int e = tid; e < 4 * n_items; e += blockDim.x) s_site[e] = wsites[e];
+  __syncthreads();
+  // A - I of every row item and B - I of the CTA's column items, formed in
+  // FP64 and rounded once (zero for singletons); consecutive threads take
+  // consecutive items of one entry, four entries per thread in flight
+  const int n_ent = (n_items + WRAPC_C) * DIM * DIM;
+  for (int e0 = tid; e0 < n_ent; e0 += 4 * blockDim.x) {
+    cplx x[4];
+    int slot[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * blockDim.x;
+      slot[u] = -1;
+      x[u] = mk(0.0);
+      if (e >= n_ent) continue;
+      const bool isc = e >= n_items * DIM * DIM;
+      const int e2 = isc ? e - n_items * DIM * DIM : e;
+      const int nl = isc ? WRAPC_C : n_items;
+      const int il = e2 % nl, ent = e2 / nl, a = ent % DIM, b = ent / DIM;
+      const int item = isc ? ic0 + il : il;
+      slot[u] = isc ? n_items * DIM * DIM + ent * WRAPC_C + il : ent * n_items + il;
+      if (item < n_items) {
+        const int p = s_pla[item], dm = s_dim[item];
+        if (p >= 0 && a < dm && b < dm) {
+          const cplx* X = (isc ? (left ? d.expkv_inv : d.expkv) : (left ? d.expkv : d.expkv_inv)) + M.kv_base(p, pf, t);
+          x[u] = csub(X[a + pd * b], mk(a == b ? 1.0 : 0.0));
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (slot[u] >= 0) s_am[slot[u]] = f2(x[u]);   // s_bm follows s_am contiguously
+  }
+  if (!mbar_wait_bounded(&s_bar, 0)) s_fail = 1;
+  __syncthreads();
+  if (s_fail) {
+    if (tid == 0) atomicExch(d.err, PQMC_ERR_TIMEOUT);
+    return;
+  }
+  for (int pr = tid; pr < n_items * ncl; pr += blockDim.x) {
+    const int ir = pr % n_items, icl = pr / n_items, ic = ic0 + icl;
+    const int dr = s_dim[ir], dc = s_dim[ic];
+    int Sr[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) Sr[k] = k < dr ? s_site[4 * ir + k] : 0;
+    float4* col = s_col + (size_t)icl * DIM * ns;
+    float4 gd[DIM][DIM];
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int a = 0; a < DIM; ++a)
+        gd[a][b] = (a < dr && b < dc) ? col[(size_t)b * ns + Sr[a]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // corr = (A - I) (G B) + G (B - I), as in k_bwrap
+    float2 gb[DIM][DIM];   // G (B - I)
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        float2 sum = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) sum = fa(sum, fm(dg_f2(gd[a][k]), s_bm[(size_t)(k + DIM * b) * WRAPC_C + icl]));
+        gb[a][b] = sum;
+      }
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        float2 corr = gb[a][b];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+          corr = fa(corr, fm(s_am[(size_t)(a + DIM * k) * n_items + ir], fa(dg_f2(gd[k][b]), gb[k][b])));
+        if (a < dr && b < dc) col[(size_t)b * ns + Sr[a]] = dg_addf(gd[a][b], corr);
+      }
+  }
+  fence_proxy_async_smem();   // the updated columns visible to the bulk stores
+  __syncthreads();
+  if (tid == 0) {
+    for (int icl = 0; icl < ncl; ++icl) {
+      const int dc = s_dim[ic0 + icl];
+      for (int b = 0; b < dc; ++b)
+        bulk_s2g(gout + (size_t)ns * s_site[4 * (ic0 + icl) + b], s_col + (size_t)(icl * DIM + b) * ns, cbytes);
+    }
+    bulk_commit_wait_all();
+  }
+}
+
 // G of every chain converted in place between FP64 complex (at rest) and the
 // double-float float4 form the mixed sweep works on
 __global__ void k_gconv(const BDesc* D, int to_df, long n, int parity) {
@@ -1317,6 +1481,7 @@ struct pqmc_batch {
     int kernels;  // kernel nodes per replay
   };
   bool graphs = false;
+  std::vector<char> wrap_cols;   // per family: k_bwrap_cols (columns of G fit in shared memory) or k_bwrap
   std::deque<SliceGraph> gcache;
   // proposal records of every family per chain (n_pf x max_pla); when the
   // families' bosons are disjoint, a slice's draws and proposals of all
@@ -1423,10 +1588,23 @@ static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
   const int C = b->g_count[g];
   const BDesc* D = b->d_desc + b->g_first[g];
   cudaStream_t st = b->g_stream[g];
-  const dim3 grid((unsigned)((w.n_items + WRAP_R - 1) / WRAP_R), (unsigned)((w.n_items + WRAP_C - 1) / WRAP_C),
-                  (unsigned)C);
   const int l = left ? 1 : 0;
   cudaEvent_t tw = gphase_begin(b, g);
+  if (pf < (int)b->wrap_cols.size() && b->wrap_cols[pf]) {
+    const dim3 gc((unsigned)((w.n_items + WRAPC_C - 1) / WRAPC_C), (unsigned)C);
+    const size_t sm = wrapc_smem(c0->ns, w.n_items, c0->h_pf_dim[pf]);
+    switch (c0->h_pf_dim[pf]) {
+      case 1: k_bwrap_cols<1><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+      case 2: k_bwrap_cols<2><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+      case 3: k_bwrap_cols<3><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+      default: k_bwrap_cols<4><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+    }
+    PQMC_LAUNCHED();
+    gphase_end(b, g, PQMC_PHASE_WRAP, tw);
+    return PQMC_OK;
+  }
+  const dim3 grid((unsigned)((w.n_items + WRAP_R - 1) / WRAP_R), (unsigned)((w.n_items + WRAP_C - 1) / WRAP_C),
+                  (unsigned)C);
   switch (c0->h_pf_dim[pf]) {
     case 1: k_bwrap<1><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
     case 2: k_bwrap<2><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
@@ -1889,6 +2067,25 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     PQMC_CUDA(cudaMalloc((void**)&b->d_img, ib));
     PQMC_CUDA(cudaMemset(b->d_img, 0, ib));
     PQMC_CUDA(raise_dyn_smem(k_bflush_um, 6 * UM_IMG));
+    // wrap with whole columns staged in shared memory where they fit
+    // (PQMC_WRAP_COLS=0 keeps the gather form)
+    const char* wenv = getenv("PQMC_WRAP_COLS");
+    const bool wc_on = !(wenv && atoi(wenv) == 0);
+    b->wrap_cols.assign(c0->n_pf, 0);
+    for (int f = 0; f < c0->n_pf && wc_on; ++f) {
+      const int dim = c0->h_pf_dim[f];
+      const size_t sm = wrapc_smem(c0->ns, c0->wrap[f].n_items, dim);
+      if (dim < 1 || dim > 4 || sm > WRAPC_MAX_SMEM) continue;
+      cudaError_t e;
+      switch (dim) {
+        case 1: e = raise_dyn_smem(k_bwrap_cols<1>, (int)sm); break;
+        case 2: e = raise_dyn_smem(k_bwrap_cols<2>, (int)sm); break;
+        case 3: e = raise_dyn_smem(k_bwrap_cols<3>, (int)sm); break;
+        default: e = raise_dyn_smem(k_bwrap_cols<4>, (int)sm); break;
+      }
+      PQMC_CUDA(e);
+      b->wrap_cols[f] = 1;
+    }
   }
   b->h_desc.resize(n_chains);
   for (int i = 0; i < n_chains; ++i) {

@@ -210,6 +210,25 @@ def test_slice_graphs_bit_identical():
         assert s0["positive_accept"] > 0
 
 
+def test_wrap_column_staging_bit_identical(monkeypatch):
+    """The wrap with whole columns of G staged in shared memory (bulk copies
+    in and out, blocks updated in place) and the gather form that reads and
+    writes each block of a cover-item pair directly compute every entry with
+    the same arithmetic: the chains come out bit for bit the same."""
+    ms = []
+    for i in range(3):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=140 + i)
+        ms.append((m, f, seed_words(1400 + i)))
+    monkeypatch.setenv("PQMC_WRAP_COLS", "0")
+    gather, _, _ = _run_batch(ms, (1, 2), graphs=True)
+    monkeypatch.setenv("PQMC_WRAP_COLS", "1")
+    staged, _, _ = _run_batch(ms, (1, 2), graphs=True)
+    for (f0, g0, s0), (f1, g1, s1) in zip(gather, staged):
+        assert np.array_equal(f0, f1) and np.array_equal(g0, g1)
+        assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
+        assert s0["positive_accept"] > 0
+
+
 def test_uneven_batch_matches_its_classes():
     """A mixed batch of chains of uneven L and Lt (C3-shaped, scaled down)
     splits into geometry classes that interleave on their own streams; every

@@ -200,7 +200,7 @@ def cpu_baseline(m, field, words, slices: int) -> dict:
     o.init_g(1)
     secs = o.time_parallel(cores, cores, 1, slices)
     sweeps = cores * slices / m.ntime
-    return {"value": sweeps / secs, "unit": "sweeps/s", "cores": cores, "kind": "port",
+    return {"value": sweeps / secs, "unit": "chain-sweeps/s", "cores": cores, "kind": "port",
             "sample": f"{cores} chains x {slices} slices of one backward sweep ({slices}/{m.ntime} sweep each, "
                       f"incl. {slices // m.ngroup} recomputes), {secs:.1f} s wall",
             "per_core": sweeps / secs / cores}

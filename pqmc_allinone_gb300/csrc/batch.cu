@@ -1040,24 +1040,42 @@ __device__ __forceinline__ void um_ld32(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
+// 32 lanes x 16 consecutive FP32 columns of tensor memory into registers
+__device__ __forceinline__ void um_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
 
-// one CTA per (128-row tile, 64-column tile, chain); 8 warps: warps w and w+4
-// read accumulator lanes 32(w%4).. and take column halves 0 and 1.  Thread 0
-// issues the copies of the three splits on three barriers and starts the
-// products of a split pair as soon as both of its images have landed.
-__global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigned char* img_all, int parity) {
+// one CTA per (128-row tile, 64-column tile, chain), two CTAs per SM; 8
+// warps: warps w and w+4 read accumulator lanes 32(w%4).. and take column
+// halves 0 and 1.  Thread 0 streams the six images through shared memory in
+// their two K halves (the Ar/Br part, then the Ai part): copies of a half,
+// the six split products over it, and the next half's copies once those
+// products have read the buffer.  Each thread reads the first 16 of its 32
+// G entries while the copies and products run, the rest after.
+constexpr int UM_HALF = UM_IMG / 2;   // bytes of one K half of a tile image (16 KB)
+__global__ void __launch_bounds__(256, 2) k_bflush_um(const BDesc* D, const unsigned char* img_all, int parity) {
   __shared__ BDesc sd;
-  __shared__ __align__(8) uint64_t s_load[3], s_mma;
+  __shared__ __align__(8) uint64_t s_load[2], s_mma[2];
   __shared__ uint32_t s_taddr;
-  __shared__ int s_fail, s_commit;
-  extern __shared__ __align__(1024) unsigned char um_dyn[];   // 3 A images, then 3 B images
+  __shared__ int s_fail, s_last;
+  extern __shared__ __align__(1024) unsigned char um_dyn[];   // 3 A half-images, then 3 B half-images
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     sd = D[blockIdx.y];
     s_fail = 0;
-    s_commit = 0;
-    for (int s3 = 0; s3 < 3; ++s3) mbar_init(&s_load[s3], 1);
-    mbar_init(&s_mma, 1);
+    s_last = -1;
+    for (int h = 0; h < 2; ++h) {
+      mbar_init(&s_load[h], 1);
+      mbar_init(&s_mma[h], 1);
+    }
     fence_mbar_init();
   }
   __syncwarp();
@@ -1081,78 +1099,84 @@ __global__ void __launch_bounds__(256) k_bflush_um(const BDesc* D, const unsigne
     const unsigned char* img = img_all + um_chain_bytes(ns) * blockIdx.y;
     const uint32_t ka = (uint32_t)nrg_a * 128, kb = (uint32_t)nrg_b * 128;   // bytes per K group
     const uint32_t part_a = (uint32_t)(K16 / 8) * ka, part_b = (uint32_t)(K16 / 8) * kb;   // k < K16 of one half
-    const uint32_t h2a = (uint32_t)(UM_KP / 8) * ka, h2b = (uint32_t)(UM_KP / 8) * kb;
+    const uint32_t h2a = (uint32_t)(UM_KP / 8) * ka, h2b = (uint32_t)(UM_KP / 8) * kb;     // second half in global
     if (tid == 0) {
-      for (int s3 = 0; s3 < 3; ++s3) {
-        const unsigned char* ga = img + ((size_t)ti * 3 + s3) * UM_IMG;
-        const unsigned char* gb = img + ((size_t)(RT + tj) * 3 + s3) * UM_IMG;
-        unsigned char* sa = um_dyn + (size_t)s3 * UM_IMG;
-        unsigned char* sb = um_dyn + (size_t)(3 + s3) * UM_IMG;
-        mbar_arrive_tx(&s_load[s3], 2u * (part_a + part_b));
-        bulk_g2s(sa, ga, part_a, &s_load[s3]);
-        bulk_g2s(sa + h2a, ga + h2a, part_a, &s_load[s3]);
-        bulk_g2s(sb, gb, part_b, &s_load[s3]);
-        bulk_g2s(sb + h2b, gb + h2b, part_b, &s_load[s3]);
-      }
       // split pairs (A', B'): (0,0) (0,1) (1,0) (0,2) (1,1) (2,0), packed 2 bits each
       constexpr uint32_t PA = 0u | (0u << 2) | (1u << 4) | (0u << 6) | (1u << 8) | (2u << 10);
       constexpr uint32_t PB = 0u | (1u << 2) | (0u << 4) | (2u << 6) | (1u << 8) | (0u << 10);
       const uint32_t base = smem_addr(um_dyn), idesc = um_idesc(16u * (uint32_t)ncg);
       uint32_t acc = 0;
-      int landed = 0;   // splits whose images are in shared memory
-      for (int pr = 0; pr < 6 && !s_fail; ++pr) {
-        const uint32_t sa = (PA >> (2 * pr)) & 3u, sb = (PB >> (2 * pr)) & 3u;
-        const int need = (int)(sa > sb ? sa : sb);
-        while (landed <= need && !s_fail) {
-          if (!mbar_wait_bounded(&s_load[landed], 0)) s_fail = 1;
-          ++landed;
+      for (int half = 0; half < 2 && !s_fail; ++half) {
+        if (half == 1) {   // the products of half 0 have read the buffer
+          if (!mbar_wait_bounded(&s_mma[0], 0)) {
+            s_fail = 1;
+            break;
+          }
+          um_fence_after();
         }
-        if (s_fail) break;
+        mbar_arrive_tx(&s_load[half], 3u * (part_a + part_b));
+        for (int s3 = 0; s3 < 3; ++s3) {
+          const unsigned char* ga = img + ((size_t)ti * 3 + s3) * UM_IMG + half * h2a;
+          const unsigned char* gb = img + ((size_t)(RT + tj) * 3 + s3) * UM_IMG + half * h2b;
+          bulk_g2s(um_dyn + (size_t)s3 * UM_HALF, ga, part_a, &s_load[half]);
+          bulk_g2s(um_dyn + (size_t)(3 + s3) * UM_HALF, gb, part_b, &s_load[half]);
+        }
+        if (!mbar_wait_bounded(&s_load[half], 0)) {
+          s_fail = 1;
+          break;
+        }
         um_fence_after();
-        for (int half = 0; half < 2; ++half)
+        for (int pr = 0; pr < 6; ++pr) {
+          const uint32_t sa = (PA >> (2 * pr)) & 3u, sb = (PB >> (2 * pr)) & 3u;
           for (int kk = 0; kk < K16 / 16; ++kk) {
-            const uint64_t ad = um_desc(base + sa * UM_IMG + half * h2a + kk * 2 * ka, ka, 128);
-            const uint64_t bd = um_desc(base + (3 + sb) * UM_IMG + half * h2b + kk * 2 * kb, kb, 128);
+            const uint64_t ad = um_desc(base + sa * UM_HALF + kk * 2 * ka, ka, 128);
+            const uint64_t bd = um_desc(base + (3 + sb) * UM_HALF + kk * 2 * kb, kb, 128);
             um_mma(taddr, ad, bd, idesc, acc);
             acc = 1;
           }
-      }
-      if (acc) {   // track every issued product, so TMEM is not freed under it
-        um_commit(&s_mma);
-        s_commit = 1;
+        }
+        um_commit(&s_mma[half]);   // also tracks every earlier product
+        s_last = half;
       }
     }
     // epilogue: accumulator lanes (rows) 32(w%4)..+31, columns of half w/4
-    // (re at TMEM column c, im at 8 ncg + c).  The thread's 32 G entries are
-    // read while the images load and the MMAs run (the tile belongs to this
-    // CTA alone), so the epilogue only waits for the accumulator.
+    // (re at TMEM column c, im at 8 ncg + c), in two chunks of 16 columns
     float4* G = reinterpret_cast<float4*>(parity ? d.g_alt : d.g);
     const int q = warp & 3, half = warp >> 2;
     const int r = ti * 128 + q * 32 + lane;
     const int col0 = tj * 64 + half * 32;
     const int ncol = min(32, ns - col0);
-    float4 gv[32];
+    float4 gv[16];
     if (r < ns) {
 #pragma unroll
-      for (int c = 0; c < 32; ++c)
+      for (int c = 0; c < 16; ++c)
         if (c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c)];
     }
     __syncthreads();
-    if (s_commit) {
-      if (!mbar_wait_bounded(&s_mma, 0)) s_fail = 1;   // every thread observes the commit
+    const int last = s_last;
+    if (last >= 0) {
+      if (!mbar_wait_bounded(&s_mma[last], 0)) s_fail = 1;   // every thread observes the last commit
       um_fence_after();
     }
     __syncthreads();
     if (!s_fail) {
-      if (ncol > 0) {   // warp-uniform
-        float re[32], im[32];
-        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
-        um_ld32(taddr + lane_base + half * 32, re);
-        um_ld32(taddr + lane_base + 8 * ncg + half * 32, im);
+      const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+#pragma unroll 1
+      for (int ch = 0; ch < 2; ++ch) {
+        const int c0 = ch * 16;
+        if (ncol <= c0) break;   // warp-uniform
+        if (ch == 1 && r < ns) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c)
+            if (c0 + c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c0 + c)];
+        }
+        float re[16], im[16];
+        um_ld16(taddr + lane_base + half * 32 + c0, re);
+        um_ld16(taddr + lane_base + 8 * ncg + half * 32 + c0, im);
         if (r < ns) {
 #pragma unroll
-          for (int c = 0; c < 32; ++c)
-            if (c < ncol) G[r + (size_t)ns * (col0 + c)] = dg_addf(gv[c], make_float2(re[c], im[c]));
+          for (int c = 0; c < 16; ++c)
+            if (c0 + c < ncol) G[r + (size_t)ns * (col0 + c0 + c)] = dg_addf(gv[c], make_float2(re[c], im[c]));
         }
       }
     } else if (tid == 0) {
@@ -1674,7 +1698,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     }
     cudaEvent_t tf = gphase_begin(b, g);
     if (b->flush_mode == 1 && img && kd <= UM_KP) {
-      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_IMG, st>>>(Dg, img, parity);
+      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_HALF, st>>>(Dg, img, parity);
       PQMC_LAUNCHED();
     } else {
       k_bflush<<<dim3(tiles, C), 256, 0, st>>>(Dg, parity);
@@ -2066,7 +2090,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     const size_t ib = um_chain_bytes(c0->ns) * (size_t)n_chains;
     PQMC_CUDA(cudaMalloc((void**)&b->d_img, ib));
     PQMC_CUDA(cudaMemset(b->d_img, 0, ib));
-    PQMC_CUDA(raise_dyn_smem(k_bflush_um, 6 * UM_IMG));
+    PQMC_CUDA(raise_dyn_smem(k_bflush_um, 6 * UM_HALF));
     // wrap with whole columns staged in shared memory where they fit
     // (PQMC_WRAP_COLS=0 keeps the gather form)
     const char* wenv = getenv("PQMC_WRAP_COLS");

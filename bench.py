@@ -392,7 +392,8 @@ def run_mixed(args, world, rank, local):
     # the delayed-update contraction G += A B (rank-K flush, k_bflush_um).  At
     # delay depth K it does 8*Ns^2*K flop against 32*Ns^2 bytes of G
     # (double-float read and write): 2K/8 = 16 flop/B at K=64, under the HBM
-    # roof (7.3 TB/s x 16 = 117 TFLOP/s), far below the tensor roof.
+    # roof (6.8 TB/s measured copy bandwidth x 16 = 109 TFLOP/s), far below
+    # the tensor roof.
     # Algorithmic bytes: 32*Ns^2 per flush that had columns to fold in
     # (counted on the device per chain), over the flush kernel's own event
     # time (the BF16 split kernel is timed apart).

@@ -1123,6 +1123,7 @@ __global__ void __launch_bounds__(256, 2) k_bflush_um(const BDesc* D, const unsi
         }
         if (!mbar_wait_bounded(&s_load[half], 0)) {
           s_fail = 1;
+          mbar_wait_bounded(&s_load[half], 0);   // a second bounded wait for the copies in flight
           break;
         }
         um_fence_after();
@@ -1389,7 +1390,10 @@ __global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, i
   if (!mbar_wait_bounded(&s_bar, 0)) s_fail = 1;
   __syncthreads();
   if (s_fail) {
-    if (tid == 0) atomicExch(d.err, PQMC_ERR_TIMEOUT);
+    if (tid == 0) {   // a second bounded wait for the copies in flight
+      mbar_wait_bounded(&s_bar, 0);
+      atomicExch(d.err, PQMC_ERR_TIMEOUT);
+    }
     return;
   }
   for (int pr = tid; pr < n_items * ncl; pr += blockDim.x) {

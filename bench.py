@@ -231,7 +231,7 @@ def run_reference(args, world, rank):
            "data": "synthetic", "config": ref_config, "impl": "reference",
            "cpu_baseline": cb, "e2e": {"value": v, "unit": "chain-sweeps/s", "h2d_bytes_per_step": 0,
                                        "d2h_bytes_per_step": 0},
-           "note": "the reference Fortran cannot be built here or on the GPU box (no Fortran compiler, no "
+           "note": "the reference Fortran cannot be built on these machines (no Fortran compiler, no "
                    "LAPACK); this arm times the oracle, the line-cited C++ FP64 restatement of the same path, "
                    "one chain per host core"}
     print(json.dumps(out))

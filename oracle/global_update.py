@@ -3,7 +3,7 @@
 (src/Main_PQMC.f90:87-96), restated in numpy on top of the C++ oracle's
 ran2 stream (oracle_rng_draw) and cal_new_weight_T0.
 
-TEST INFRASTRUCTURE ONLY -- imported by tests/ as the checker.  Parity status:
+TEST INFRASTRUCTURE ONLY -- imported by tests/ to check the GPU results.  Parity status:
 unpinned against reference outputs (the reference ships no golden vectors for
 these moves); the restatement follows the cited lines draw by draw.
 

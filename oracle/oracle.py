@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle/pqmc_oracle.cpp).
 
-TEST INFRASTRUCTURE ONLY -- imported by tests/, __graft_entry__.smoke() (as
-the checker) and bench.py's cpu_baseline leg.  Parity status: unpinned
+TEST INFRASTRUCTURE ONLY -- imported by tests/, __graft_entry__.smoke() (to
+check the GPU results) and bench.py's cpu_baseline leg.  Parity status: unpinned
 against reference outputs (the reference has no golden vectors and cannot
 be built here); see the header of pqmc_oracle.cpp for the invariants that
 pin it instead.

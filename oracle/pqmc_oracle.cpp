@@ -1,6 +1,6 @@
 // pqmc_oracle.cpp -- CPU FP64 restatement of the projector-DQMC hot path of
 // LEOMMM816/PQMC_allinone.  TEST INFRASTRUCTURE ONLY: used by tests/, by
-// __graft_entry__.smoke() as the checker, and by bench.py's cpu_baseline leg.
+// __graft_entry__.smoke() to check the GPU results, and by bench.py's cpu_baseline leg.
 // The product (pqmc_allinone_gb300) never links or calls this file.
 //
 // Parity status: UNPINNED against reference outputs.  The reference ships no

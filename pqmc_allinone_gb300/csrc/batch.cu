@@ -1483,6 +1483,9 @@ struct pqmc_batch {
   int kd = 64;            // delay depth (panel columns per flush)
   int qc = 8;             // panel columns per streamed chunk of the scan
   int flush_mode = 1;     // 1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush
+  // kernels launched at the device's highest stream priority (bit 0: the
+  // scan, bit 1: the split and flush); slice graphs then use node priorities
+  int prio_mask = 3, prio_hi = 0;
   unsigned char* d_img = nullptr;   // split operand tile images of the tcgen05 flush
   CUtensorMap* d_tmaps = nullptr;   // per chain: maps of its two G buffers
   int rb = 0, nrb = 0;              // row box of the maps (columns) and boxes per row
@@ -1663,6 +1666,26 @@ static int bprepare(pqmc_batch* b, int g, int pf_first, int pf_step, int n_fam) 
   return PQMC_OK;
 }
 
+// a launch of k on stream st, at priority prio when use is set (the
+// attribute also marks the node when the stream is being captured)
+template <typename... P, typename... A>
+static cudaError_t launch_at(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool use, int prio,
+                             A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  if (use) {
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = prio;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+
 static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
   const int C = b->g_count[g], c_first = b->g_first[g];
   const BDesc* Dg = b->d_desc + c_first;
@@ -1683,7 +1706,9 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     const size_t smem = scan_layout(npla, ns, h0.ldp, b->qc, kd, 4 * h0.nrb * h0.rb * (int)sizeof(float4)).total;
     cudaEvent_t ts = gphase_begin(b, g);
     const bool one = ns <= SCAN_THREADS;
-#define PQMC_SCAN(DM, R) k_bscan<DM, R><<<C, SCAN_THREADS, smem, st>>>(Dg, pf, parity, kd, b->qc, next)
+#define PQMC_SCAN(DM, R)                                                                                         \
+  PQMC_CUDA(launch_at(k_bscan<DM, R>, dim3(C), dim3(SCAN_THREADS), smem, st, (b->prio_mask & 1) != 0, b->prio_hi, Dg, \
+                      pf, parity, kd, b->qc, next))
     switch (dim) {
       case 1: if (one) PQMC_SCAN(1, 1); else PQMC_SCAN(1, 2); break;
       case 2: if (one) PQMC_SCAN(2, 1); else PQMC_SCAN(2, 2); break;
@@ -1696,13 +1721,15 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     if (b->flush_mode == 1 && img && kd <= UM_KP) {
       const long items = 2L * ((ns + 7) / 8 * 8) * (((kd + 15) & ~15) / 8);
       cudaEvent_t tsp = gphase_begin(b, g);
-      k_bsplit<<<dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), 256, 0, st>>>(Dg, img);
+      PQMC_CUDA(launch_at(k_bsplit, dim3((unsigned)std::min<long>((items + 255) / 256, 256), C), dim3(256), 0, st,
+                          (b->prio_mask & 2) != 0, b->prio_hi, Dg, img));
       PQMC_LAUNCHED();
       gphase_end(b, g, PQMC_PHASE_SPLIT, tsp);
     }
     cudaEvent_t tf = gphase_begin(b, g);
     if (b->flush_mode == 1 && img && kd <= UM_KP) {
-      k_bflush_um<<<dim3(um_rtiles(ns) * um_ctiles(ns), C), 256, 6 * UM_HALF, st>>>(Dg, img, parity);
+      PQMC_CUDA(launch_at(k_bflush_um, dim3(um_rtiles(ns) * um_ctiles(ns), C), dim3(256), (size_t)(6 * UM_HALF), st,
+                          (b->prio_mask & 2) != 0, b->prio_hi, Dg, (const unsigned char*)img, parity));
       PQMC_LAUNCHED();
     } else {
       k_bflush<<<dim3(tiles, C), 256, 0, st>>>(Dg, parity);
@@ -1766,7 +1793,8 @@ static int slice_graph(pqmc_batch* b, int g, bool forward, int parity, pqmc_batc
   pqmc_batch::SliceGraph e{};
   std::copy(key, key + 6, e.key);
   e.kernels = n_kernels;
-  const cudaError_t ei = cudaGraphInstantiate(&e.exec, graph, 0);
+  const cudaError_t ei =
+      cudaGraphInstantiate(&e.exec, graph, b->prio_mask ? (unsigned long long)cudaGraphInstantiateFlagUseNodePriority : 0ull);
   cudaGraphDestroy(graph);
   if (ei != cudaSuccess) {
     set_error("slice graph instantiate: %s", cudaGetErrorString(ei));
@@ -2097,6 +2125,17 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     PQMC_CUDA(raise_dyn_smem(k_bflush_um, 6 * UM_HALF));
     // wrap with whole columns staged in shared memory where they fit
     // (PQMC_WRAP_COLS=0 keeps the gather form)
+    {
+      // the family step's chain of kernels (scan, split, flush) ahead of
+      // the other groups' wraps and recompute GEMMs when SMs free up: a
+      // group's scan is one CTA per chain on its sequential path
+      // (PQMC_PRIORITY=0 launches everything at the default priority)
+      const char* penv = getenv("PQMC_PRIORITY");
+      b->prio_mask = penv ? atoi(penv) & 3 : 3;
+      int lo = 0, hi = 0;
+      PQMC_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      b->prio_hi = hi;
+    }
     const char* wenv = getenv("PQMC_WRAP_COLS");
     const bool wc_on = !(wenv && atoi(wenv) == 0);
     b->wrap_cols.assign(c0->n_pf, 0);

@@ -229,6 +229,26 @@ def test_wrap_column_staging_bit_identical(monkeypatch):
         assert s0["positive_accept"] > 0
 
 
+def test_launch_priorities_bit_identical(monkeypatch):
+    """The family-step kernels launched at the highest stream priority (node
+    priorities in the slice graphs) and every kernel at the default priority:
+    priorities only change which group's CTAs the GPU dispatches first, never
+    the order of a group's own kernels, so two chain groups come out bit for
+    bit the same."""
+    ms = []
+    for i in range(16):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=180 + i)
+        ms.append((m, f, seed_words(1800 + i)))
+    monkeypatch.setenv("PQMC_PRIORITY", "0")
+    plain, _, _ = _run_batch(ms, (1, 2), graphs=True)
+    monkeypatch.setenv("PQMC_PRIORITY", "3")
+    prio, _, _ = _run_batch(ms, (1, 2), graphs=True)
+    for (f0, g0, s0), (f1, g1, s1) in zip(plain, prio):
+        assert np.array_equal(f0, f1) and np.array_equal(g0, g1)
+        assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
+        assert s0["positive_accept"] > 0
+
+
 def test_uneven_batch_matches_its_classes():
     """A mixed batch of chains of uneven L and Lt (C3-shaped, scaled down)
     splits into geometry classes that interleave on their own streams; every

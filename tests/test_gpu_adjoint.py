@@ -89,6 +89,24 @@ def test_grad_all_entries_vs_oracle_fd():
     assert np.abs(g).max() > 1e-3     # the field does move the weight
 
 
+@pytest.mark.parametrize("name,builder,kw", MODELS, ids=[m[0] for m in MODELS])
+def test_grad_vs_fp64_trace_formula(name, builder, kw):
+    """Every entry against the FP64 Green's-function trace formula
+    c Re Tr[g dE E^-1] evaluated directly on the CPU (oracle/trace_gradient.py:
+    the oracle's propagators, unstabilised dense G, no code shared with the
+    device adjoint).  Both are exact formulas for the same derivative, so the
+    tolerance is far below the finite-difference one: 1e-9 absolute plus
+    1e-7 of the largest entry (the entries are O(1e-2))."""
+    from oracle.trace_gradient import logweight_grad_trace
+    m, f = builder(ntime=20, ngroup=5, **kw)
+    ch = _chain(m, f)
+    w, g = _grad(ch, m)
+    wt, gt, _ = logweight_grad_trace(m, f, SEED_WORDS)
+    assert abs(w.real - wt) <= 1e-9 * abs(wt) + 1e-9
+    assert np.abs(gt).max() > 1e-3
+    assert np.abs(g - gt).max() <= 1e-9 + 1e-7 * np.abs(gt).max(), (name, np.abs(g - gt).max())
+
+
 def test_grad_leaves_state():
     m, f = epsocz_small(ntime=20, ngroup=5)
     ch = _chain(m, f)

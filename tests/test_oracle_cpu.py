@@ -228,3 +228,27 @@ def test_measurement_symmetries():
     assert np.allclose(kfields, fields @ m.lat.k_phase.T / nc, atol=1e-12)
     # BF_X equals the field average on the measured slice
     assert np.isclose(r[2].real, o.field()[:, m.ntime // 2 - 1].sum() / nc)
+
+
+@pytest.mark.parametrize("L", [4, 6])
+def test_k_space_matches_fft2(L):
+    """The _k observables against numpy's 2-D FFT of their real-space fields,
+    the cross-check of pprocess/check_core_data.py:47-111: with the first
+    Brillouin zone centred at Gamma (src/mod_lattice.f90:164-202) the k
+    index m holds k = 2 pi (m - floor(L/2)) / L, so the record is the
+    fftshift of the inverse FFT over the cells."""
+    m, f = epsocz_small(L=L, ntime=20, ngroup=10)
+    o = OracleChain(m, field=f, seed_words=SEED_WORDS)
+    o.init_expkv()
+    o.init_g(1)
+    r = o.sweep(1, 1, warmup=0, meas_number=0, cap=2)[0]
+    nc = m.lat.n_cell
+    fields = r[3:3 + 25 * nc].reshape(25, nc)
+    kfields = r[3 + 25 * nc:].reshape(25, nc)
+    dp = m.lat.cell_dpos
+    assert np.abs(fields).max() > 1e-3
+    for j in range(25):
+        grid = np.zeros((L, L), dtype=np.complex128)
+        grid[dp[:, 0], dp[:, 1]] = fields[j]
+        want = np.fft.fftshift(np.fft.ifft2(grid))[dp[:, 0], dp[:, 1]]
+        assert np.allclose(kfields[j], want, atol=1e-12), j

@@ -417,8 +417,9 @@ def run_mixed(args, world, rank, local):
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
             "per_launch_bytes_algorithmic": bytes_alg / max(1, flush_n),
-            "traffic_note": "ncu dram__bytes_read+write of one full-depth flush launch (profiles/traffic.json), "
-                            "scaled to the chains of one launch (chain group 0)",
+            "traffic_note": "ncu dram__bytes_read+write of one full-depth flush launch (profiles/traffic.json, "
+                            "captured on the one-CTA-per-SM form of the kernel), scaled to the chains of one launch "
+                            "(chain group 0)",
             "tensor_achieved_tflops": flops / secs / 1e12 if secs > 0 else 0.0,
             "tensor_peak_tflops": pk["bf16_tflops_sustained"],
             "kernel": ("k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "

@@ -252,3 +252,36 @@ def test_k_space_matches_fft2(L):
         grid[dp[:, 0], dp[:, 1]] = fields[j]
         want = np.fft.fftshift(np.fft.ifft2(grid))[dp[:, 0], dp[:, 1]]
         assert np.allclose(kfields[j], want, atol=1e-12), j
+
+
+def test_spin_half_gaussian_bond_model():
+    """The 4x4 bond-modulated hopping t(1 - lambda x_b) configuration with
+    spin 1/2 as ncopy = 2 (weight det^ncopy, src/mod_update.f90:104) and the
+    Gaussian proposal (sigma = 0.3, Box-Muller on two ran2 draws, then the
+    Metropolis draw :117): the weight doubles the ncopy = 1 one, a family
+    step consumes three draws per plaquette, and the err_fast invariant
+    (src/mod_evolution.f90:179-193) holds over Lt = 80."""
+    import dataclasses
+    from oracle.oracle import rng_draw
+    from pqmc_allinone_gb300 import model as M
+    m1, f = general_bond_model(L=4, ntime=80, ngroup=10, lam=0.8)
+    spec2 = dataclasses.replace(m1.spec, ncopy=2, proposal_kind=M.PROPOSAL_GAUSSIAN, jump_distance=0.3)
+    m2 = M.build_model(spec2, twist_seed=3, twist=1e-3)
+    assert m2.jump_distance == pytest.approx(0.3)
+    o1 = OracleChain(m1, field=f, seed_words=SEED_WORDS, meas=False)
+    o2 = OracleChain(m2, field=f, seed_words=SEED_WORDS, meas=False)
+    for o in (o1, o2):
+        o.init_expkv()
+        o.init_g(1)
+    assert abs(o2.state()["ln_cw"].real - 2.0 * o1.state()["ln_cw"].real) < 1e-9 * abs(o1.state()["ln_cw"].real)
+    # one family step at the first slice: 3 draws per plaquette
+    o2.update_phonon_field(1, 1)
+    _, words = rng_draw(SEED_WORDS, 3 * m2.pf[0].n_pla)
+    assert o2.state()["rng"] == words
+    o2.set_rng(SEED_WORDS)
+    o2.init_g(1)
+    for loop in range(1, 3):
+        o2.sweep(loop, 1)
+        s = o2.state()
+        assert s["err_fast_max"] <= 1e-6 + 1e-15
+    assert s["positive_accept"] > 0 and s["negative_accept"] > 0

@@ -4,7 +4,8 @@ on the CPU: its value equals the oracle's cal_new_weight_T0
 (src/mod_evolution.f90:359-408) and every entry of its gradient equals a
 central finite difference of that weight, for the three propagator forms
 (EPSOCZ closed form with a static spin-orbit term and twisted boundaries,
-EPSOC closed form under TR_weight, general expm)."""
+EPSOC closed form under TR_weight, general expm, and the latter with
+ncopy = 2)."""
 import numpy as np
 import pytest
 
@@ -12,10 +13,21 @@ from tests.helpers import SEED_WORDS, epsoc_model, epsocz_small, general_bond_mo
 
 H = 1e-6
 
+
+def spin_half_bond_model(ntime=8, ngroup=4):
+    """The bond model with spin 1/2 as ncopy = 2 (weight det^2)."""
+    import dataclasses
+    from pqmc_allinone_gb300 import model as M
+    m, f = general_bond_model(ntime=ntime, ngroup=ngroup)
+    m2 = M.build_model(dataclasses.replace(m.spec, ncopy=2), twist_seed=3, twist=1e-3)
+    return m2, f
+
+
 CASES = [
     ("epsocz_soc", epsocz_small, {"alpha": 0.3, "bc": (1.0, 1.0)}),
     ("epsoc", epsoc_model, {}),
     ("general", general_bond_model, {}),
+    ("general_ncopy2", spin_half_bond_model, {}),
 ]
 
 

@@ -25,6 +25,11 @@ slice t (the g_h of src/mod_evolution.f90:330-357 at that point of the
 string); only the plaquette's dim x dim block of g enters, because dE_p
 touches its sites alone.  A boson that several plaquettes carry collects
 every one of their terms.
+
+Parity status: pinned against the oracle's own weight (value to 1e-12, every
+gradient entry to its central finite difference, tests/test_trace_gradient_cpu.py);
+like the oracle it builds on, unpinned against reference outputs, which the
+reference does not ship.
 """
 from __future__ import annotations
 

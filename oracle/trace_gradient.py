@@ -45,17 +45,16 @@ def _dexp(o, kind: int, pf: int, pla: int, x: float, h: float = 1e-3) -> np.ndar
 
 
 def logweight_grad_trace(m, field: np.ndarray, seed_words=None):
-    """(W, grad) with grad[b, t] = dW/dx_{b,t} for the field (n_bf, ntime),
-    and the determinant det(P^H B P) seen at every (slice, family) position
-    (all equal in exact arithmetic; their spread is a check of the string)."""
+    """(W, grad, dets): the weight, grad[b, t] = dW/dx_{b,t} for the field
+    (n_bf, ntime), and slogdet(P^H B P) as seen at every (slice, family)
+    position (all equal in exact arithmetic; their spread checks the string)."""
     from oracle.oracle import OracleChain
 
     o = OracleChain(m, field=np.asarray(field, dtype=np.float64), seed_words=seed_words, meas=False)
     o.init_expkv()
-    ekv, ekv_inv = o.expkv()
+    _, ekv_inv = o.expkv()
     npf, pd, mp, nt = len(m.pf), m.pdim, m.max_pla, m.ntime
     # flat (pdim, pdim, max_pla, n_pf, ntime), column-major
-    ekv = ekv.reshape((pd, pd, mp, npf, nt), order="F")
     ekv_inv = ekv_inv.reshape((pd, pd, mp, npf, nt), order="F")
     P = np.asarray(m.slater_q, dtype=np.complex128).reshape((m.ns, m.nelec), order="F")
     d = np.asarray(m.slater_d, dtype=np.complex128)

@@ -431,8 +431,8 @@ def run_mixed(args, world, rank, local):
                            "launches of empty rounds included)",
             "flush_rounds_group0": rounds_g0,
             "peak_source": f"{pk['source']} HBM copy bandwidth; bf16 sustained for the tensor figure",
-            "dominant_by_time": "k_bscan (59% of the serialised kernel time in profiles/"
-                                "launches_mixed_14x14_lt1000_16chains.md): the sequential ratio scan, one CTA per "
+            "dominant_by_time": "k_bscan (59% of the serialised kernel time in the committed launch list of "
+                                "two 16-chain blocks): the sequential ratio scan, one CTA per "
                                 "chain, latency-bound by the Markov order (FMA pipe 33% active), neither an HBM nor "
                                 "a tensor-pipe kernel"}
     total_ms = sum(v[0] for v in phases.values())

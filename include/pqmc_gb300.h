@@ -4,8 +4,8 @@
  * Every entry point replaces one Fortran subroutine of the reference
  * (LEOMMM816/PQMC_allinone) on its local-update / B-string / measurement
  * path.  The Fortran side keeps its subroutine signatures and forwards to
- * these functions through an ISO_C_BINDING shim (the shim source is shown in
- * INTEGRATION.md).  All state the reference keeps as module globals
+ * these functions through a thin ISO_C_BINDING shim.  All state the
+ * reference keeps as module globals
  * (src/input.f90:72-96) lives on the device inside an opaque handle; the
  * host passes plain pointers and sizes.
  *
@@ -119,8 +119,9 @@ typedef struct pqmc_meas_layout {
 } pqmc_meas_layout;
 
 /* Observable slots of one measurement record (per-measurement vector,
- * like MeasurementSystem%data(:,m,b)).  Scalars first, then fields of
- * width n_cell each, each field followed by its _k transform. */
+ * like MeasurementSystem%data(:,m,b)).  Scalars first, then the r-space
+ * block of the fields (width n_cell each, in the order below), then the
+ * k-space block (the _k transform of each field, same order). */
 #define PQMC_OBS_BF_KE 0
 #define PQMC_OBS_BF_PE 1
 #define PQMC_OBS_BF_X 2
@@ -439,20 +440,25 @@ int pqmc_batch_graph_count(pqmc_batch* batch, int* n);
 /* ---- recompute without device allocation ---------------------------- */
 /* No counterpart in the reference.  g_out = R (X^H R)^-1 X^H and
  * logdet_out = log det(X^H R) (complex), i.e. cal_g_and_det_T0 without the
- * D-string and TR/ncopy terms, for callers that cannot call cudaMalloc (code
- * running under CUDA-graph stream capture, hosts that give the device to a
- * fixed memory arena, Fortran drivers bound only to this library).  All
- * pointers are DEVICE pointers: x_left and rmat are Ns x nelec complex,
- * column-major; g_out is Ns x Ns; logdet_out holds 2 doubles.  `stream` is a
- * cudaStream_t (NULL: legacy default stream); the call returns after the
- * stream has finished it.
+ * D-string and TR/ncopy terms, for callers that cannot call cudaMalloc:
+ * hosts that hand the whole device to a fixed memory arena at start-up (a
+ * further allocation would fail or fragment it) and Fortran drivers whose
+ * only CUDA binding is this library (they have no way to allocate device
+ * memory of their own).  All pointers are DEVICE pointers: x_left and rmat
+ * are Ns x nelec complex, column-major; g_out is Ns x Ns; logdet_out holds 2
+ * doubles.  `stream` is a cudaStream_t (NULL: legacy default stream); the
+ * call copies the pivot flag of its LU to the host and synchronises the
+ * stream before it returns.  On PQMC_ERR_SINGULAR (an exact zero pivot)
+ * g_out and logdet_out have been overwritten and hold no meaningful values.
  * Work space: one file-scope device array of about 3.2 MB, reserved when the
  * library loads and held by every GPU that loads it until the process exits.
  * Sizes above PQMC_NOALLOC_MAX_NS / PQMC_NOALLOC_MAX_NELEC return
- * PQMC_ERR_ARG.  Every call shares that array: calls that overlap on the GPU
- * race.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture begins. */
+ * PQMC_ERR_ARG.  Every call shares that array, which keeps the last call's
+ * contents: calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current and keeps it for the life of the process; make that first
+ * call before any stream capture begins, and do not call the entry point
+ * after cudaDeviceReset on that device (the kept address is then stale). */
 #define PQMC_NOALLOC_MAX_NS 512
 #define PQMC_NOALLOC_MAX_NELEC 256
 int pqmc_cal_g_and_det_noalloc(const double* x_left, const double* rmat, int ns, int nelec, double* g_out,

@@ -1,19 +1,22 @@
 // noalloc.cu -- pqmc_cal_g_and_det_noalloc: the Green's-function recompute
 // from stabilised factors without any device allocation.
 //
-// Some callers cannot call cudaMalloc: code that runs while a stream is being
-// captured into a CUDA graph (allocation is not a capturable operation),
-// hosts that hand the whole device to a fixed memory arena at start-up, and
-// Fortran drivers whose only CUDA binding is this C library.  For them this
-// entry point keeps its work space in one file-scope device array of fixed
-// size, reserved when the library is loaded and held by every GPU that loads
-// it until the process exits.
+// Some callers cannot call cudaMalloc: hosts that hand the whole device to a
+// fixed memory arena at start-up (any further allocation fails or fragments
+// the arena), and Fortran drivers whose only CUDA binding is this C library
+// (they have no allocator of their own to call).  For them this entry point
+// keeps its work space in one file-scope device array of fixed size,
+// reserved when the library is loaded and held by every GPU that loads it
+// until the process exits.
 //
 // Limits: ns <= PQMC_NOALLOC_MAX_NS and nelec <= PQMC_NOALLOC_MAX_NELEC; larger
 // problems are rejected with PQMC_ERR_ARG.  Every call uses the same array,
 // so calls that overlap on the GPU (two host threads, or two streams without
 // ordering between them) race on it.  The array keeps the last call's
-// contents; this routine writes every word it reads before reading it.
+// contents; this routine writes every word it reads before reading it.  The
+// call ends by copying the LU pivot flag to the host and synchronising the
+// stream; on PQMC_ERR_SINGULAR the outputs have been overwritten with
+// meaningless values.
 #include <mutex>
 #include "chain.cuh"
 #include "linalg.cuh"
@@ -34,8 +37,9 @@ std::mutex g_mu;
 void* g_addr[64] = {nullptr};
 
 // The host-side name g_noalloc_scratch is only a stand-in for the device
-// array; its device address is looked up once per device, with that device
-// current, and cached.
+// array; its device address is looked up on the first call on each device,
+// with that device current, and kept for the life of the process (a
+// cudaDeviceReset of that device leaves the kept address stale).
 int scratch_address(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

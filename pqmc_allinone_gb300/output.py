@@ -34,12 +34,13 @@ KIND_SCALAR, KIND_FIELD = 1, 2      # mod_meas.f90:7
 def device_slots(m: Model) -> dict[str, tuple[int, int]]:
     """name -> (offset, width) in a device measurement record."""
     nc = m.lat.n_cell
+    ns, nf = len(SCALAR_NAMES), len(FIELD_NAMES)
     out = {n: (i, 1) for i, n in enumerate(SCALAR_NAMES)}
-    off = len(SCALAR_NAMES)
-    for n in FIELD_NAMES:
-        out[n] = (off, nc)
-        out[n + "_k"] = (off + nc, nc)
-        off += 2 * nc
+    # r-space block of every field, then the k-space block (meas.cu
+    # k_meas_finish writes field f's transform at ns + (nf + f) * nc)
+    for f, n in enumerate(FIELD_NAMES):
+        out[n] = (ns + f * nc, nc)
+        out[n + "_k"] = (ns + (nf + f) * nc, nc)
     return out
 
 

@@ -19,3 +19,16 @@ def has_gpu() -> bool:
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+# The reference checkout, read as text or imported by CPU tests only (it is
+# not present where the GPU tests run).  PQMC_REFERENCE overrides the
+# location; tests that need it skip when it is absent.
+REFERENCE_ROOT = os.environ.get("PQMC_REFERENCE", "/root/reference")
+
+
+@pytest.fixture
+def reference_root():
+    if not os.path.isdir(REFERENCE_ROOT):
+        pytest.skip("reference checkout not present")
+    return REFERENCE_ROOT

@@ -10,7 +10,6 @@ from pqmc_allinone_gb300.rng import Ran2, seed_words
 from tests.helpers import SEED_WORDS, epsoc_model, epsocz_small, general_bond_model, rel_fro
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
-REF_NML = "/root/reference/input/model/EPSOCZ.nml"
 
 
 # ---- ran2 (src/mod_ranstate.f90) --------------------------------------
@@ -32,9 +31,9 @@ def test_ran2_seed_words():
 
 
 # ---- model set-up -------------------------------------------------------
-@pytest.mark.skipif(not os.path.exists(REF_NML), reason="reference namelist not mounted")
-def test_namelist_matches_builder():
-    spec = M.spec_from_namelist(open(REF_NML).read())
+def test_namelist_matches_builder(reference_root):
+    nml = os.path.join(reference_root, "input", "model", "EPSOCZ.nml")
+    spec = M.spec_from_namelist(open(nml).read())
     m1 = M.build_model(spec, with_slater=False)
     s2 = M.epsocz_spec(tuple(spec.lat_size), lam=spec.ep_parameter, ntime=m1.ntime, ngroup=spec.ngroup,
                        filling=spec.filling, jump_distance=spec.jump_distance, bc_phase=tuple(spec.bc_phase))

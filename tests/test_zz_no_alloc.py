@@ -1,13 +1,14 @@
-"""The allocation-free recompute entry point against the chain's own.
+"""The allocation-free recompute entry point against the chain's own and the oracle.
 
-pqmc_cal_g_and_det_noalloc serves callers that cannot call cudaMalloc: code
-running while a stream is captured into a CUDA graph, hosts that give the
-device to a fixed memory arena, Fortran drivers bound only to this C
-library.  It keeps its work space in a fixed device array inside the
-library.  This test feeds it the stabilised factors of a chain after
-init_g_T0 and checks G and the log-weight against what pqmc_init_g produced,
-on two calls in a row (the shared work space must not leak state between
-calls).  It runs last in the suite and also passes alone in a fresh process.
+pqmc_cal_g_and_det_noalloc serves callers that cannot call cudaMalloc: hosts
+that hand the whole device to a fixed memory arena at start-up, and Fortran
+drivers whose only CUDA binding is this C library.  It keeps its work space
+in a fixed device array inside the library.  This test feeds it the
+stabilised factors of a chain after init_g_T0 and checks G and the
+log-weight against what pqmc_init_g produced and G against the CPU oracle's
+init_g_T0 on the same field, on two calls in a row (the shared work space
+must not leak state between calls).  It runs last in the suite and also
+passes alone in a fresh process.
 """
 import ctypes
 
@@ -35,6 +36,11 @@ def test_noalloc_recompute_matches_init_g():
     ch.init_expkv()
     ch.init_g(1)
     g_ref = ch.g()
+    from oracle.oracle import OracleChain
+    o = OracleChain(m, field=f, seed_words=SEED_WORDS)
+    o.init_expkv()
+    o.init_g(1)
+    g_oracle = o.g()
     lncw = ch.state()["ln_cw"]
     ql, _ = ch.qd(m.nblock)          # left factor X = Q_string(nblock), L = X^H
     qr, _ = ch.qd(m.nblock - 1)      # right factor after the last stabilisation
@@ -52,6 +58,7 @@ def test_noalloc_recompute_matches_init_g():
         assert st == 0, lib.pqmc_last_error()
         g = g_d.cpu().numpy().view(np.complex128).reshape((m.ns, m.ns), order="F")
         assert rel_fro(g, g_ref) < G_TOL, call
+        assert rel_fro(g, g_oracle) < G_TOL, call
         ld = complex(*ld_d.cpu().numpy())
         assert abs((ld + sumlogd).real - lncw.real) <= 1e-9 * abs(lncw.real) + 1e-9, call
 

@@ -34,6 +34,8 @@
 #include "update_dev.cuh"
 #include "recompute_b.cuh"
 #include "df32.cuh"
+#include "tc.cuh"
+#include "exact.cuh"
 
 namespace pqmc {
 
@@ -59,12 +61,19 @@ struct BDesc {
   int rb, nrb;
   int t;         // 0-based time index of the slice in progress (k_bsettime)
   unsigned long long* nflush;   // flush rounds with work (for the roofline accounting)
+  // the round's accepted moves for the exact update (exact.cuh)
+  int* acc_site;
+  float4* acc_delta;
+  float2* acc_detf;
+  double* acc_thr;
 };
 
 __device__ __forceinline__ float2 f2(cplx a) { return make_float2((float)a.x, (float)a.y); }
 __device__ __forceinline__ float2 fm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 fa(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 fsb(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// the high words of a double-float complex (the FP32 rounding of its value)
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.x, v.y); }
 // acc + a*b in four FMAs
 __device__ __forceinline__ float2 fcfma(float2 a, float2 b, float2 acc) {
   return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y)));
@@ -202,6 +211,7 @@ __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf_first, int
     if (i == j) a = csub(a, mk(1.0));
     pre[p].delta[sl] = a;
     pre[p].deltaf[sl] = make_float2((float)a.x, (float)a.y);
+    pre[p].deltad[sl] = dg_make(a);
   }
 }
 
@@ -344,46 +354,6 @@ __device__ __forceinline__ void wf_inverse(int dim, float2* R, float2 det, int l
   __syncwarp();
 }
 
-// ---- 1-D bulk copies (TMA) global -> shared with mbarrier completion ----
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(b)), "r"(parity)
-      : "memory");
-  return ok;
-}
-// wait for the phase of parity `parity` to complete; false after ~2 s
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(b, parity))
-    if (clock64() - t0 > (4LL << 30)) return false;
-  return true;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst)),
-               "l"(src), "r"(bytes), "r"(smem_addr(b))
-               : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
-// 2-D tiled TMA load of the box at (x, y) of the tensor map into shared memory
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* b) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_addr(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(smem_addr(b))
-      : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 constexpr int SCAN_NSTAGE = 3;   // panel chunks in flight
 constexpr int SCAN_RPT = 2;      // rows per thread: Ns <= SCAN_RPT * SCAN_THREADS
@@ -426,7 +396,7 @@ __device__ __forceinline__ void scan_issue(float2* s_stage, uint64_t* s_full, co
 
 template <int DIM, int RPT>
 __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int parity, int kd, int qc,
-                                                         int* next_p) {
+                                                         int* next_p, int exact) {
   constexpr int NW = SCAN_THREADS / 32;
   __shared__ BDesc sd;
   __shared__ float2 s_R[NW][16];
@@ -714,6 +684,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     const int pa_ = s_accp[ja];
     d.field[M.bf[pa_ + M.max_pla * pf] + (size_t)M.n_bf * t] = pre[pa_].xnew;
   }
+  if (exact) {
+    // the accepted moves for the exact update: sites, Delta, the FP32 ratio
+    // and the threshold it passed (ln_cw is updated there from the exact
+    // ratios)
+    for (int e = tid; e < n_acc * dim; e += blockDim.x) d.acc_site[e] = s_site[4 * s_accp[e / dim] + e % dim];
+    for (int e = tid; e < n_acc * 16; e += blockDim.x) d.acc_delta[e] = pre[s_accp[e / 16]].deltad[e % 16];
+    for (int ja = tid; ja < n_acc; ja += blockDim.x) {
+      d.acc_detf[ja] = s_accd[ja];
+      d.acc_thr[ja] = s_thr[s_accp[ja]];
+    }
+  }
   if (warp == 0) {
     // ln_cw += log prod_j Re(R_j^ncopy) (|R_j|^2 under TR_weight), as a
     // mantissa/exponent product so long rounds cannot overflow
@@ -747,7 +728,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     if (lane == 0) {
       *d.kcount = K;
       next_p[blockIdx.x] = p;
-      if (n_acc > 0) {
+      if (n_acc > 0 && !exact) {
         const double l = (mant > 0.0) ? log(mant) + (double)ex * 0.69314718055994530942 : log(mant);
         d.sc->ln_cw = cadd(d.sc->ln_cw, mk(l));
       }
@@ -900,27 +881,6 @@ __global__ void __launch_bounds__(256) k_bflush(const BDesc* D, int parity) {
 // never written and only reach accumulator columns that are not read), so
 // the flush of a ragged tile copies and multiplies only what it needs
 // (N = 16 ncg).
-constexpr int UM_KP = 64;                    // panel columns per flush on this path (delay depth <= 64)
-constexpr int UM_IMG = 128 * 2 * UM_KP * 2;  // bytes per tile image slot (32 KB)
-
-__host__ __device__ __forceinline__ int um_rtiles(int ns) { return (ns + 127) / 128; }
-__host__ __device__ __forceinline__ int um_ctiles(int ns) { return (ns + 63) / 64; }
-__host__ __device__ __forceinline__ size_t um_chain_bytes(int ns) {
-  return (size_t)3 * (um_rtiles(ns) + um_ctiles(ns)) * UM_IMG;
-}
-// row groups of row tile t, column groups of column tile t
-__host__ __device__ __forceinline__ int um_rg(int ns, int t) {
-  const int g = (ns - 128 * t + 7) / 8;
-  return g < 16 ? g : 16;
-}
-__host__ __device__ __forceinline__ int um_cg(int ns, int t) {   // 4 or 8, so im starts at TMEM column 32 or 64
-  const int g = (ns - 64 * t + 7) / 8;
-  return g <= 4 ? 4 : 8;
-}
-// byte offset of (row, k) in a tile image of nrg row groups
-__device__ __forceinline__ int um_off(int row, int k, int nrg) {
-  return (k >> 3) * nrg * 128 + (row >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
-}
 
 // three-way BF16 split of an FP32 value
 __device__ __forceinline__ void split3b(float x, __nv_bfloat16* o) {
@@ -998,60 +958,6 @@ __global__ void __launch_bounds__(256) k_bsplit(const BDesc* D, unsigned char* i
   }
 }
 
-// shared-memory operand descriptor (no swizzle, K-major), Blackwell format
-__device__ __forceinline__ uint64_t um_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t dsc = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  dsc |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  dsc |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  dsc |= (uint64_t)1 << 46;   // descriptor version 1 (tcgen05)
-  return dsc;                 // base offset 0, layout type 0 = no swizzle
-}
-// instruction descriptor: kind::f16, D = F32, A = B = BF16, both K-major,
-// M = 128, N = n (a multiple of 16, at most 256)
-__device__ __forceinline__ uint32_t um_idesc(uint32_t n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
-}
-
-__device__ __forceinline__ void um_mma(uint32_t dtm, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtm),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void um_commit(uint64_t* mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar))
-               : "memory");
-}
-__device__ __forceinline__ void um_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void um_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-// 32 lanes x 32 consecutive FP32 columns of tensor memory into registers
-__device__ __forceinline__ void um_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
-      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-// 32 lanes x 16 consecutive FP32 columns of tensor memory into registers
-__device__ __forceinline__ void um_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 // one CTA per (128-row tile, 64-column tile, chain), two CTAs per SM; 8
 // warps: warps w and w+4 read accumulator lanes 32(w%4).. and take column
@@ -1198,13 +1104,50 @@ __global__ void __launch_bounds__(256, 2) k_bflush_um(const BDesc* D, const unsi
 // of its column items once, in FP64 rounded to FP32, into shared memory
 // (entry-major, so the threads of a warp read consecutive words).
 constexpr int WRAP_R = 32, WRAP_C = 4;
-template <int DIM>
-__global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int left, int n_items, int parity,
+
+// the wrap of one DIM x DIM block of G (rows of one cover item, columns of
+// another) in double-float: corr = (A - I)(G + G(B - I)) + G(B - I), every
+// product formed error-free, added to G.  am(a, k) and bm(k, b) read the
+// double-float (A - I) and (B - I) entries; out(a, b, v) stores entry (a, b).
+template <int DIM, typename AM, typename BM, typename OUT>
+__device__ __forceinline__ void wrap_block_df(const float4 (&gd)[DIM][DIM], int dr, int dc, AM am, BM bm, OUT out) {
+  dfc gb[DIM][DIM];   // G (B - I)
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      dfc acc = dfc_zero();
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        const float4 v = bm(k, b);
+        acc = dfc_fms(acc, dfc{df{-gd[a][k].x, -gd[a][k].z}, df{-gd[a][k].y, -gd[a][k].w}}, dfc{df{v.x, v.z}, df{v.y, v.w}});
+      }
+      gb[a][b] = acc;
+    }
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      if (a >= dr || b >= dc) continue;
+      dfc corr = gb[a][b];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        const float4 v = am(a, k);
+        const dfc x = dfc_add(dfc{df{gd[k][b].x, gd[k][b].z}, df{gd[k][b].y, gd[k][b].w}}, gb[k][b]);
+        corr = dfc_fms(corr, dfc{df{-v.x, -v.z}, df{-v.y, -v.w}}, x);
+      }
+      const dfc n = dfc_add(dfc{df{gd[a][b].x, gd[a][b].z}, df{gd[a][b].y, gd[a][b].w}}, corr);
+      out(a, b, make_float4(n.re.hi, n.im.hi, n.re.lo, n.im.lo));
+    }
+}
+
+template <int DIM, int DF>
+__global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap(const BDesc* D, int pf, int left, int n_items, int parity,
                                                const int* __restrict__ wpla, const int* __restrict__ wsites,
                                                const int* __restrict__ wdim) {
   __shared__ BDesc sd;
-  __shared__ float2 s_am[DIM * DIM][WRAP_R];   // (A - I)(a, b) of row item lr at [a + DIM b][lr]
-  __shared__ float2 s_bm[DIM * DIM][WRAP_C];
+  __shared__ float4 s_am[DIM * DIM][WRAP_R];   // (A - I)(a, b) of row item lr at [a + DIM b][lr] (double-float)
+  __shared__ float4 s_bm[DIM * DIM][WRAP_C];
   if (threadIdx.x == 0) sd = D[blockIdx.z];
   __syncthreads();
   const BDesc& d = sd;
@@ -1241,12 +1184,13 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
     const int nl = isc ? WRAP_C : WRAP_R;
     const int il = e2 % nl, ent = e2 / nl, a = ent % DIM, b = ent / DIM;
     const int item = (isc ? ic0 : ir0) + il;
-    float2 v = make_float2(0.f, 0.f);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     if (item < n_items) {
       const int p = wpla[item], dm = wdim[item];
       if (p >= 0 && a < dm && b < dm) {
         const cplx* X = (isc ? (left ? d.expkv_inv : d.expkv) : (left ? d.expkv : d.expkv_inv)) + M.kv_base(p, pf, t);
-        v = f2(csub(X[a + pd * b], mk(a == b ? 1.0 : 0.0)));
+        const cplx x = csub(X[a + pd * b], mk(a == b ? 1.0 : 0.0));
+        v = DF ? dg_make(x) : make_float4((float)x.x, (float)x.y, 0.f, 0.f);
       }
     }
     if (isc) s_bm[ent][il] = v;
@@ -1254,6 +1198,12 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
   }
   __syncthreads();
   if (!live) return;
+  if (DF) {
+    wrap_block_df<DIM>(gd, dr, dc, [&](int a, int k) { return s_am[a + DIM * k][lr]; },
+                       [&](int k, int b) { return s_bm[k + DIM * b][lc]; },
+                       [&](int a, int b, float4 v) { gout[Sr[a] + (size_t)ns * Sc[b]] = v; });
+    return;
+  }
   // corr = (A - I) (G B) + G (B - I) = (A - I) G + (A - I) G (B - I) + G (B - I)
   float2 gb[DIM][DIM];   // G (B - I)
 #pragma unroll
@@ -1262,7 +1212,7 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
     for (int a = 0; a < DIM; ++a) {
       float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) s = fa(s, fm(dg_f2(gd[a][k]), s_bm[k + DIM * b][lc]));
+      for (int k = 0; k < DIM; ++k) s = fa(s, fm(dg_f2(gd[a][k]), hi2(s_bm[k + DIM * b][lc])));
       gb[a][b] = s;
     }
 #pragma unroll
@@ -1271,7 +1221,7 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
     for (int a = 0; a < DIM; ++a) {
       float2 corr = gb[a][b];
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) corr = fa(corr, fm(s_am[a + DIM * k][lr], fa(dg_f2(gd[k][b]), gb[k][b])));
+      for (int k = 0; k < DIM; ++k) corr = fa(corr, fm(hi2(s_am[a + DIM * k][lr]), fa(dg_f2(gd[k][b]), gb[k][b])));
       if (a < dr && b < dc) gout[Sr[a] + (size_t)ns * Sc[b]] = dg_addf(gd[a][b], corr);
     }
 }
@@ -1287,21 +1237,11 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
 constexpr int WRAPC_C = 2;
 constexpr size_t WRAPC_MAX_SMEM = 200 * 1024;   // dynamic shared memory of k_bwrap_cols at most
 __host__ __device__ inline size_t wrapc_smem(int ns, int n_items, int dim) {
-  return (size_t)WRAPC_C * dim * ns * 16 + (size_t)dim * dim * (n_items + WRAPC_C) * 8 + (size_t)n_items * 6 * 4;
+  return (size_t)WRAPC_C * dim * ns * 16 + (size_t)dim * dim * (n_items + WRAPC_C) * 16 + (size_t)n_items * 6 * 4;
 }
-__device__ __forceinline__ void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_addr(ssrc)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit_wait_all() {
-  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-}
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-template <int DIM>
-__global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
+template <int DIM, int DF>
+__global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
                                                     const int* __restrict__ wpla, const int* __restrict__ wsites,
                                                     const int* __restrict__ wdim) {
   __shared__ BDesc sd;
@@ -1322,8 +1262,8 @@ __global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, i
   const int ns = M.ns, pd = M.pdim;
   const int ic0 = blockIdx.x * WRAPC_C, ncl = min(WRAPC_C, n_items - ic0);
   float4* s_col = reinterpret_cast<float4*>(wc_dyn);                              // [WRAPC_C * DIM][ns]
-  float2* s_am = reinterpret_cast<float2*>(s_col + (size_t)WRAPC_C * DIM * ns);   // [DIM * DIM][n_items]
-  float2* s_bm = s_am + (size_t)DIM * DIM * n_items;                              // [DIM * DIM][WRAPC_C]
+  float4* s_am = s_col + (size_t)WRAPC_C * DIM * ns;                              // [DIM * DIM][n_items]
+  float4* s_bm = s_am + (size_t)DIM * DIM * n_items;                              // [DIM * DIM][WRAPC_C]
   int* s_pla = reinterpret_cast<int*>(s_bm + (size_t)DIM * DIM * WRAPC_C);        // cover items: plaquette,
   int* s_dim = s_pla + n_items;                                                   // dimension and
   int* s_site = s_dim + n_items;                                                  // sites (4 per item)
@@ -1384,8 +1324,8 @@ __global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, i
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (slot[u] >= 0) s_am[slot[u]] = f2(x[u]);   // s_bm follows s_am contiguously
+    for (int u = 0; u < 4; ++u)   // s_bm follows s_am contiguously
+      if (slot[u] >= 0) s_am[slot[u]] = DF ? dg_make(x[u]) : make_float4((float)x[u].x, (float)x[u].y, 0.f, 0.f);
   }
   if (!mbar_wait_bounded(&s_bar, 0)) s_fail = 1;
   __syncthreads();
@@ -1409,6 +1349,12 @@ __global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, i
 #pragma unroll
       for (int a = 0; a < DIM; ++a)
         gd[a][b] = (a < dr && b < dc) ? col[(size_t)b * ns + Sr[a]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (DF) {
+      wrap_block_df<DIM>(gd, dr, dc, [&](int a, int k) { return s_am[(size_t)(a + DIM * k) * n_items + ir]; },
+                         [&](int k, int b) { return s_bm[(size_t)(k + DIM * b) * WRAPC_C + icl]; },
+                         [&](int a, int b, float4 v) { col[(size_t)b * ns + Sr[a]] = v; });
+      continue;
+    }
     // corr = (A - I) (G B) + G (B - I), as in k_bwrap
     float2 gb[DIM][DIM];   // G (B - I)
 #pragma unroll
@@ -1417,7 +1363,7 @@ __global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, i
       for (int a = 0; a < DIM; ++a) {
         float2 sum = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) sum = fa(sum, fm(dg_f2(gd[a][k]), s_bm[(size_t)(k + DIM * b) * WRAPC_C + icl]));
+        for (int k = 0; k < DIM; ++k) sum = fa(sum, fm(dg_f2(gd[a][k]), hi2(s_bm[(size_t)(k + DIM * b) * WRAPC_C + icl])));
         gb[a][b] = sum;
       }
 #pragma unroll
@@ -1427,7 +1373,7 @@ __global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, i
         float2 corr = gb[a][b];
 #pragma unroll
         for (int k = 0; k < DIM; ++k)
-          corr = fa(corr, fm(s_am[(size_t)(a + DIM * k) * n_items + ir], fa(dg_f2(gd[k][b]), gb[k][b])));
+          corr = fa(corr, fm(hi2(s_am[(size_t)(a + DIM * k) * n_items + ir]), fa(dg_f2(gd[k][b]), gb[k][b])));
         if (a < dr && b < dc) col[(size_t)b * ns + Sr[a]] = dg_addf(gd[a][b], corr);
       }
   }
@@ -1482,7 +1428,14 @@ struct pqmc_batch {
   int parity = 0;
   int kd = 64;            // delay depth (panel columns per flush)
   int qc = 8;             // panel columns per streamed chunk of the scan
-  int flush_mode = 1;     // 1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush
+  // 2: exact round update (exact.cuh; delay depth <= 64), 1: tcgen05 flush of
+  // the scan's FP32 panels (delay depth <= 64), 0: mma.sync flush of them
+  int flush_mode = 2;
+  pqmc::XDesc* d_xdesc = nullptr;   // per chain: the exact update's view
+  std::vector<pqmc::XDesc> h_xdesc;
+  unsigned char* d_ximg = nullptr;  // slice images of the exact update
+  unsigned char* d_acc = nullptr;   // accepted-move records of every chain
+  bool wrap_df = true;              // double-float wraps with the exact update
   // kernels launched at the device's highest stream priority (bit 0: the
   // scan, bit 1: the split and flush); slice graphs then use node priorities
   int prio_mask = 3, prio_hi = 0;
@@ -1590,6 +1543,14 @@ static int batch_refresh(pqmc_batch* b) {
   b->parity = 0;
   PQMC_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), sizeof(BDesc) * b->h_desc.size(), cudaMemcpyHostToDevice,
                             b->stream));
+  if (b->d_xdesc) {
+    for (size_t i = 0; i < b->chains.size(); ++i) {
+      b->h_xdesc[i].g = reinterpret_cast<float4*>(b->chains[i]->g);
+      b->h_xdesc[i].g_alt = reinterpret_cast<float4*>(b->chains[i]->g_alt);
+    }
+    PQMC_CUDA(cudaMemcpyAsync(b->d_xdesc, b->h_xdesc.data(), sizeof(XDesc) * b->h_xdesc.size(),
+                              cudaMemcpyHostToDevice, b->stream));
+  }
   return PQMC_OK;
 }
 
@@ -1620,28 +1581,43 @@ static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
   const BDesc* D = b->d_desc + b->g_first[g];
   cudaStream_t st = b->g_stream[g];
   const int l = left ? 1 : 0;
+  // double-float wrap with the exact round update (PQMC_WRAP_DF=0 keeps the
+  // FP32 correction there too)
+  const bool df = b->flush_mode == 2 && b->d_xdesc && b->wrap_df;
   cudaEvent_t tw = gphase_begin(b, g);
   if (pf < (int)b->wrap_cols.size() && b->wrap_cols[pf]) {
     const dim3 gc((unsigned)((w.n_items + WRAPC_C - 1) / WRAPC_C), (unsigned)C);
     const size_t sm = wrapc_smem(c0->ns, w.n_items, c0->h_pf_dim[pf]);
-    switch (c0->h_pf_dim[pf]) {
-      case 1: k_bwrap_cols<1><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
-      case 2: k_bwrap_cols<2><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
-      case 3: k_bwrap_cols<3><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
-      default: k_bwrap_cols<4><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+#define PQMC_WC(DM, F) k_bwrap_cols<DM, F><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim)
+    switch (c0->h_pf_dim[pf] + (df ? 4 : 0)) {
+      case 1: PQMC_WC(1, 0); break;
+      case 2: PQMC_WC(2, 0); break;
+      case 3: PQMC_WC(3, 0); break;
+      case 4: PQMC_WC(4, 0); break;
+      case 5: PQMC_WC(1, 1); break;
+      case 6: PQMC_WC(2, 1); break;
+      case 7: PQMC_WC(3, 1); break;
+      default: PQMC_WC(4, 1); break;
     }
+#undef PQMC_WC
     PQMC_LAUNCHED();
     gphase_end(b, g, PQMC_PHASE_WRAP, tw);
     return PQMC_OK;
   }
   const dim3 grid((unsigned)((w.n_items + WRAP_R - 1) / WRAP_R), (unsigned)((w.n_items + WRAP_C - 1) / WRAP_C),
                   (unsigned)C);
-  switch (c0->h_pf_dim[pf]) {
-    case 1: k_bwrap<1><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
-    case 2: k_bwrap<2><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
-    case 3: k_bwrap<3><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
-    default: k_bwrap<4><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim); break;
+#define PQMC_WG(DM, F) k_bwrap<DM, F><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim)
+  switch (c0->h_pf_dim[pf] + (df ? 4 : 0)) {
+    case 1: PQMC_WG(1, 0); break;
+    case 2: PQMC_WG(2, 0); break;
+    case 3: PQMC_WG(3, 0); break;
+    case 4: PQMC_WG(4, 0); break;
+    case 5: PQMC_WG(1, 1); break;
+    case 6: PQMC_WG(2, 1); break;
+    case 7: PQMC_WG(3, 1); break;
+    default: PQMC_WG(4, 1); break;
   }
+#undef PQMC_WG
   PQMC_LAUNCHED();
   gphase_end(b, g, PQMC_PHASE_WRAP, tw);
   return PQMC_OK;
@@ -1666,26 +1642,6 @@ static int bprepare(pqmc_batch* b, int g, int pf_first, int pf_step, int n_fam) 
   return PQMC_OK;
 }
 
-// a launch of k on stream st, at priority prio when use is set (the
-// attribute also marks the node when the stream is being captured)
-template <typename... P, typename... A>
-static cudaError_t launch_at(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool use, int prio,
-                             A&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  if (use) {
-    at[0].id = cudaLaunchAttributePriority;
-    at[0].val.priority = prio;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-  }
-  return cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
-}
-
 static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
   const int C = b->g_count[g], c_first = b->g_first[g];
   const BDesc* Dg = b->d_desc + c_first;
@@ -1695,7 +1651,8 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
   const int npla = c0->h_pf_npla[pf], dim = c0->h_pf_dim[pf];
   if (!b->slice_prep) PQMC_TRY(bprepare(b, g, pf, 1, 1));
   PQMC_CUDA(cudaMemsetAsync(next, 0, sizeof(int) * C, st));
-  const int kd = std::max(dim, std::min(b->kd, b->h_desc[0].kmax));
+  const bool exact = b->flush_mode == 2 && b->d_xdesc;
+  const int kd = std::max(dim, std::min(std::min(b->kd, b->h_desc[0].kmax), exact ? UM_KP : SCAN_KSTAGE));
   // enough rounds for the worst case (every proposal accepted)
   const int rounds = (npla * dim + (kd / dim) * dim - 1) / ((kd / dim) * dim);
   const int tiles = ((c0->ns + FB_M - 1) / FB_M) * ((c0->ns + FB_N - 1) / FB_N);
@@ -1708,7 +1665,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     const bool one = ns <= SCAN_THREADS;
 #define PQMC_SCAN(DM, R)                                                                                         \
   PQMC_CUDA(launch_at(k_bscan<DM, R>, dim3(C), dim3(SCAN_THREADS), smem, st, (b->prio_mask & 1) != 0, b->prio_hi, Dg, \
-                      pf, parity, kd, b->qc, next))
+                      pf, parity, kd, b->qc, next, exact ? 1 : 0))
     switch (dim) {
       case 1: if (one) PQMC_SCAN(1, 1); else PQMC_SCAN(1, 2); break;
       case 2: if (one) PQMC_SCAN(2, 1); else PQMC_SCAN(2, 2); break;
@@ -1726,8 +1683,15 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
       PQMC_LAUNCHED();
       gphase_end(b, g, PQMC_PHASE_SPLIT, tsp);
     }
+    if (exact) {   // double-float core and operand slices (timed as the split phase)
+      cudaEvent_t tsp = gphase_begin(b, g);
+      PQMC_TRY(exact_core(b->d_xdesc + c_first, C, ns, dim, parity, st, (b->prio_mask & 2) != 0, b->prio_hi));
+      gphase_end(b, g, PQMC_PHASE_SPLIT, tsp);
+    }
     cudaEvent_t tf = gphase_begin(b, g);
-    if (b->flush_mode == 1 && img && kd <= UM_KP) {
+    if (exact) {
+      PQMC_TRY(exact_products(b->d_xdesc + c_first, C, ns, parity, st, (b->prio_mask & 2) != 0, b->prio_hi));
+    } else if (b->flush_mode == 1 && img && kd <= UM_KP) {
       PQMC_CUDA(launch_at(k_bflush_um, dim3(um_rtiles(ns) * um_ctiles(ns), C), dim3(256), (size_t)(6 * UM_HALF), st,
                           (b->prio_mask & 2) != 0, b->prio_hi, Dg, (const unsigned char*)img, parity));
       PQMC_LAUNCHED();
@@ -2136,6 +2100,8 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       PQMC_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
       b->prio_hi = hi;
     }
+    const char* denv = getenv("PQMC_WRAP_DF");
+    b->wrap_df = !(denv && atoi(denv) == 0);
     const char* wenv = getenv("PQMC_WRAP_COLS");
     const bool wc_on = !(wenv && atoi(wenv) == 0);
     b->wrap_cols.assign(c0->n_pf, 0);
@@ -2145,10 +2111,10 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       if (dim < 1 || dim > 4 || sm > WRAPC_MAX_SMEM) continue;
       cudaError_t e;
       switch (dim) {
-        case 1: e = raise_dyn_smem(k_bwrap_cols<1>, (int)sm); break;
-        case 2: e = raise_dyn_smem(k_bwrap_cols<2>, (int)sm); break;
-        case 3: e = raise_dyn_smem(k_bwrap_cols<3>, (int)sm); break;
-        default: e = raise_dyn_smem(k_bwrap_cols<4>, (int)sm); break;
+        case 1: e = raise_dyn_smem(k_bwrap_cols<1, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<1, 1>, (int)sm); break;
+        case 2: e = raise_dyn_smem(k_bwrap_cols<2, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<2, 1>, (int)sm); break;
+        case 3: e = raise_dyn_smem(k_bwrap_cols<3, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<3, 1>, (int)sm); break;
+        default: e = raise_dyn_smem(k_bwrap_cols<4, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<4, 1>, (int)sm); break;
       }
       PQMC_CUDA(e);
       b->wrap_cols[f] = 1;
@@ -2193,6 +2159,45 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   PQMC_CUDA(cudaMalloc((void**)&b->d_nflush, sizeof(unsigned long long) * n_chains));
   PQMC_CUDA(cudaMemset(b->d_nflush, 0, sizeof(unsigned long long) * n_chains));
   for (int i = 0; i < n_chains; ++i) b->h_desc[i].nflush = b->d_nflush + i;
+  if (precision == PQMC_PREC_MIXED) {
+    // the exact round update: accepted-move records and slice images per
+    // chain (images zero outside the rows and columns of G)
+    PQMC_TRY(exact_setup());
+    const size_t acc_b = (size_t)UM_KP * (sizeof(int) + 16 * sizeof(float4) + sizeof(float2) + sizeof(double));
+    const size_t xib = oz_chain_bytes(c0->ns);
+    PQMC_CUDA(cudaMalloc((void**)&b->d_acc, acc_b * n_chains));
+    PQMC_CUDA(cudaMalloc((void**)&b->d_ximg, xib * n_chains));
+    PQMC_CUDA(cudaMemset(b->d_ximg, 0, xib * n_chains));
+    b->h_xdesc.resize(n_chains);
+    for (int i = 0; i < n_chains; ++i) {
+      pqmc_chain* c = b->chains[i];
+      BDesc& h = b->h_desc[i];
+      unsigned char* a = b->d_acc + acc_b * i;   // float4 and double parts first (alignment)
+      h.acc_delta = reinterpret_cast<float4*>(a);
+      h.acc_thr = reinterpret_cast<double*>(a + (size_t)UM_KP * 16 * sizeof(float4));
+      h.acc_detf = reinterpret_cast<float2*>(a + (size_t)UM_KP * (16 * sizeof(float4) + sizeof(double)));
+      h.acc_site = reinterpret_cast<int*>(a + (size_t)UM_KP * (16 * sizeof(float4) + sizeof(double) + sizeof(float2)));
+      XDesc& x = b->h_xdesc[i];
+      memset(&x, 0, sizeof(x));
+      x.g = reinterpret_cast<float4*>(c->g);
+      x.g_alt = reinterpret_cast<float4*>(c->g_alt);
+      x.ns = c->ns;
+      x.ncopy = c->M.ncopy;
+      x.tr_weight = c->M.tr_weight;
+      x.kmax = UM_KP;
+      x.kcount = h.kcount;
+      x.acc_site = h.acc_site;
+      x.acc_delta = h.acc_delta;
+      x.acc_detf = h.acc_detf;
+      x.acc_thr = h.acc_thr;
+      x.img = b->d_ximg + xib * i;
+      x.sc = c->sc;
+      x.err = b->d_err;
+      x.nflush = b->d_nflush + i;
+    }
+    PQMC_CUDA(cudaMalloc((void**)&b->d_xdesc, sizeof(XDesc) * n_chains));
+    PQMC_CUDA(cudaMemcpy(b->d_xdesc, b->h_xdesc.data(), sizeof(XDesc) * n_chains, cudaMemcpyHostToDevice));
+  }
   PQMC_CUDA(cudaMalloc((void**)&b->d_desc, sizeof(BDesc) * n_chains));
   PQMC_CUDA(cudaMalloc((void**)&b->d_next, sizeof(int) * n_chains));
   // chain groups: PQMC_BATCH_GROUPS (1..16) when set, else one per 8 chains
@@ -2253,6 +2258,9 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
   if (b->d_img) cudaFree(b->d_img);
+  if (b->d_xdesc) cudaFree(b->d_xdesc);
+  if (b->d_ximg) cudaFree(b->d_ximg);
+  if (b->d_acc) cudaFree(b->d_acc);
   if (b->d_tmaps) cudaFree(b->d_tmaps);
   for (int g = 1; g < pqmc_batch::MAX_GROUPS; ++g)
     if (b->g_stream[g]) {
@@ -2268,7 +2276,10 @@ int pqmc_batch_destroy(pqmc_batch* b) {
 }
 
 int pqmc_batch_set_flush(pqmc_batch* b, int mode) {
-  if (!b || (mode != 0 && mode != 1)) { set_error("batch_set_flush: mode 0 (mma.sync) or 1 (tcgen05)"); return PQMC_ERR_ARG; }
+  if (!b || mode < 0 || mode > 2) {
+    set_error("batch_set_flush: mode 0 (mma.sync), 1 (tcgen05) or 2 (exact round update)");
+    return PQMC_ERR_ARG;
+  }
   for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_flush(p, mode));
   b->flush_mode = mode;
   return PQMC_OK;
@@ -2438,6 +2449,21 @@ int pqmc_batch_states(pqmc_batch* b, pqmc_state* out) {
   return PQMC_OK;
 }
 
+int pqmc_batch_exact_stats(pqmc_batch* b, double* ratio_err, long long* flips) {
+  if (!b || !ratio_err || !flips) { set_error("batch_exact_stats: null argument"); return PQMC_ERR_ARG; }
+  const size_t n = b->chains.size();
+  if (!b->h_states) PQMC_CUDA(cudaMallocHost((void**)&b->h_states, sizeof(DevScalars) * n));
+  for (size_t i = 0; i < n; ++i)
+    PQMC_CUDA(cudaMemcpyAsync(b->h_states + i, b->chains[i]->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost,
+                              b->chains[i]->stream));
+  for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
+  for (size_t i = 0; i < n; ++i) {
+    ratio_err[i] = b->h_states[i].err_ratio_max;
+    flips[i] = b->h_states[i].n_flip;
+  }
+  return PQMC_OK;
+}
+
 int pqmc_batch_classes(pqmc_batch* b, int* n) {
   if (!b || !n) { set_error("batch_classes: null argument"); return PQMC_ERR_ARG; }
   *n = b->parts.empty() ? 1 : (int)b->parts.size();
@@ -2504,6 +2530,10 @@ int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, con
   for (int i = 0; i < n_candidates && st == PQMC_OK; ++i) {
     const int kd = candidates[i];
     if (kd < 1 || kd > SCAN_KSTAGE) { st = PQMC_ERR_ARG; set_error("batch_autotune: depth %d out of range", kd); break; }
+    if (b->flush_mode == 2 && kd > UM_KP) {   // the exact update takes at most UM_KP columns
+      if (ms_out) ms_out[i] = -1.0;
+      continue;
+    }
     b->kd = kd;
     const int n = std::min(n_slices, nt - tc + 1);
     cudaEventRecord(e0, b->stream);
@@ -2523,7 +2553,7 @@ int pqmc_batch_autotune(pqmc_batch* b, int loop, int first_tc, int n_slices, con
   b->graphs = graphs;
   if (st != PQMC_OK) return st;
   b->kd = best_kd;
-  b->flush_mode = best_kd <= UM_KP ? 1 : 0;
+  if (b->flush_mode != 2) b->flush_mode = best_kd <= UM_KP ? 1 : 0;
   *best = best_kd;
   return PQMC_OK;
 }

@@ -25,6 +25,11 @@ struct DevScalars {
   int lu_info;
   int status;
   int pad;
+  // exact round update of the mixed batch: largest relative error of the
+  // scan's FP32 ratio det R against the double-float one, and the accepted
+  // moves whose double-float ratio is below the Metropolis threshold
+  double err_ratio_max;
+  long long n_flip;
 };
 
 // Control record the proposer publishes at every grid barrier of the update
@@ -45,6 +50,7 @@ struct PlaqPre {
   cplx enew[16];    // expKV(new)
   cplx einv[16];    // expKV_inv(new)
   float2 deltaf[16];// Delta rounded to FP32 for the fast test
+  float4 deltad[16];// Delta in double-float {re_hi, im_hi, re_lo, im_lo} (mixed batch)
   double dE;        // -dtau * (E_new - E_old)
   double xnew;
   double r;         // acceptance draw rands()

@@ -1,0 +1,749 @@
+// exact.cu -- the exact round update (see exact.cuh): G <- G + G(:,S) M Z
+// with M = Delta_S (I + G(S,S) Delta_S)^-1 and Z = E_S - G(S,:), from the
+// double-float G the round started from.
+#include <cuda_bf16.h>
+#include <string.h>
+#include <vector>
+#include "df32.cuh"
+#include "exact.cuh"
+
+namespace pqmc {
+
+// ---------------------------------------------------------------------------
+// Ozaki slices.  A row (column) whose entries have magnitude below 2^e is
+// cut into OZ_S pieces on the grids 2^(e-8), 2^(e-16), ...: piece s is an
+// integer of at most 256 (129 after the first) times 2^(e-8(s+1)), exact in
+// BF16.  Two pieces multiply exactly, and the products of one level (i + j)
+// of pieces share a grid, so up to 128 of them (the real inner dimension of
+// a flush) sum exactly in FP32: |sum| < 2^24 grid units.
+__device__ __forceinline__ int oz_exp(float vmax) {
+  const int b = (__float_as_int(vmax) >> 23) & 0xff;   // vmax >= 0
+  return vmax > 0.f ? max(b - 126, -80) : -80;         // vmax < 2^(b-126)
+}
+__device__ __forceinline__ float oz_pow2(int k) { return __int_as_float((127 + k) << 23); }   // |k| <= 126
+
+// the OZ_S pieces of the double-float value (h, l) for the exponent e
+__device__ __forceinline__ void oz_split(float h, float l, int e, float* q) {
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) {
+    const int sh = 8 * (s + 1) - e;
+    const float v = rintf(__fmul_rn(h, oz_pow2(sh)));
+    const float qs = __fmul_rn(v, oz_pow2(-sh));
+    q[s] = qs;
+    h = __fsub_rn(h, qs);   // exact: h and qs lie within half a grid step
+    const df n = two_sum(h, l);
+    h = n.hi;
+    l = n.lo;
+  }
+}
+__device__ __forceinline__ uint32_t oz_pack2(float a, float b) {
+  __nv_bfloat162 t = __floats2bfloat162_rn(a, b);   // a at the lower address
+  return *reinterpret_cast<uint32_t*>(&t);
+}
+__device__ __forceinline__ uint4 oz_pack8(const float* v) {
+  return make_uint4(oz_pack2(v[0], v[1]), oz_pack2(v[2], v[3]), oz_pack2(v[4], v[5]), oz_pack2(v[6], v[7]));
+}
+// three accumulator levels (exact, exact, rounded) combined in double-float
+__device__ __forceinline__ df oz_combine(float l0, float l1, float l2) {
+  const df s = two_sum(l0, l1);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, l2));
+}
+
+// double-float complex helpers
+__device__ __forceinline__ dfc dg_dfc(float4 g) { return dfc{df{g.x, g.z}, df{g.y, g.w}}; }
+__device__ __forceinline__ float4 dfc_dg(dfc a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
+// acc + a*b, one renormalisation per component
+__device__ __forceinline__ dfc dfc_mac(dfc acc, dfc a, dfc b) {
+  return dfc_fms(acc, dfc{df_neg(a.re), df_neg(a.im)}, b);
+}
+// 1/a: conj(a) / |a|^2 with the reciprocal refined by one Newton step
+__device__ __forceinline__ dfc dfc_inv(dfc a) {
+  const df n = df_add(df_mul(a.re, a.re), df_mul(a.im, a.im));
+  const float r0 = __frcp_rn(n.hi);
+  const df e = df_sub(df{1.0f, 0.0f}, df_mulf(n, r0));   // 1 - n r0
+  const df r = df_add(df{r0, 0.0f}, df_mulf(e, r0));
+  return dfc{df_mul(a.re, r), df_neg(df_mul(a.im, r))};
+}
+
+// ---------------------------------------------------------------------------
+// k_xcore: CTA 0 of each chain inverts W = I + G(S,S) Delta_S by
+// Gauss-Jordan in double-float, forms M = Delta_S W^-1, writes the slice
+// images of M (the B operand of X = G(:,S) M) and updates ln_cw from the
+// exact ratios; CTAs 1..n_a cut the rows of G(:,S) (the A operand), the
+// rest cut the columns of Z = E_S - G(S,:) (the B operand of the flush),
+// one warp per column.
+constexpr int XC_THREADS = 512;
+constexpr int XC_LD = UM_KP;   // leading dimension of W in shared memory
+constexpr size_t XC_SMEM = sizeof(float4) * ((size_t)XC_LD * XC_LD + 16 * UM_KP + 3 * UM_KP) + sizeof(int) * 2 * UM_KP;
+
+__device__ __forceinline__ void xc_write_b1(const XDesc& d, const float4* W, int K, int tid) {
+  // M is W (rows: inner k, columns: output column c of X); column exponents
+  __shared__ int s_ce[UM_KP];
+  if (tid < UM_KP) {
+    float m = 0.f;
+    if (tid < K)
+      for (int k = 0; k < K; ++k) {
+        const float4 v = W[k * XC_LD + tid];
+        m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+      }
+    s_ce[tid] = oz_exp(m);
+  }
+  __syncthreads();
+  const int K16 = (K + 15) & ~15, KG = K16 / 8;
+  const int ns = d.ns;
+  for (int it = tid; it < UM_KP * KG; it += XC_THREADS) {
+    const int c = it % UM_KP, kg = it / UM_KP;
+    float rs[OZ_S][8], is[OZ_S][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = kg * 8 + u;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (c < K && k < K) v = W[k * XC_LD + c];
+      float qr[OZ_S], qi[OZ_S];
+      oz_split(v.x, v.z, s_ce[c], qr);
+      oz_split(v.y, v.w, s_ce[c], qi);
+#pragma unroll
+      for (int s = 0; s < OZ_S; ++s) {
+        rs[s][u] = qr[s];
+        is[s][u] = qi[s];
+      }
+    }
+    // B' re row c = [Mr | -Mi], im row 64 + c = [Mi | Mr]  (ncg = 8, 16 row groups)
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) {
+      unsigned char* im = d.img + (size_t)oz_slot_b1(ns, s) * UM_IMG;
+      float ni[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) ni[u] = -is[s][u];
+      *reinterpret_cast<uint4*>(im + um_off(c, kg * 8, 16)) = oz_pack8(rs[s]);
+      *reinterpret_cast<uint4*>(im + um_off(c, UM_KP + kg * 8, 16)) = oz_pack8(ni);
+      *reinterpret_cast<uint4*>(im + um_off(64 + c, kg * 8, 16)) = oz_pack8(is[s]);
+      *reinterpret_cast<uint4*>(im + um_off(64 + c, UM_KP + kg * 8, 16)) = oz_pack8(rs[s]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(XC_THREADS) k_xcore(const XDesc* X, int dim, int parity, int n_a) {
+  __shared__ XDesc sd;
+  __shared__ dfc s_inv;
+  __shared__ int s_fail;
+  extern __shared__ __align__(16) unsigned char xc_dyn[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    sd = X[blockIdx.y];
+    s_fail = 0;
+  }
+  __syncthreads();
+  const XDesc& d = sd;
+  const int K = *d.kcount;
+  if (K == 0) return;
+  const int ns = d.ns;
+  const float4* G = parity ? d.g_alt : d.g;
+  const int K16 = (K + 15) & ~15;
+  if (blockIdx.x == 0) {
+    // ---- W = I + G(S,S) Delta_S, inverted in place -------------------------
+    float4* W = reinterpret_cast<float4*>(xc_dyn);              // [K][XC_LD], row i at W + i*XC_LD
+    float4* s_dl = W + (size_t)XC_LD * XC_LD;                    // [n_acc][16] Delta blocks
+    float4* s_row = s_dl + 16 * UM_KP;                           // pivot row (before scaling)
+    float4* s_col = s_row + UM_KP;                               // pivot column
+    float4* s_det = s_col + UM_KP;                               // det of each block (double-float complex)
+    int* s_site = reinterpret_cast<int*>(s_det + UM_KP);
+    int* s_perm = s_site + UM_KP;
+    const int nb = K / dim;
+    for (int k = tid; k < K; k += XC_THREADS) s_site[k] = d.acc_site[k];
+    for (int e = tid; e < nb * 16; e += XC_THREADS) s_dl[e] = d.acc_delta[e];
+    for (int b = tid; b < nb; b += XC_THREADS) s_det[b] = make_float4(1.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    // (i, column block jb): the dim entries W(i, jb*dim + jj)
+    for (int it = tid; it < K * nb; it += XC_THREADS) {
+      const int i = it % K, jb = it / K;
+      dfc gs[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        if (m < dim) gs[m] = dg_dfc(G[s_site[i] + (size_t)ns * s_site[jb * dim + m]]);
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) {
+        if (jj >= dim) break;
+        const int j = jb * dim + jj;
+        dfc a = dfc{df{i == j ? 1.f : 0.f, 0.f}, df{0.f, 0.f}};
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+          if (m < dim) a = dfc_mac(a, gs[m], dg_dfc(s_dl[jb * 16 + m + dim * jj]));
+        W[i * XC_LD + j] = dfc_dg(a);
+      }
+    }
+    __syncthreads();
+    // Gauss-Jordan, pivots searched within the pivot's block (the block
+    // pivots are the sequential ratio matrices R_j)
+    const int ri = tid / 8, cg = tid % 8;   // row ri, columns cg, cg + 8, ...
+    for (int k = 0; k < K; ++k) {
+      if (warp == 0) {
+        int p = k;
+        if (lane == 0) {
+          const int end = (k / dim + 1) * dim;
+          float best = -1.f;
+          for (int r = k; r < end; ++r) {
+            const float4 v = W[r * XC_LD + k];
+            const float a = fabsf(v.x) + fabsf(v.y);
+            if (a > best) { best = a; p = r; }
+          }
+          s_perm[k] = p;
+        }
+        p = __shfl_sync(0xffffffffu, p, 0);
+        if (p != k)
+          for (int j = lane; j < K; j += 32) {
+            const float4 t = W[k * XC_LD + j];
+            W[k * XC_LD + j] = W[p * XC_LD + j];
+            W[p * XC_LD + j] = t;
+          }
+        __syncwarp();
+        for (int j = lane; j < K; j += 32) {
+          s_row[j] = W[k * XC_LD + j];
+          s_col[j] = W[j * XC_LD + k];
+        }
+        if (lane == 0) {
+          const dfc piv = dg_dfc(W[k * XC_LD + k]);
+          if (piv.re.hi == 0.f && piv.im.hi == 0.f) {
+            s_fail = 1;
+            s_inv = dfc_zero();
+          } else {
+            s_inv = dfc_inv(piv);
+          }
+          const int b = k / dim;
+          dfc dt = dfc_mul(dg_dfc(s_det[b]), piv);
+          if (p != k) dt = dfc{df_neg(dt.re), df_neg(dt.im)};
+          s_det[b] = dfc_dg(dt);
+        }
+      }
+      __syncthreads();
+      if (ri < K) {
+        const dfc inv = s_inv;
+        if (ri == k) {
+          for (int j = cg; j < K; j += 8)
+            W[k * XC_LD + j] = j == k ? dfc_dg(inv) : dfc_dg(dfc_mul(dg_dfc(s_row[j]), inv));
+        } else {
+          const dfc f = dfc_mul(dg_dfc(s_col[ri]), inv);
+          for (int j = cg; j < K; j += 8) {
+            if (j == k) W[ri * XC_LD + k] = dfc_dg(dfc{df_neg(f.re), df_neg(f.im)});
+            else W[ri * XC_LD + j] = dfc_dg(dfc_fms(dg_dfc(W[ri * XC_LD + j]), f, dg_dfc(s_row[j])));
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // undo the row interchanges on the columns of the inverse
+    for (int k = K - 1; k >= 0; --k) {
+      const int p = s_perm[k];
+      if (p != k) {   // uniform
+        for (int i = tid; i < K; i += XC_THREADS) {
+          const float4 t = W[i * XC_LD + k];
+          W[i * XC_LD + k] = W[i * XC_LD + p];
+          W[i * XC_LD + p] = t;
+        }
+        __syncthreads();
+      }
+    }
+    // M = Delta_S W^-1, block row by block row in place
+    for (int it = tid; it < nb * K; it += XC_THREADS) {
+      const int jb = it / K, c = it % K;
+      dfc w[4], m[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+        if (a < dim) w[a] = dg_dfc(W[(jb * dim + a) * XC_LD + c]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        if (a >= dim) break;
+        m[a] = dfc_zero();
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          if (b < dim) m[a] = dfc_mac(m[a], dg_dfc(s_dl[jb * 16 + a + dim * b]), w[b]);
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+        if (a < dim) W[(jb * dim + a) * XC_LD + c] = dfc_dg(m[a]);
+    }
+    __syncthreads();
+    xc_write_b1(d, W, K, tid);
+    // ln_cw += sum_j log Re(R_j^ncopy) (|R_j|^2 under TR_weight), the
+    // weight update of src/mod_update.f90:102-104,153 with the exact ratios;
+    // the scan's FP32 determinants are compared with them
+    if (warp == 0) {
+      double lsum = 0.0, rel = 0.0;
+      int flips = 0;
+      for (int b = lane; b < nb; b += 32) {
+        const dfc dt = dg_dfc(s_det[b]);
+        const double dr = (double)dt.re.hi + (double)dt.re.lo, di = (double)dt.im.hi + (double)dt.im.lo;
+        double rr = dr, ri2 = di;
+        if (d.tr_weight) { rr = dr * dr + di * di; ri2 = 0.0; }
+        double ar = 1.0, ai = 0.0;
+        for (int c = 0; c < d.ncopy; ++c) {
+          const double tr = ar * rr - ai * ri2;
+          ai = ar * ri2 + ai * rr;
+          ar = tr;
+        }
+        lsum += log(ar);
+        const float2 f = d.acc_detf[b];
+        const double m2 = dr * dr + di * di;
+        const double ex = sqrt(((double)f.x - dr) * ((double)f.x - dr) + ((double)f.y - di) * ((double)f.y - di));
+        rel = fmax(rel, m2 > 0.0 ? ex / sqrt(m2) : 0.0);
+        if (m2 < d.acc_thr[b]) ++flips;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+        rel = fmax(rel, __shfl_down_sync(0xffffffffu, rel, o));
+        flips += __shfl_down_sync(0xffffffffu, flips, o);
+      }
+      if (lane == 0) {
+        d.sc->ln_cw = cadd(d.sc->ln_cw, mk(lsum));
+        d.sc->err_ratio_max = fmax(d.sc->err_ratio_max, rel);
+        d.sc->n_flip += flips;
+        if (s_fail) {
+          d.sc->status = PQMC_ERR_SINGULAR;
+          atomicExch(d.err, PQMC_ERR_SINGULAR);
+        }
+      }
+    }
+    return;
+  }
+  if ((int)blockIdx.x <= n_a) {
+    // ---- rows of G(:,S): A operand of X = G(:,S) M ------------------------
+    const int r = ((int)blockIdx.x - 1) * XC_THREADS + tid;
+    if (r >= ns) return;
+    const int* S = d.acc_site;
+    float m = 0.f;
+    for (int k = 0; k < K; ++k) {
+      const float4 v = G[r + (size_t)ns * S[k]];
+      m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+    const int e = oz_exp(m);
+    const int t = r / 128, row = r % 128, nrg = um_rg(ns, t);
+    for (int kg = 0; kg < K16 / 8; ++kg) {
+      float rs[OZ_S][8], is[OZ_S][8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = kg * 8 + u;
+        const float4 v = k < K ? G[r + (size_t)ns * S[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float qr[OZ_S], qi[OZ_S];
+        oz_split(v.x, v.z, e, qr);
+        oz_split(v.y, v.w, e, qi);
+#pragma unroll
+        for (int s = 0; s < OZ_S; ++s) {
+          rs[s][u] = qr[s];
+          is[s][u] = qi[s];
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < OZ_S; ++s) {   // A' row = [Gr | Gi]
+        unsigned char* im = d.img + (size_t)oz_slot_a1(ns, t, s) * UM_IMG;
+        *reinterpret_cast<uint4*>(im + um_off(row, kg * 8, nrg)) = oz_pack8(rs[s]);
+        *reinterpret_cast<uint4*>(im + um_off(row, UM_KP + kg * 8, nrg)) = oz_pack8(is[s]);
+      }
+    }
+    return;
+  }
+  // ---- columns of Z = E_S - G(S,:): B operand of the flush, a warp each ----
+  const int c = ((int)blockIdx.x - 1 - n_a) * (XC_THREADS / 32) + warp;
+  if (c >= ns) return;
+  dfc z[2];
+  float m = 0.f;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = lane + 32 * h;
+    z[h] = dfc_zero();
+    if (k < K) {
+      const int sk = d.acc_site[k];
+      const dfc g = dg_dfc(G[sk + (size_t)ns * c]);
+      z[h] = dfc{sk == c ? df_sub(df{1.f, 0.f}, g.re) : df_neg(g.re), df_neg(g.im)};
+      m = fmaxf(m, fmaxf(fabsf(z[h].re.hi), fabsf(z[h].im.hi)));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const int e = oz_exp(m);
+  const int tj = c / 64, cc = c % 64, ncg = um_cg(ns, tj), nrg = 2 * ncg;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = lane + 32 * h;
+    if (k >= K16) break;
+    float qr[OZ_S], qi[OZ_S];
+    oz_split(z[h].re.hi, z[h].re.lo, e, qr);
+    oz_split(z[h].im.hi, z[h].im.lo, e, qi);
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) {
+      // B' re row cc = [Zr | -Zi], im row 8 ncg + cc = [Zi | Zr]
+      unsigned char* im = d.img + (size_t)oz_slot_b2(ns, tj, s) * UM_IMG;
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(cc, k, nrg)) = __float2bfloat16_rn(qr[s]);
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(cc, UM_KP + k, nrg)) = __float2bfloat16_rn(-qi[s]);
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, k, nrg)) = __float2bfloat16_rn(qi[s]);
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, UM_KP + k, nrg)) = __float2bfloat16_rn(qr[s]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_xgemm: one CTA per output tile, one CTA per SM (160 KB of images, 384
+// tensor-memory columns).  Thread 0 streams the OZ_S A and OZ_S B half-images
+// of a K half through shared memory and issues the products of slice pairs
+// (i, j) with i + j < OZ_S into three FP32 accumulators: level 0 and level
+// 1 (exact), levels 2.. (rounded at 2^-40 of the result).  MODE 0: X = G(:,S)
+// M over a 128-row tile, written as the slice images of the flush's A
+// operand (row exponents from the tile itself); MODE 1: the flush G += X Z
+// over a 128 x 64 tile of G.
+constexpr int XG_SMEM = 2 * OZ_S * (UM_IMG / 2);
+
+__device__ __forceinline__ void um_ld16_nw(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void um_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// the three levels of 16 re and 16 im columns from accumulator column col
+__device__ __forceinline__ void xg_load(uint32_t tbase, int col, int im_off, float (*re)[16], float (*im)[16]) {
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    um_ld16_nw(tbase + l * 128 + col, re[l]);
+    um_ld16_nw(tbase + l * 128 + im_off + col, im[l]);
+  }
+  um_wait_ld();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256, 1) k_xgemm(const XDesc* X, int parity) {
+  __shared__ XDesc sd;
+  __shared__ __align__(8) uint64_t s_load[2], s_mma[2];
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_fail, s_last;
+  __shared__ float s_rmax[2][128];
+  extern __shared__ __align__(1024) unsigned char xg_dyn[];   // OZ_S A half-images, then OZ_S B half-images
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    sd = X[blockIdx.y];
+    s_fail = 0;
+    s_last = -1;
+    for (int h = 0; h < 2; ++h) {
+      mbar_init(&s_load[h], 1);
+      mbar_init(&s_mma[h], 1);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const XDesc& d = sd;
+  const int K = *d.kcount;
+  if (K == 0) return;   // uniform: no tensor memory taken
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_addr(&s_taddr))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  um_fence_before();
+  __syncthreads();
+  um_fence_after();
+  const uint32_t taddr = s_taddr;
+  const int ns = d.ns, RT = um_rtiles(ns);
+  const int ti = MODE == 0 ? (int)blockIdx.x : (int)blockIdx.x % RT;
+  const int tj = MODE == 0 ? 0 : (int)blockIdx.x / RT;
+  const int nrg_a = um_rg(ns, ti);
+  const int ncg = MODE == 0 ? 8 : um_cg(ns, tj), nrg_b = 2 * ncg;
+  const int K16 = (K + 15) & ~15;
+  if (tid == 0) {
+    if (MODE == 1 && blockIdx.x == 0) atomicAdd(d.nflush, 1ull);
+    const uint32_t ka = (uint32_t)nrg_a * 128, kb = (uint32_t)nrg_b * 128;   // bytes per K group of 8
+    const uint32_t part_a = (uint32_t)(K16 / 8) * ka, part_b = (uint32_t)(K16 / 8) * kb;
+    const uint32_t h2a = (uint32_t)(UM_KP / 8) * ka, h2b = (uint32_t)(UM_KP / 8) * kb;
+    const uint32_t base = smem_addr(xg_dyn), idesc = um_idesc(16u * (uint32_t)ncg);
+    constexpr uint32_t HALF = UM_IMG / 2;
+    uint32_t started = 0;
+    for (int half = 0; half < 2; ++half) {
+      if (half == 1) {   // the products of half 0 have read the buffer
+        if (!mbar_wait_bounded(&s_mma[0], 0)) {
+          s_fail = 1;
+          break;
+        }
+        um_fence_after();
+      }
+      mbar_arrive_tx(&s_load[half], (uint32_t)OZ_S * (part_a + part_b));
+      for (int s = 0; s < OZ_S; ++s) {
+        const int sa = MODE == 0 ? oz_slot_a1(ns, ti, s) : oz_slot_a2(ns, ti, s);
+        const int sb = MODE == 0 ? oz_slot_b1(ns, s) : oz_slot_b2(ns, tj, s);
+        bulk_g2s(xg_dyn + (size_t)s * HALF, d.img + (size_t)sa * UM_IMG + half * h2a, part_a, &s_load[half]);
+        bulk_g2s(xg_dyn + (size_t)(OZ_S + s) * HALF, d.img + (size_t)sb * UM_IMG + half * h2b, part_b, &s_load[half]);
+      }
+      if (!mbar_wait_bounded(&s_load[half], 0)) {
+        s_fail = 1;
+        mbar_wait_bounded(&s_load[half], 0);   // a second bounded wait for the copies in flight
+        break;
+      }
+      um_fence_after();
+      for (int i = 0; i < OZ_S; ++i)
+        for (int j = 0; i + j < OZ_S; ++j) {
+          const int l = min(i + j, 2);
+          for (int kk = 0; kk < K16 / 16; ++kk) {
+            const uint64_t ad = um_desc(base + i * HALF + kk * 2 * ka, ka, 128);
+            const uint64_t bd = um_desc(base + (OZ_S + j) * HALF + kk * 2 * kb, kb, 128);
+            um_mma(taddr + (uint32_t)(l * 128), ad, bd, idesc, (started >> l) & 1u);
+            started |= 1u << l;
+          }
+        }
+      um_commit(&s_mma[half]);   // also tracks every earlier product
+      s_last = half;
+    }
+  }
+  const int q = warp & 3, hf = warp >> 2;
+  const int r = ti * 128 + q * 32 + lane;
+  __syncthreads();
+  const int last = s_last;
+  if (last >= 0) {   // every exit path waits for the last commit (it tracks all earlier products)
+    if (!mbar_wait_bounded(&s_mma[last], 0)) s_fail = 1;
+    um_fence_after();
+  }
+  __syncthreads();
+  const uint32_t tbase = taddr + ((uint32_t)(q * 32) << 16);
+  if (!s_fail) {
+    if (MODE == 1) {
+      // G tile += (level 0 + level 1 + level 2) in double-float
+      float4* G = parity ? d.g_alt : d.g;
+      const int col0 = tj * 64 + hf * 32;
+      const int ncol = min(32, ns - col0);
+#pragma unroll 1
+      for (int ch = 0; ch < 2; ++ch) {
+        const int c0 = ch * 16;
+        if (ncol <= c0) break;   // warp-uniform
+        float4 gv[16];
+        if (r < ns) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c)
+            if (c0 + c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c0 + c)];
+        }
+        float re[3][16], im[3][16];
+        xg_load(tbase, hf * 32 + c0, 8 * ncg, re, im);
+        if (r < ns) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            if (c0 + c >= ncol) continue;
+            const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
+            const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
+            const float4 g = gv[c];
+            const df nr = df_add(df{g.x, g.z}, vr), ni = df_add(df{g.y, g.w}, vi);
+            G[r + (size_t)ns * (col0 + c0 + c)] = make_float4(nr.hi, ni.hi, nr.lo, ni.lo);
+          }
+        }
+      }
+    } else {
+      // X tile (128 rows x 64 complex columns): row exponent over both
+      // column halves, then the slices of the flush's A operand [Xr | Xi]
+      float mx = 0.f;
+#pragma unroll 1
+      for (int ch = 0; ch < 2; ++ch) {
+        float re[3][16], im[3][16];
+        xg_load(tbase, hf * 32 + ch * 16, 64, re, im);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
+          const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
+          mx = fmaxf(mx, fmaxf(fabsf(vr.hi), fabsf(vi.hi)));
+        }
+      }
+      s_rmax[hf][q * 32 + lane] = mx;
+      __syncthreads();
+      const int e = oz_exp(fmaxf(s_rmax[0][q * 32 + lane], s_rmax[1][q * 32 + lane]));
+      const int row = q * 32 + lane;
+#pragma unroll 1
+      for (int ch = 0; ch < 2; ++ch) {
+        float re[3][16], im[3][16];
+        xg_load(tbase, hf * 32 + ch * 16, 64, re, im);
+        if (r < ns) {
+#pragma unroll
+          for (int g8 = 0; g8 < 2; ++g8) {
+            float rs[OZ_S][8], is[OZ_S][8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int c = g8 * 8 + u;
+              const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
+              const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
+              float qr[OZ_S], qi[OZ_S];
+              oz_split(vr.hi, vr.lo, e, qr);
+              oz_split(vi.hi, vi.lo, e, qi);
+#pragma unroll
+              for (int s = 0; s < OZ_S; ++s) {
+                rs[s][u] = qr[s];
+                is[s][u] = qi[s];
+              }
+            }
+            const int k = hf * 32 + ch * 16 + g8 * 8;
+#pragma unroll
+            for (int s = 0; s < OZ_S; ++s) {
+              unsigned char* im2 = d.img + (size_t)oz_slot_a2(ns, ti, s) * UM_IMG;
+              *reinterpret_cast<uint4*>(im2 + um_off(row, k, nrg_a)) = oz_pack8(rs[s]);
+              *reinterpret_cast<uint4*>(im2 + um_off(row, UM_KP + k, nrg_a)) = oz_pack8(is[s]);
+            }
+          }
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(d.err, PQMC_ERR_TIMEOUT);
+  }
+  um_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(taddr) : "memory");
+}
+
+int exact_setup() {
+  PQMC_CUDA(raise_dyn_smem(k_xcore, (int)XC_SMEM));
+  PQMC_CUDA(raise_dyn_smem(k_xgemm<0>, XG_SMEM));
+  PQMC_CUDA(raise_dyn_smem(k_xgemm<1>, XG_SMEM));
+  return PQMC_OK;
+}
+
+int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi) {
+  const int n_a = (ns + XC_THREADS - 1) / XC_THREADS, n_b = (ns + XC_THREADS / 32 - 1) / (XC_THREADS / 32);
+  PQMC_CUDA(launch_at(k_xcore, dim3(1 + n_a + n_b, C), dim3(XC_THREADS), XC_SMEM, st, prio, prio_hi, d_x, dim, parity,
+                      n_a));
+  PQMC_LAUNCHED();
+  return PQMC_OK;
+}
+
+int exact_products(const XDesc* d_x, int C, int ns, int parity, cudaStream_t st, bool prio, int prio_hi) {
+  const int RT = um_rtiles(ns), CT = um_ctiles(ns);
+  PQMC_CUDA(launch_at(k_xgemm<0>, dim3(RT, C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
+  PQMC_LAUNCHED();
+  PQMC_CUDA(launch_at(k_xgemm<1>, dim3(RT * CT, C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
+  PQMC_LAUNCHED();
+  return PQMC_OK;
+}
+
+}  // namespace pqmc
+
+// ---------------------------------------------------------------------------
+// pqmc_exact_update_check: the exact round update of one round applied to a
+// G given on the host (validation entry point, see include/pqmc_gb300.h).
+namespace pqmc {
+__global__ void k_x_to_df(const cplx* a, float4* b, long n) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    b[e] = dg_make(a[e]);
+}
+__global__ void k_x_from_df(const float4* a, cplx* b, long n) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    b[e] = dg_to_d(a[e]);
+}
+}  // namespace pqmc
+
+extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g,
+                                       double* lncw_out) {
+  using namespace pqmc;
+  if (!sites || !delta || !g || !lncw_out || dim < 1 || dim > 4 || k < dim || k > UM_KP || k % dim || ns < k ||
+      ns > 4096) {
+    set_error("exact_update_check: need 1 <= dim <= 4, dim <= k <= %d, k %% dim == 0, k <= ns <= 4096", UM_KP);
+    return PQMC_ERR_ARG;
+  }
+  for (int i = 0; i < k; ++i)
+    if (sites[i] < 0 || sites[i] >= ns) {
+      set_error("exact_update_check: site %d out of range", sites[i]);
+      return PQMC_ERR_ARG;
+    }
+  PQMC_TRY(exact_setup());
+  const size_t n2 = (size_t)ns * ns;
+  const int nb = k / dim;
+  cplx* d_g64 = nullptr;
+  float4* d_g = nullptr;
+  int* d_site = nullptr;
+  float4* d_dl = nullptr;
+  float2* d_detf = nullptr;
+  double* d_thr = nullptr;
+  int* d_k = nullptr;
+  unsigned char* d_img = nullptr;
+  DevScalars* d_sc = nullptr;
+  int* d_err = nullptr;
+  unsigned long long* d_nf = nullptr;
+  XDesc* d_x = nullptr;
+  int st = PQMC_OK;
+  auto run = [&]() -> int {
+    PQMC_CUDA(cudaMalloc((void**)&d_g64, sizeof(cplx) * n2));
+    PQMC_CUDA(cudaMalloc((void**)&d_g, sizeof(float4) * n2));
+    PQMC_CUDA(cudaMalloc((void**)&d_site, sizeof(int) * k));
+    PQMC_CUDA(cudaMalloc((void**)&d_dl, sizeof(float4) * 16 * nb));
+    PQMC_CUDA(cudaMalloc((void**)&d_detf, sizeof(float2) * nb));
+    PQMC_CUDA(cudaMalloc((void**)&d_thr, sizeof(double) * nb));
+    PQMC_CUDA(cudaMalloc((void**)&d_k, sizeof(int)));
+    PQMC_CUDA(cudaMalloc((void**)&d_img, oz_chain_bytes(ns)));
+    PQMC_CUDA(cudaMalloc((void**)&d_sc, sizeof(DevScalars)));
+    PQMC_CUDA(cudaMalloc((void**)&d_err, sizeof(int)));
+    PQMC_CUDA(cudaMalloc((void**)&d_nf, sizeof(unsigned long long)));
+    PQMC_CUDA(cudaMalloc((void**)&d_x, sizeof(XDesc)));
+    PQMC_CUDA(cudaMemset(d_img, 0, oz_chain_bytes(ns)));
+    PQMC_CUDA(cudaMemset(d_sc, 0, sizeof(DevScalars)));
+    PQMC_CUDA(cudaMemset(d_err, 0, sizeof(int)));
+    PQMC_CUDA(cudaMemset(d_nf, 0, sizeof(unsigned long long)));
+    PQMC_CUDA(cudaMemset(d_detf, 0, sizeof(float2) * nb));
+    PQMC_CUDA(cudaMemset(d_thr, 0, sizeof(double) * nb));
+    PQMC_CUDA(cudaMemcpy(d_g64, g, sizeof(cplx) * n2, cudaMemcpyHostToDevice));
+    PQMC_CUDA(cudaMemcpy(d_site, sites, sizeof(int) * k, cudaMemcpyHostToDevice));
+    PQMC_CUDA(cudaMemcpy(d_k, &k, sizeof(int), cudaMemcpyHostToDevice));
+    // Delta blocks (dim x dim, column-major, FP64 complex) -> 16-entry double-float records
+    std::vector<cplx> dl((size_t)16 * nb, mk(0.0));
+    for (int b = 0; b < nb; ++b)
+      for (int e = 0; e < dim * dim; ++e)
+        dl[(size_t)16 * b + e] = mk(delta[2 * ((size_t)b * dim * dim + e)], delta[2 * ((size_t)b * dim * dim + e) + 1]);
+    cplx* d_dl64 = nullptr;
+    PQMC_CUDA(cudaMalloc((void**)&d_dl64, sizeof(cplx) * dl.size()));
+    PQMC_CUDA(cudaMemcpy(d_dl64, dl.data(), sizeof(cplx) * dl.size(), cudaMemcpyHostToDevice));
+    k_x_to_df<<<64, 256>>>(d_dl64, d_dl, (long)dl.size());
+    PQMC_LAUNCHED();
+    k_x_to_df<<<256, 256>>>(d_g64, d_g, (long)n2);
+    PQMC_LAUNCHED();
+    XDesc x;
+    memset(&x, 0, sizeof(x));
+    x.g = d_g;
+    x.g_alt = d_g;
+    x.ns = ns;
+    x.ncopy = 1;
+    x.tr_weight = 0;
+    x.kmax = UM_KP;
+    x.kcount = d_k;
+    x.acc_site = d_site;
+    x.acc_delta = d_dl;
+    x.acc_detf = d_detf;
+    x.acc_thr = d_thr;
+    x.img = d_img;
+    x.sc = d_sc;
+    x.err = d_err;
+    x.nflush = d_nf;
+    PQMC_CUDA(cudaMemcpy(d_x, &x, sizeof(XDesc), cudaMemcpyHostToDevice));
+    PQMC_TRY(exact_core(d_x, 1, ns, dim, 0, 0, false, 0));
+    PQMC_TRY(exact_products(d_x, 1, ns, 0, 0, false, 0));
+    k_x_from_df<<<256, 256>>>(d_g, d_g64, (long)n2);
+    PQMC_LAUNCHED();
+    PQMC_CUDA(cudaDeviceSynchronize());
+    cudaFree(d_dl64);
+    int herr = 0;
+    PQMC_CUDA(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr != 0) {
+      set_error("exact_update_check: device error %d", herr);
+      return herr;
+    }
+    PQMC_CUDA(cudaMemcpy(g, d_g64, sizeof(cplx) * n2, cudaMemcpyDeviceToHost));
+    DevScalars hs;
+    PQMC_CUDA(cudaMemcpy(&hs, d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
+    *lncw_out = hs.ln_cw.x;
+    return PQMC_OK;
+  };
+  st = run();
+  cudaFree(d_g64);
+  cudaFree(d_g);
+  cudaFree(d_site);
+  cudaFree(d_dl);
+  cudaFree(d_detf);
+  cudaFree(d_thr);
+  cudaFree(d_k);
+  cudaFree(d_img);
+  cudaFree(d_sc);
+  cudaFree(d_err);
+  cudaFree(d_nf);
+  cudaFree(d_x);
+  return st;
+}

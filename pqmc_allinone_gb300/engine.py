@@ -388,7 +388,7 @@ class PqmcBatch:
             check(self.lib, self.lib.pqmc_batch_class_info(self.h, k, v.ctypes.data_as(_i32p)),
                   "pqmc_batch_class_info")
             out.append({"chains": int(v[0]), "ns": int(v[1]), "ntime": int(v[2]), "delay_depth": int(v[3]),
-                        "flush": "tcgen05" if v[4] == 1 else "mma.sync", "groups": int(v[5])})
+                        "flush": {2: "exact", 1: "tcgen05"}.get(int(v[4]), "mma.sync"), "groups": int(v[5])})
         return out
 
     def graph_count(self) -> int:
@@ -397,8 +397,22 @@ class PqmcBatch:
         return int(n[0])
 
     def set_flush(self, mode: int):
-        """1: tcgen05 flush (delay depth <= 64), 0: mma.sync flush."""
+        """2: exact round update (default; double-float Woodbury update of the
+        round from G with Ozaki-split tcgen05 products, double-float wraps),
+        1: tcgen05 flush of the scan's FP32 panels, 0: mma.sync flush of them
+        (both delay depth <= 64 on the tensor cores)."""
         check(self.lib, self.lib.pqmc_batch_set_flush(self.h, mode), "pqmc_batch_set_flush")
+
+    def exact_stats(self) -> tuple[list, list]:
+        """Per chain: largest relative error of the scan's FP32 ratios against
+        the double-float ones, and accepted moves the double-float ratio would
+        have rejected (exact round update only)."""
+        n = len(self.chains)
+        err = np.zeros(n)
+        fl = (ctypes.c_longlong * n)()
+        check(self.lib, self.lib.pqmc_batch_exact_stats(self.h, err.ctypes.data_as(_f64p), fl),
+              "pqmc_batch_exact_stats")
+        return [float(v) for v in err], [int(v) for v in fl]
 
     def close(self):
         if getattr(self, "h", None) is not None:
@@ -412,3 +426,22 @@ class PqmcBatch:
             self.close()
         except Exception:
             pass
+
+
+def exact_update_check(g: np.ndarray, sites, delta) -> tuple[np.ndarray, float]:
+    """The batch's exact round update applied to a host G (validation):
+    returns (G + G(:,S) Delta_S W^-1 (E_S - G(S,:)), sum_j log Re det R_j),
+    sites in acceptance order (dim per move), delta (n_moves, dim, dim)."""
+    lib = load_library()
+    ns = g.shape[0]
+    d = np.asarray(delta, dtype=np.complex128)
+    nb, dim = d.shape[0], d.shape[1]
+    s = np.ascontiguousarray(sites, dtype=np.int32)
+    gg = np.asfortranarray(g, dtype=np.complex128).copy(order="F")
+    dl = np.ascontiguousarray(np.stack([np.asfortranarray(x).ravel(order="F") for x in d]))
+    out = np.zeros(1)
+    check(lib, lib.pqmc_exact_update_check(ns, len(s), dim, s.ctypes.data_as(_i32p),
+                                            dl.view(np.float64).ctypes.data_as(_f64p),
+                                            gg.ravel(order="K").view(np.float64).ctypes.data_as(_f64p),
+                                            out.ctypes.data_as(_f64p)), "pqmc_exact_update_check")
+    return gg, float(out[0])

@@ -51,8 +51,10 @@ def parse():
     p.add_argument("--chains", type=int, default=0, help="chains per GPU of the mixed batch (default 64)")
     p.add_argument("--delay", type=int, default=0,
                    help="delay depth of the mixed batch (0: chosen by the autotuner during warm-up)")
-    p.add_argument("--flush", type=int, default=1, choices=[0, 1],
-                   help="rank-K flush engine: 1 tcgen05 (tensor memory accumulator), 0 mma.sync")
+    p.add_argument("--flush", type=int, default=2, choices=[0, 1, 2],
+                   help="round update: 2 exact (double-float Woodbury update of the round from G, Ozaki-split "
+                        "tcgen05 products, double-float wraps), 1 tcgen05 flush of the FP32 panels, 0 mma.sync "
+                        "flush of them")
     p.add_argument("--plain-steps", type=int, default=3, help="timed blocks of the plain FP64 chain")
     p.add_argument("--cpu-slices", type=int, default=0, help="slices per chain in the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -330,6 +332,7 @@ def run_mixed(args, world, rank, local):
     fields = [M.field_gaussian(m, s) for s in seeds]
     b = PqmcBatch([m] * C, fields, [seed_words(s) for s in seeds], precision=1)
     b.set_graphs(bool(args.graphs))
+    b.set_flush(args.flush)
     t0 = time.perf_counter()
     b.init()
     t_init = time.perf_counter() - t0
@@ -340,8 +343,9 @@ def run_mixed(args, world, rank, local):
         b.set_flush(args.flush)
         depth = args.delay
     else:
-        # the autotuner runs one block per candidate depth (part of the warm-up)
-        cands = (32, 48, 64, 96, 128)
+        # the autotuner runs one block per candidate depth (part of the warm-up);
+        # the tensor-core round updates take at most 64 columns
+        cands = (16, 32, 48, 64) if args.flush in (1, 2) else (32, 48, 64, 96, 128)
         depth, table = b.autotune(cur.loop, cur.tc, m.ngroup, cands)
         for _ in cands:
             cur.next()

@@ -424,13 +424,6 @@ int pqmc_batch_get_timing(pqmc_batch* batch, double* ms, long long* launches);
  * to fold in since the last pqmc_batch_set_timing, i.e. the number of
  * read-modify-writes of the chain's G by the flush. */
 int pqmc_batch_flush_rounds(pqmc_batch* batch, long long* rounds);
-/* Per chain (no reference counterpart): with the exact round update
- * (flush mode 2) every accepted move's ratio det R is recomputed in
- * double-float from the G the round started from; ratio_err[i] is the
- * largest relative difference of the scan's FP32 det R from it so far and
- * flips[i] the accepted moves whose double-float |det R|^2 fell below the
- * Metropolis threshold the FP32 value passed. */
-int pqmc_batch_exact_stats(pqmc_batch* batch, double* ratio_err, long long* flips);
 /* Slice graphs (mixed batches, on by default; no reference counterpart):
  * the family steps of a slice (draws, proposals, scan rounds, flushes,
  * wraps) are captured once per chain group, direction and G-buffer parity
@@ -479,12 +472,11 @@ int pqmc_cal_g_and_det_noalloc(const double* x_left, const double* rmat, int ns,
  *   g <- g + g(:,S) Delta_S W^-1 (E_S - g(S,:)),  W = I + g(S,S) Delta_S,
  * with S = sites[0..k) (0-based, dim per move, in acceptance order) and
  * Delta_S block diagonal (delta: k/dim blocks of dim x dim complex,
- * column-major).  The arithmetic is the batch's: double-float Gauss-Jordan
- * for W^-1 and Ozaki-split BF16 tensor-core products.  *lncw_out receives
- * sum_j log Re det R_j of the moves' ratio matrices (ncopy 1, no TR).
+ * column-major).  The arithmetic is the batch's: W^-1 from an FP32
+ * Gauss-Jordan refined by one Newton step with a double-float residual, and
+ * Ozaki-split BF16 tensor-core products.
  * Limits: 1 <= dim <= 4, k <= 64, k % dim == 0, k <= ns <= 4096. */
-int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g,
-                            double* lncw_out);
+int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g);
 
 /* ---- introspection --------------------------------------------------- */
 const char* pqmc_version(void);

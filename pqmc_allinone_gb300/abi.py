@@ -253,9 +253,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_states": ([vp, ctypes.POINTER(PqmcState)], ctypes.c_int),
         "pqmc_batch_class_info": ([vp, ctypes.c_int, _i32p], ctypes.c_int),
         "pqmc_batch_graph_count": ([vp, _i32p], ctypes.c_int),
-        "pqmc_batch_exact_stats": ([vp, _f64p, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
-        "pqmc_exact_update_check": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _f64p, _f64p, _f64p],
-                                    ctypes.c_int),
+        "pqmc_exact_update_check": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _f64p, _f64p], ctypes.c_int),
         "pqmc_version": ([], ctypes.c_char_p),
         "pqmc_last_error": ([], ctypes.c_char_p),
         "pqmc_kernel_launches": ([], ctypes.c_int64),

@@ -64,20 +64,7 @@ struct BDesc {
   // the round's accepted moves for the exact update (exact.cuh)
   int* acc_site;
   float4* acc_delta;
-  float2* acc_detf;
-  double* acc_thr;
 };
-
-__device__ __forceinline__ float2 f2(cplx a) { return make_float2((float)a.x, (float)a.y); }
-__device__ __forceinline__ float2 fm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ float2 fa(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 fsb(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-// the high words of a double-float complex (the FP32 rounding of its value)
-__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.x, v.y); }
-// acc + a*b in four FMAs
-__device__ __forceinline__ float2 fcfma(float2 a, float2 b, float2 acc) {
-  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y)));
-}
 
 // ---------------------------------------------------------------------------
 // the ran2 draws of n_fam family steps in sweep order (family pf_first,
@@ -232,128 +219,6 @@ __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf_first, int
 // plaquettes.
 constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_KSTAGE = 512;   // max delay depth (panel columns)
-
-__device__ __forceinline__ float2 fdiv1(float2 a) {   // 1/a
-  float n = a.x * a.x + a.y * a.y;
-  return make_float2(a.x / n, -a.y / n);
-}
-
-// small complex inverse in FP32 by Gauss-Jordan with partial pivoting on one
-// thread (sizes below 4)
-__device__ void finv_small(int n, float2* a) {
-  float2 inv[16];
-  for (int j = 0; j < n; ++j)
-    for (int i = 0; i < n; ++i) inv[i + n * j] = make_float2(i == j ? 1.f : 0.f, 0.f);
-  for (int j = 0; j < n; ++j) {
-    int jp = j;
-    float best = -1.f;
-    for (int i = j; i < n; ++i) {
-      float v = fabsf(a[i + n * j].x) + fabsf(a[i + n * j].y);
-      if (v > best) { best = v; jp = i; }
-    }
-    if (jp != j)
-      for (int k = 0; k < n; ++k) {
-        float2 t = a[j + n * k]; a[j + n * k] = a[jp + n * k]; a[jp + n * k] = t;
-        t = inv[j + n * k]; inv[j + n * k] = inv[jp + n * k]; inv[jp + n * k] = t;
-      }
-    float2 r = fdiv1(a[j + n * j]);
-    for (int k = 0; k < n; ++k) { a[j + n * k] = fm(a[j + n * k], r); inv[j + n * k] = fm(inv[j + n * k], r); }
-    for (int i = 0; i < n; ++i) {
-      if (i == j) continue;
-      float2 f = a[i + n * j];
-      for (int k = 0; k < n; ++k) {
-        a[i + n * k] = fsb(a[i + n * k], fm(f, a[j + n * k]));
-        inv[i + n * k] = fsb(inv[i + n * k], fm(f, inv[j + n * k]));
-      }
-    }
-  }
-  for (int k = 0; k < n * n; ++k) a[k] = inv[k];
-}
-
-__device__ float2 fdet_small(int n, const float2* a) {
-  if (n == 1) return a[0];
-  if (n == 2) return fsb(fm(a[0], a[3]), fm(a[2], a[1]));
-  float2 b[16];
-  for (int k = 0; k < n * n; ++k) b[k] = a[k];
-  float2 det = make_float2(1.f, 0.f);
-  for (int j = 0; j < n; ++j) {
-    int jp = j;
-    float best = -1.f;
-    for (int i = j; i < n; ++i) {
-      float v = fabsf(b[i + n * j].x) + fabsf(b[i + n * j].y);
-      if (v > best) { best = v; jp = i; }
-    }
-    if (jp != j) {
-      for (int k = 0; k < n; ++k) { float2 t = b[j + n * k]; b[j + n * k] = b[jp + n * k]; b[jp + n * k] = t; }
-      det = make_float2(-det.x, -det.y);
-    }
-    det = fm(det, b[j + n * j]);
-    float2 r = fdiv1(b[j + n * j]);
-    for (int i = j + 1; i < n; ++i) {
-      float2 f = fm(b[i + n * j], r);
-      for (int k = j; k < n; ++k) b[i + n * k] = fsb(b[i + n * k], fm(f, b[j + n * k]));
-    }
-  }
-  return det;
-}
-
-// determinant of the dim x dim FP32 matrix R (shared, column-major) returned
-// to every lane: Laplace expansion along rows 0,1 over six lanes for dim 4,
-// lane 0 otherwise
-__device__ __forceinline__ float2 wf_det(int dim, const float2* R, int lane) {
-  float2 v = make_float2(0.f, 0.f);
-  if (dim == 4) {
-    if (lane < 6) {
-      // column pair (j,k) of rows 0,1 and the complementary pair (l,m) of
-      // rows 2,3, packed one hex digit per lane (no local-memory tables)
-      const int sh = 4 * lane;
-      const int j = (0x211000 >> sh) & 15, k = (0x332321 >> sh) & 15;
-      const int l = (0x000112 >> sh) & 15, m = (0x123233 >> sh) & 15;
-      const float sg = ((0x12 >> lane) & 1) ? -1.f : 1.f;
-      float2 mi = fsb(fm(R[0 + 4 * j], R[1 + 4 * k]), fm(R[0 + 4 * k], R[1 + 4 * j]));
-      float2 co = fsb(fm(R[2 + 4 * l], R[3 + 4 * m]), fm(R[2 + 4 * m], R[3 + 4 * l]));
-      float2 t = fm(mi, co);
-      v = make_float2(sg * t.x, sg * t.y);
-    }
-    for (int o = 4; o > 0; o >>= 1) {
-      float vx = __shfl_down_sync(0xffffffffu, v.x, o), vy = __shfl_down_sync(0xffffffffu, v.y, o);
-      if (lane + o < 8) { v.x += vx; v.y += vy; }
-    }
-  } else if (lane == 0) {
-    v = fdet_small(dim, R);
-  }
-  return make_float2(__shfl_sync(0xffffffffu, v.x, 0), __shfl_sync(0xffffffffu, v.y, 0));
-}
-
-// R <- R^-1 in place (shared, column-major): adjugate over 16 lanes for dim 4
-// (the complementary row/column triples formed branch-free, one reciprocal
-// of |det|^2 per lane), lane-0 Gauss-Jordan otherwise
-__device__ __forceinline__ void wf_inverse(int dim, float2* R, float2 det, int lane) {
-  if (dim == 4) {
-    float2 cof = make_float2(0.f, 0.f);
-    const int i = lane & 3, j = lane >> 2;
-    if (lane < 16) {
-      // rows other than i and columns other than j, ascending
-      const int r0 = i == 0 ? 1 : 0, r1 = i <= 1 ? 2 : 1, r2 = i <= 2 ? 3 : 2;
-      const int c0 = j == 0 ? 1 : 0, c1 = j <= 1 ? 2 : 1, c2 = j <= 2 ? 3 : 2;
-      const float2 a00 = R[r0 + 4 * c0], a01 = R[r0 + 4 * c1], a02 = R[r0 + 4 * c2];
-      const float2 a10 = R[r1 + 4 * c0], a11 = R[r1 + 4 * c1], a12 = R[r1 + 4 * c2];
-      const float2 a20 = R[r2 + 4 * c0], a21 = R[r2 + 4 * c1], a22 = R[r2 + 4 * c2];
-      cof = fa(fsb(fm(a00, fsb(fm(a11, a22), fm(a12, a21))), fm(a01, fsb(fm(a10, a22), fm(a12, a20)))),
-               fm(a02, fsb(fm(a10, a21), fm(a11, a20))));
-      if ((i + j) & 1) cof = make_float2(-cof.x, -cof.y);
-      const float rn = __frcp_rn(det.x * det.x + det.y * det.y);   // 1/det = conj(det)/|det|^2
-      cof = fm(cof, make_float2(det.x * rn, -det.y * rn));
-    }
-    __syncwarp();
-    if (lane < 16) R[j + 4 * i] = cof;
-    __syncwarp();
-    return;
-  }
-  if (lane == 0) finv_small(dim, R);
-  __syncwarp();
-}
-
 
 constexpr int SCAN_NSTAGE = 3;   // panel chunks in flight
 constexpr int SCAN_RPT = 2;      // rows per thread: Ns <= SCAN_RPT * SCAN_THREADS
@@ -684,16 +549,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     const int pa_ = s_accp[ja];
     d.field[M.bf[pa_ + M.max_pla * pf] + (size_t)M.n_bf * t] = pre[pa_].xnew;
   }
-  if (exact) {
-    // the accepted moves for the exact update: sites, Delta, the FP32 ratio
-    // and the threshold it passed (ln_cw is updated there from the exact
-    // ratios)
+  if (exact) {   // the accepted moves for the exact update: sites and Delta
     for (int e = tid; e < n_acc * dim; e += blockDim.x) d.acc_site[e] = s_site[4 * s_accp[e / dim] + e % dim];
     for (int e = tid; e < n_acc * 16; e += blockDim.x) d.acc_delta[e] = pre[s_accp[e / 16]].deltad[e % 16];
-    for (int ja = tid; ja < n_acc; ja += blockDim.x) {
-      d.acc_detf[ja] = s_accd[ja];
-      d.acc_thr[ja] = s_thr[s_accp[ja]];
-    }
   }
   if (warp == 0) {
     // ln_cw += log prod_j Re(R_j^ncopy) (|R_j|^2 under TR_weight), as a
@@ -728,7 +586,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
     if (lane == 0) {
       *d.kcount = K;
       next_p[blockIdx.x] = p;
-      if (n_acc > 0 && !exact) {
+      if (n_acc > 0) {
         const double l = (mant > 0.0) ? log(mant) + (double)ex * 0.69314718055994530942 : log(mant);
         d.sc->ln_cw = cadd(d.sc->ln_cw, mk(l));
       }
@@ -1111,9 +969,12 @@ constexpr int WRAP_R = 32, WRAP_C = 4;
 // double-float (A - I) and (B - I) entries; out(a, b, v) stores entry (a, b).
 template <int DIM, typename AM, typename BM, typename OUT>
 __device__ __forceinline__ void wrap_block_df(const float4 (&gd)[DIM][DIM], int dr, int dc, AM am, BM bm, OUT out) {
-  dfc gb[DIM][DIM];   // G (B - I)
+  // one column b of the block at a time: G (B - I) of column b, then the
+  // correction of column b
 #pragma unroll
-  for (int b = 0; b < DIM; ++b)
+  for (int b = 0; b < DIM; ++b) {
+    if (b >= dc) break;
+    dfc gb[DIM];
 #pragma unroll
     for (int a = 0; a < DIM; ++a) {
       dfc acc = dfc_zero();
@@ -1122,29 +983,52 @@ __device__ __forceinline__ void wrap_block_df(const float4 (&gd)[DIM][DIM], int 
         const float4 v = bm(k, b);
         acc = dfc_fms(acc, dfc{df{-gd[a][k].x, -gd[a][k].z}, df{-gd[a][k].y, -gd[a][k].w}}, dfc{df{v.x, v.z}, df{v.y, v.w}});
       }
-      gb[a][b] = acc;
+      gb[a] = acc;
     }
 #pragma unroll
-  for (int b = 0; b < DIM; ++b)
-#pragma unroll
     for (int a = 0; a < DIM; ++a) {
-      if (a >= dr || b >= dc) continue;
-      dfc corr = gb[a][b];
+      if (a >= dr) break;
+      dfc corr = gb[a];
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
         const float4 v = am(a, k);
-        const dfc x = dfc_add(dfc{df{gd[k][b].x, gd[k][b].z}, df{gd[k][b].y, gd[k][b].w}}, gb[k][b]);
+        const dfc x = dfc_add(dfc{df{gd[k][b].x, gd[k][b].z}, df{gd[k][b].y, gd[k][b].w}}, gb[k]);
         corr = dfc_fms(corr, dfc{df{-v.x, -v.z}, df{-v.y, -v.w}}, x);
       }
       const dfc n = dfc_add(dfc{df{gd[a][b].x, gd[a][b].z}, df{gd[a][b].y, gd[a][b].w}}, corr);
       out(a, b, make_float4(n.re.hi, n.im.hi, n.re.lo, n.im.lo));
     }
+  }
+}
+
+// the double-float (A - I) (row use) and (B - I) (column use) of every cover
+// item of family pf at the group's slice, once per wrap and chain:
+// tab[0][e][item] and tab[1][e][item], e = a + DIM b, zero for singletons
+template <int DIM>
+__global__ void k_wtab(const BDesc* D, int pf, int left, int n_items, const int* __restrict__ wpla,
+                       const int* __restrict__ wdim, float4* tab_all) {
+  const BDesc& d = D[blockIdx.y];
+  const DevModel& M = d.M;
+  const int t = d.t, pd = M.pdim;
+  float4* tab = tab_all + (size_t)blockIdx.y * 2 * 16 * n_items;
+  const int n = 2 * DIM * DIM * n_items;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int item = e % n_items, ent = (e / n_items) % (DIM * DIM), isc = e / (n_items * DIM * DIM);
+    const int a = ent % DIM, b = ent / DIM;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int p = wpla[item], dm = wdim[item];
+    if (p >= 0 && a < dm && b < dm) {
+      const cplx* X = (isc ? (left ? d.expkv_inv : d.expkv) : (left ? d.expkv : d.expkv_inv)) + M.kv_base(p, pf, t);
+      v = dg_make(csub(X[a + pd * b], mk(a == b ? 1.0 : 0.0)));
+    }
+    tab[(size_t)isc * 16 * n_items + (size_t)ent * n_items + item] = v;
+  }
 }
 
 template <int DIM, int DF>
-__global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap(const BDesc* D, int pf, int left, int n_items, int parity,
+__global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int left, int n_items, int parity,
                                                const int* __restrict__ wpla, const int* __restrict__ wsites,
-                                               const int* __restrict__ wdim) {
+                                               const int* __restrict__ wdim, const float4* __restrict__ tab_all) {
   __shared__ BDesc sd;
   __shared__ float4 s_am[DIM * DIM][WRAP_R];   // (A - I)(a, b) of row item lr at [a + DIM b][lr] (double-float)
   __shared__ float4 s_bm[DIM * DIM][WRAP_C];
@@ -1178,6 +1062,7 @@ __global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap(const BDesc* D, int p
       gd[a][b] = (a < dr && b < dc) ? gin[Sr[a] + (size_t)ns * Sc[b]] : make_float4(0.f, 0.f, 0.f, 0.f);
   // A - I and B - I formed in FP64 and rounded once; zero for singletons.
   // Consecutive threads take consecutive items of one entry.
+  const float4* tab = DF ? tab_all + (size_t)blockIdx.z * 2 * 16 * n_items : nullptr;
   for (int e = threadIdx.x; e < (WRAP_R + WRAP_C) * DIM * DIM; e += blockDim.x) {
     const bool isc = e >= WRAP_R * DIM * DIM;
     const int e2 = isc ? e - WRAP_R * DIM * DIM : e;
@@ -1185,12 +1070,14 @@ __global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap(const BDesc* D, int p
     const int il = e2 % nl, ent = e2 / nl, a = ent % DIM, b = ent / DIM;
     const int item = (isc ? ic0 : ir0) + il;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (item < n_items) {
+    if (DF) {   // the tables of k_wtab
+      if (item < n_items) v = tab[(size_t)(isc ? 1 : 0) * 16 * n_items + (size_t)ent * n_items + item];
+    } else if (item < n_items) {
       const int p = wpla[item], dm = wdim[item];
       if (p >= 0 && a < dm && b < dm) {
         const cplx* X = (isc ? (left ? d.expkv_inv : d.expkv) : (left ? d.expkv : d.expkv_inv)) + M.kv_base(p, pf, t);
         const cplx x = csub(X[a + pd * b], mk(a == b ? 1.0 : 0.0));
-        v = DF ? dg_make(x) : make_float4((float)x.x, (float)x.y, 0.f, 0.f);
+        v = make_float4((float)x.x, (float)x.y, 0.f, 0.f);
       }
     }
     if (isc) s_bm[ent][il] = v;
@@ -1241,9 +1128,9 @@ __host__ __device__ inline size_t wrapc_smem(int ns, int n_items, int dim) {
 }
 
 template <int DIM, int DF>
-__global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
+__global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
                                                     const int* __restrict__ wpla, const int* __restrict__ wsites,
-                                                    const int* __restrict__ wdim) {
+                                                    const int* __restrict__ wdim, const float4* __restrict__ tab_all) {
   __shared__ BDesc sd;
   __shared__ __align__(8) uint64_t s_bar;
   __shared__ int s_fail;
@@ -1300,7 +1187,19 @@ __global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap_cols(const BDesc* D, 
   // FP64 and rounded once (zero for singletons); consecutive threads take
   // consecutive items of one entry, four entries per thread in flight
   const int n_ent = (n_items + WRAPC_C) * DIM * DIM;
-  for (int e0 = tid; e0 < n_ent; e0 += 4 * blockDim.x) {
+  if (DF) {   // the tables of k_wtab
+    const float4* tab = tab_all + (size_t)blockIdx.y * 2 * 16 * n_items;
+    for (int e = tid; e < n_ent; e += blockDim.x) {
+      const bool isc = e >= n_items * DIM * DIM;
+      const int e2 = isc ? e - n_items * DIM * DIM : e;
+      const int nl = isc ? WRAPC_C : n_items;
+      const int il = e2 % nl, ent = e2 / nl, item = isc ? ic0 + il : il;
+      s_am[isc ? n_items * DIM * DIM + ent * WRAPC_C + il : ent * n_items + il] =
+          item < n_items ? tab[(size_t)(isc ? 1 : 0) * 16 * n_items + (size_t)ent * n_items + item]
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  for (int e0 = tid; e0 < n_ent && !DF; e0 += 4 * blockDim.x) {
     cplx x[4];
     int slot[4];
 #pragma unroll
@@ -1325,7 +1224,7 @@ __global__ void __launch_bounds__(128, DF ? 2 : 3) k_bwrap_cols(const BDesc* D, 
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u)   // s_bm follows s_am contiguously
-      if (slot[u] >= 0) s_am[slot[u]] = DF ? dg_make(x[u]) : make_float4((float)x[u].x, (float)x[u].y, 0.f, 0.f);
+      if (slot[u] >= 0) s_am[slot[u]] = make_float4((float)x[u].x, (float)x[u].y, 0.f, 0.f);
   }
   if (!mbar_wait_bounded(&s_bar, 0)) s_fail = 1;
   __syncthreads();
@@ -1435,7 +1334,8 @@ struct pqmc_batch {
   std::vector<pqmc::XDesc> h_xdesc;
   unsigned char* d_ximg = nullptr;  // slice images of the exact update
   unsigned char* d_acc = nullptr;   // accepted-move records of every chain
-  bool wrap_df = true;              // double-float wraps with the exact update
+  int wrap_df_mode = -1;            // double-float wraps: -1 with the exact update, 0 never, 1 always
+  float4* d_wtab = nullptr;         // per chain: the wrap's double-float (A - I), (B - I) tables
   // kernels launched at the device's highest stream priority (bit 0: the
   // scan, bit 1: the split and flush); slice graphs then use node priorities
   int prio_mask = 3, prio_hi = 0;
@@ -1581,14 +1481,28 @@ static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
   const BDesc* D = b->d_desc + b->g_first[g];
   cudaStream_t st = b->g_stream[g];
   const int l = left ? 1 : 0;
-  // double-float wrap with the exact round update (PQMC_WRAP_DF=0 keeps the
-  // FP32 correction there too)
-  const bool df = b->flush_mode == 2 && b->d_xdesc && b->wrap_df;
+  // double-float wrap with the exact round update; PQMC_WRAP_DF=0 keeps the
+  // FP32 correction there too, PQMC_WRAP_DF=1 uses double-float with every
+  // flush mode
+  const bool df = b->d_wtab && (b->wrap_df_mode == 1 || (b->wrap_df_mode < 0 && b->flush_mode == 2));
   cudaEvent_t tw = gphase_begin(b, g);
+  float4* tab = df ? b->d_wtab + (size_t)b->g_first[g] * 2 * 16 * w.n_items : nullptr;
+  if (df) {
+    const int n = 2 * 16 * w.n_items;
+    const dim3 gt((unsigned)((n + 255) / 256), (unsigned)C);
+    switch (c0->h_pf_dim[pf]) {
+      case 1: k_wtab<1><<<gt, 256, 0, st>>>(D, pf, l, w.n_items, w.d_pla, w.d_dim, tab); break;
+      case 2: k_wtab<2><<<gt, 256, 0, st>>>(D, pf, l, w.n_items, w.d_pla, w.d_dim, tab); break;
+      case 3: k_wtab<3><<<gt, 256, 0, st>>>(D, pf, l, w.n_items, w.d_pla, w.d_dim, tab); break;
+      default: k_wtab<4><<<gt, 256, 0, st>>>(D, pf, l, w.n_items, w.d_pla, w.d_dim, tab); break;
+    }
+    PQMC_LAUNCHED();
+  }
   if (pf < (int)b->wrap_cols.size() && b->wrap_cols[pf]) {
     const dim3 gc((unsigned)((w.n_items + WRAPC_C - 1) / WRAPC_C), (unsigned)C);
     const size_t sm = wrapc_smem(c0->ns, w.n_items, c0->h_pf_dim[pf]);
-#define PQMC_WC(DM, F) k_bwrap_cols<DM, F><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim)
+#define PQMC_WC(DM, F) \
+  k_bwrap_cols<DM, F><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim, tab)
     switch (c0->h_pf_dim[pf] + (df ? 4 : 0)) {
       case 1: PQMC_WC(1, 0); break;
       case 2: PQMC_WC(2, 0); break;
@@ -1606,7 +1520,8 @@ static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
   }
   const dim3 grid((unsigned)((w.n_items + WRAP_R - 1) / WRAP_R), (unsigned)((w.n_items + WRAP_C - 1) / WRAP_C),
                   (unsigned)C);
-#define PQMC_WG(DM, F) k_bwrap<DM, F><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim)
+#define PQMC_WG(DM, F) \
+  k_bwrap<DM, F><<<grid, 128, 0, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim, tab)
   switch (c0->h_pf_dim[pf] + (df ? 4 : 0)) {
     case 1: PQMC_WG(1, 0); break;
     case 2: PQMC_WG(2, 0); break;
@@ -2101,7 +2016,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       b->prio_hi = hi;
     }
     const char* denv = getenv("PQMC_WRAP_DF");
-    b->wrap_df = !(denv && atoi(denv) == 0);
+    b->wrap_df_mode = denv ? (atoi(denv) != 0 ? 1 : 0) : -1;
     const char* wenv = getenv("PQMC_WRAP_COLS");
     const bool wc_on = !(wenv && atoi(wenv) == 0);
     b->wrap_cols.assign(c0->n_pf, 0);
@@ -2163,7 +2078,8 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     // the exact round update: accepted-move records and slice images per
     // chain (images zero outside the rows and columns of G)
     PQMC_TRY(exact_setup());
-    const size_t acc_b = (size_t)UM_KP * (sizeof(int) + 16 * sizeof(float4) + sizeof(float2) + sizeof(double));
+    const size_t acc_b = (size_t)UM_KP * (sizeof(int) + 16 * sizeof(float4)) +
+                         (size_t)UM_KP * UM_KP * (sizeof(float4) + sizeof(float2));
     const size_t xib = oz_chain_bytes(c0->ns);
     PQMC_CUDA(cudaMalloc((void**)&b->d_acc, acc_b * n_chains));
     PQMC_CUDA(cudaMalloc((void**)&b->d_ximg, xib * n_chains));
@@ -2172,11 +2088,11 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     for (int i = 0; i < n_chains; ++i) {
       pqmc_chain* c = b->chains[i];
       BDesc& h = b->h_desc[i];
-      unsigned char* a = b->d_acc + acc_b * i;   // float4 and double parts first (alignment)
+      unsigned char* a = b->d_acc + acc_b * i;   // float4 parts first (alignment)
       h.acc_delta = reinterpret_cast<float4*>(a);
-      h.acc_thr = reinterpret_cast<double*>(a + (size_t)UM_KP * 16 * sizeof(float4));
-      h.acc_detf = reinterpret_cast<float2*>(a + (size_t)UM_KP * (16 * sizeof(float4) + sizeof(double)));
-      h.acc_site = reinterpret_cast<int*>(a + (size_t)UM_KP * (16 * sizeof(float4) + sizeof(double) + sizeof(float2)));
+      float4* wdf = h.acc_delta + (size_t)UM_KP * 16;
+      float2* v0 = reinterpret_cast<float2*>(wdf + (size_t)UM_KP * UM_KP);
+      h.acc_site = reinterpret_cast<int*>(v0 + (size_t)UM_KP * UM_KP);
       XDesc& x = b->h_xdesc[i];
       memset(&x, 0, sizeof(x));
       x.g = reinterpret_cast<float4*>(c->g);
@@ -2188,13 +2104,16 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       x.kcount = h.kcount;
       x.acc_site = h.acc_site;
       x.acc_delta = h.acc_delta;
-      x.acc_detf = h.acc_detf;
-      x.acc_thr = h.acc_thr;
+      x.wdf = wdf;
+      x.v0 = v0;
       x.img = b->d_ximg + xib * i;
       x.sc = c->sc;
       x.err = b->d_err;
       x.nflush = b->d_nflush + i;
     }
+    int max_items = 0;
+    for (int f = 0; f < c0->n_pf; ++f) max_items = std::max(max_items, c0->wrap[f].n_items);
+    PQMC_CUDA(cudaMalloc((void**)&b->d_wtab, sizeof(float4) * 2 * 16 * (size_t)max_items * n_chains));
     PQMC_CUDA(cudaMalloc((void**)&b->d_xdesc, sizeof(XDesc) * n_chains));
     PQMC_CUDA(cudaMemcpy(b->d_xdesc, b->h_xdesc.data(), sizeof(XDesc) * n_chains, cudaMemcpyHostToDevice));
   }
@@ -2259,6 +2178,7 @@ int pqmc_batch_destroy(pqmc_batch* b) {
   if (b->d_err) cudaFree(b->d_err);
   if (b->d_img) cudaFree(b->d_img);
   if (b->d_xdesc) cudaFree(b->d_xdesc);
+  if (b->d_wtab) cudaFree(b->d_wtab);
   if (b->d_ximg) cudaFree(b->d_ximg);
   if (b->d_acc) cudaFree(b->d_acc);
   if (b->d_tmaps) cudaFree(b->d_tmaps);
@@ -2445,21 +2365,6 @@ int pqmc_batch_states(pqmc_batch* b, pqmc_state* out) {
     o.negative_accept = h.neg_acc;
     for (int k = 0; k < 5; ++k) o.rng[k] = h.rng[k];
     o.reserved = 0;
-  }
-  return PQMC_OK;
-}
-
-int pqmc_batch_exact_stats(pqmc_batch* b, double* ratio_err, long long* flips) {
-  if (!b || !ratio_err || !flips) { set_error("batch_exact_stats: null argument"); return PQMC_ERR_ARG; }
-  const size_t n = b->chains.size();
-  if (!b->h_states) PQMC_CUDA(cudaMallocHost((void**)&b->h_states, sizeof(DevScalars) * n));
-  for (size_t i = 0; i < n; ++i)
-    PQMC_CUDA(cudaMemcpyAsync(b->h_states + i, b->chains[i]->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost,
-                              b->chains[i]->stream));
-  for (auto* c : b->chains) PQMC_CUDA(cudaStreamSynchronize(c->stream));
-  for (size_t i = 0; i < n; ++i) {
-    ratio_err[i] = b->h_states[i].err_ratio_max;
-    flips[i] = b->h_states[i].n_flip;
   }
   return PQMC_OK;
 }

@@ -25,11 +25,6 @@ struct DevScalars {
   int lu_info;
   int status;
   int pad;
-  // exact round update of the mixed batch: largest relative error of the
-  // scan's FP32 ratio det R against the double-float one, and the accepted
-  // moves whose double-float ratio is below the Metropolis threshold
-  double err_ratio_max;
-  long long n_flip;
 };
 
 // Control record the proposer publishes at every grid barrier of the update

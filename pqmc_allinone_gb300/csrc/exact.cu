@@ -66,73 +66,35 @@ __device__ __forceinline__ dfc dfc_inv(dfc a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_xcore: CTA 0 of each chain inverts W = I + G(S,S) Delta_S by
-// Gauss-Jordan in double-float, forms M = Delta_S W^-1, writes the slice
-// images of M (the B operand of X = G(:,S) M) and updates ln_cw from the
-// exact ratios; CTAs 1..n_a cut the rows of G(:,S) (the A operand), the
-// rest cut the columns of Z = E_S - G(S,:) (the B operand of the flush),
-// one warp per column.
+// M = Delta_S W^-1, W = I + G(S,S) Delta_S, in two launches:
+//   k_xinv  (CTA 0 of each chain) forms W in double-float and inverts its
+//           FP32 rounding by Gauss-Jordan over the moves' dim x dim blocks
+//           (the block pivots are the moves' ratio matrices R_j, each
+//           inverted by its adjugate): V0 = W^-1 to ~1e-6;
+//   k_xres  (XR_CTAS per chain, a column slab each) one Newton step,
+//           V1 = V0 + V0 (I - W V0), with the residual I - W V0 formed in
+//           double-float from every product's exact parts, so V1 = W^-1 to
+//           ~|I - W V0|^2; then M = Delta_S V1 and the Ozaki slices of M's
+//           columns (the B operand of X = G(:,S) M).
+// The other CTAs of k_xinv cut the rows of G(:,S) (the A operand of X) and
+// the columns of Z = E_S - G(S,:) (the B operand of the flush, a warp per
+// column); these depend on G and S only.
 constexpr int XC_THREADS = 512;
-constexpr int XC_LD = UM_KP;   // leading dimension of W in shared memory
-constexpr size_t XC_SMEM = sizeof(float4) * ((size_t)XC_LD * XC_LD + 16 * UM_KP + 3 * UM_KP) + sizeof(int) * 2 * UM_KP;
+constexpr int XC_LD = UM_KP;   // leading dimension of the K x K matrices
+constexpr int XR_CTAS = 8;     // column slabs of the Newton step per chain
+constexpr int XR_W = UM_KP / XR_CTAS;
+constexpr int XR_THREADS = UM_KP * XR_W;   // one residual entry per thread
+constexpr size_t XI_SMEM = sizeof(float4) * 16 * UM_KP + sizeof(float2) * ((size_t)XC_LD * XC_LD + 8 * UM_KP) +
+                           sizeof(int) * UM_KP;
+constexpr size_t XR_SMEM = sizeof(float4) * ((size_t)XC_LD * XC_LD + 16 * UM_KP + (size_t)UM_KP * XR_W) +
+                           sizeof(float2) * (size_t)XC_LD * XC_LD;
 
-__device__ __forceinline__ void xc_write_b1(const XDesc& d, const float4* W, int K, int tid) {
-  // M is W (rows: inner k, columns: output column c of X); column exponents
-  __shared__ int s_ce[UM_KP];
-  if (tid < UM_KP) {
-    float m = 0.f;
-    if (tid < K)
-      for (int k = 0; k < K; ++k) {
-        const float4 v = W[k * XC_LD + tid];
-        m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
-      }
-    s_ce[tid] = oz_exp(m);
-  }
-  __syncthreads();
-  const int K16 = (K + 15) & ~15, KG = K16 / 8;
-  const int ns = d.ns;
-  for (int it = tid; it < UM_KP * KG; it += XC_THREADS) {
-    const int c = it % UM_KP, kg = it / UM_KP;
-    float rs[OZ_S][8], is[OZ_S][8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int k = kg * 8 + u;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (c < K && k < K) v = W[k * XC_LD + c];
-      float qr[OZ_S], qi[OZ_S];
-      oz_split(v.x, v.z, s_ce[c], qr);
-      oz_split(v.y, v.w, s_ce[c], qi);
-#pragma unroll
-      for (int s = 0; s < OZ_S; ++s) {
-        rs[s][u] = qr[s];
-        is[s][u] = qi[s];
-      }
-    }
-    // B' re row c = [Mr | -Mi], im row 64 + c = [Mi | Mr]  (ncg = 8, 16 row groups)
-#pragma unroll
-    for (int s = 0; s < OZ_S; ++s) {
-      unsigned char* im = d.img + (size_t)oz_slot_b1(ns, s) * UM_IMG;
-      float ni[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) ni[u] = -is[s][u];
-      *reinterpret_cast<uint4*>(im + um_off(c, kg * 8, 16)) = oz_pack8(rs[s]);
-      *reinterpret_cast<uint4*>(im + um_off(c, UM_KP + kg * 8, 16)) = oz_pack8(ni);
-      *reinterpret_cast<uint4*>(im + um_off(64 + c, kg * 8, 16)) = oz_pack8(is[s]);
-      *reinterpret_cast<uint4*>(im + um_off(64 + c, UM_KP + kg * 8, 16)) = oz_pack8(rs[s]);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(XC_THREADS) k_xcore(const XDesc* X, int dim, int parity, int n_a) {
+__global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim, int parity, int n_a) {
   __shared__ XDesc sd;
-  __shared__ dfc s_inv;
-  __shared__ int s_fail;
+  __shared__ float2 s_pb[16];
   extern __shared__ __align__(16) unsigned char xc_dyn[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
-    sd = X[blockIdx.y];
-    s_fail = 0;
-  }
+  if (tid == 0) sd = X[blockIdx.y];
   __syncthreads();
   const XDesc& d = sd;
   const int K = *d.kcount;
@@ -141,20 +103,16 @@ __global__ void __launch_bounds__(XC_THREADS) k_xcore(const XDesc* X, int dim, i
   const float4* G = parity ? d.g_alt : d.g;
   const int K16 = (K + 15) & ~15;
   if (blockIdx.x == 0) {
-    // ---- W = I + G(S,S) Delta_S, inverted in place -------------------------
-    float4* W = reinterpret_cast<float4*>(xc_dyn);              // [K][XC_LD], row i at W + i*XC_LD
-    float4* s_dl = W + (size_t)XC_LD * XC_LD;                    // [n_acc][16] Delta blocks
-    float4* s_row = s_dl + 16 * UM_KP;                           // pivot row (before scaling)
-    float4* s_col = s_row + UM_KP;                               // pivot column
-    float4* s_det = s_col + UM_KP;                               // det of each block (double-float complex)
-    int* s_site = reinterpret_cast<int*>(s_det + UM_KP);
-    int* s_perm = s_site + UM_KP;
+    float4* s_dl = reinterpret_cast<float4*>(xc_dyn);                 // [n_acc][16] Delta blocks
+    float2* Wf = reinterpret_cast<float2*>(s_dl + 16 * UM_KP);        // [K][XC_LD] FP32 W, inverted in place
+    float2* s_row = Wf + (size_t)XC_LD * XC_LD;                       // [dim][UM_KP] pivot rows
+    float2* s_col = s_row + 4 * UM_KP;                                // [dim][UM_KP] pivot columns
+    int* s_site = reinterpret_cast<int*>(s_col + 4 * UM_KP);
     const int nb = K / dim;
     for (int k = tid; k < K; k += XC_THREADS) s_site[k] = d.acc_site[k];
     for (int e = tid; e < nb * 16; e += XC_THREADS) s_dl[e] = d.acc_delta[e];
-    for (int b = tid; b < nb; b += XC_THREADS) s_det[b] = make_float4(1.f, 0.f, 0.f, 0.f);
     __syncthreads();
-    // (i, column block jb): the dim entries W(i, jb*dim + jj)
+    // W(i, jb*dim + jj) = delta_ij + sum_m G(S_i, S_{jb dim + m}) Delta_jb(m, jj)
     for (int it = tid; it < K * nb; it += XC_THREADS) {
       const int i = it % K, jb = it / K;
       dfc gs[4];
@@ -169,140 +127,64 @@ __global__ void __launch_bounds__(XC_THREADS) k_xcore(const XDesc* X, int dim, i
 #pragma unroll
         for (int m = 0; m < 4; ++m)
           if (m < dim) a = dfc_mac(a, gs[m], dg_dfc(s_dl[jb * 16 + m + dim * jj]));
-        W[i * XC_LD + j] = dfc_dg(a);
+        d.wdf[i * XC_LD + j] = dfc_dg(a);
+        Wf[i * XC_LD + j] = make_float2(a.re.hi, a.im.hi);
       }
     }
     __syncthreads();
-    // Gauss-Jordan, pivots searched within the pivot's block (the block
-    // pivots are the sequential ratio matrices R_j)
+    // FP32 Gauss-Jordan in place by blocks of the moves: the pivot block P is
+    // inverted by its adjugate on 16 lanes, the multipliers F_i = W(i, bb)
+    // P^-1 are formed once per row
     const int ri = tid / 8, cg = tid % 8;   // row ri, columns cg, cg + 8, ...
-    for (int k = 0; k < K; ++k) {
+    for (int b = 0; b < nb; ++b) {
+      const int b0 = b * dim;
       if (warp == 0) {
-        int p = k;
-        if (lane == 0) {
-          const int end = (k / dim + 1) * dim;
-          float best = -1.f;
-          for (int r = k; r < end; ++r) {
-            const float4 v = W[r * XC_LD + k];
-            const float a = fabsf(v.x) + fabsf(v.y);
-            if (a > best) { best = a; p = r; }
-          }
-          s_perm[k] = p;
-        }
-        p = __shfl_sync(0xffffffffu, p, 0);
-        if (p != k)
-          for (int j = lane; j < K; j += 32) {
-            const float4 t = W[k * XC_LD + j];
-            W[k * XC_LD + j] = W[p * XC_LD + j];
-            W[p * XC_LD + j] = t;
-          }
+        if (lane < dim * dim) s_pb[lane] = Wf[(b0 + lane % dim) * XC_LD + b0 + lane / dim];   // column-major P
         __syncwarp();
-        for (int j = lane; j < K; j += 32) {
-          s_row[j] = W[k * XC_LD + j];
-          s_col[j] = W[j * XC_LD + k];
-        }
-        if (lane == 0) {
-          const dfc piv = dg_dfc(W[k * XC_LD + k]);
-          if (piv.re.hi == 0.f && piv.im.hi == 0.f) {
-            s_fail = 1;
-            s_inv = dfc_zero();
-          } else {
-            s_inv = dfc_inv(piv);
-          }
-          const int b = k / dim;
-          dfc dt = dfc_mul(dg_dfc(s_det[b]), piv);
-          if (p != k) dt = dfc{df_neg(dt.re), df_neg(dt.im)};
-          s_det[b] = dfc_dg(dt);
-        }
+        const float2 det = wf_det(dim, s_pb, lane);
+        if (lane == 0 && !(det.x * det.x + det.y * det.y > 0.f)) atomicExch(d.err, PQMC_ERR_SINGULAR);
+        wf_inverse(dim, s_pb, det, lane);   // s_pb <- P^-1
+      }
+      for (int e = tid; e < dim * K; e += XC_THREADS) {   // pivot rows and pivot columns before the step
+        const int m = e / K, j = e % K;
+        s_row[m * UM_KP + j] = Wf[(b0 + m) * XC_LD + j];
+        s_col[m * UM_KP + j] = Wf[j * XC_LD + b0 + m];
       }
       __syncthreads();
       if (ri < K) {
-        const dfc inv = s_inv;
-        if (ri == k) {
-          for (int j = cg; j < K; j += 8)
-            W[k * XC_LD + j] = j == k ? dfc_dg(inv) : dfc_dg(dfc_mul(dg_dfc(s_row[j]), inv));
-        } else {
-          const dfc f = dfc_mul(dg_dfc(s_col[ri]), inv);
-          for (int j = cg; j < K; j += 8) {
-            if (j == k) W[ri * XC_LD + k] = dfc_dg(dfc{df_neg(f.re), df_neg(f.im)});
-            else W[ri * XC_LD + j] = dfc_dg(dfc_fms(dg_dfc(W[ri * XC_LD + j]), f, dg_dfc(s_row[j])));
+        const bool piv_row = ri >= b0 && ri < b0 + dim;
+        float2 f[4];   // piv_row: row ri - b0 of P^-1; else F_ri = W(ri, bb) P^-1
+#pragma unroll
+        for (int n = 0; n < 4; ++n) {
+          f[n] = make_float2(0.f, 0.f);
+          if (n >= dim) continue;
+          if (piv_row) {
+            f[n] = s_pb[(ri - b0) + dim * n];
+          } else {
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+              if (m < dim) f[n] = fcfma(s_col[m * UM_KP + ri], s_pb[m + dim * n], f[n]);
           }
+        }
+        for (int j = cg; j < K; j += 8) {
+          float2 v;
+          if (j >= b0 && j < b0 + dim) {
+            v = piv_row ? f[j - b0] : make_float2(-f[j - b0].x, -f[j - b0].y);
+          } else {
+            v = piv_row ? make_float2(0.f, 0.f) : Wf[ri * XC_LD + j];
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+              if (m < dim) {
+                const float2 r = s_row[m * UM_KP + j];
+                v = piv_row ? fcfma(f[m], r, v) : fsb(v, fm(f[m], r));
+              }
+          }
+          Wf[ri * XC_LD + j] = v;
         }
       }
       __syncthreads();
     }
-    // undo the row interchanges on the columns of the inverse
-    for (int k = K - 1; k >= 0; --k) {
-      const int p = s_perm[k];
-      if (p != k) {   // uniform
-        for (int i = tid; i < K; i += XC_THREADS) {
-          const float4 t = W[i * XC_LD + k];
-          W[i * XC_LD + k] = W[i * XC_LD + p];
-          W[i * XC_LD + p] = t;
-        }
-        __syncthreads();
-      }
-    }
-    // M = Delta_S W^-1, block row by block row in place
-    for (int it = tid; it < nb * K; it += XC_THREADS) {
-      const int jb = it / K, c = it % K;
-      dfc w[4], m[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-        if (a < dim) w[a] = dg_dfc(W[(jb * dim + a) * XC_LD + c]);
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        if (a >= dim) break;
-        m[a] = dfc_zero();
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-          if (b < dim) m[a] = dfc_mac(m[a], dg_dfc(s_dl[jb * 16 + a + dim * b]), w[b]);
-      }
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-        if (a < dim) W[(jb * dim + a) * XC_LD + c] = dfc_dg(m[a]);
-    }
-    __syncthreads();
-    xc_write_b1(d, W, K, tid);
-    // ln_cw += sum_j log Re(R_j^ncopy) (|R_j|^2 under TR_weight), the
-    // weight update of src/mod_update.f90:102-104,153 with the exact ratios;
-    // the scan's FP32 determinants are compared with them
-    if (warp == 0) {
-      double lsum = 0.0, rel = 0.0;
-      int flips = 0;
-      for (int b = lane; b < nb; b += 32) {
-        const dfc dt = dg_dfc(s_det[b]);
-        const double dr = (double)dt.re.hi + (double)dt.re.lo, di = (double)dt.im.hi + (double)dt.im.lo;
-        double rr = dr, ri2 = di;
-        if (d.tr_weight) { rr = dr * dr + di * di; ri2 = 0.0; }
-        double ar = 1.0, ai = 0.0;
-        for (int c = 0; c < d.ncopy; ++c) {
-          const double tr = ar * rr - ai * ri2;
-          ai = ar * ri2 + ai * rr;
-          ar = tr;
-        }
-        lsum += log(ar);
-        const float2 f = d.acc_detf[b];
-        const double m2 = dr * dr + di * di;
-        const double ex = sqrt(((double)f.x - dr) * ((double)f.x - dr) + ((double)f.y - di) * ((double)f.y - di));
-        rel = fmax(rel, m2 > 0.0 ? ex / sqrt(m2) : 0.0);
-        if (m2 < d.acc_thr[b]) ++flips;
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-        rel = fmax(rel, __shfl_down_sync(0xffffffffu, rel, o));
-        flips += __shfl_down_sync(0xffffffffu, flips, o);
-      }
-      if (lane == 0) {
-        d.sc->ln_cw = cadd(d.sc->ln_cw, mk(lsum));
-        d.sc->err_ratio_max = fmax(d.sc->err_ratio_max, rel);
-        d.sc->n_flip += flips;
-        if (s_fail) {
-          d.sc->status = PQMC_ERR_SINGULAR;
-          atomicExch(d.err, PQMC_ERR_SINGULAR);
-        }
-      }
-    }
+    for (int e = tid; e < K * K; e += XC_THREADS) d.v0[(e / K) * XC_LD + e % K] = Wf[(e / K) * XC_LD + e % K];
     return;
   }
   if ((int)blockIdx.x <= n_a) {
@@ -375,6 +257,153 @@ __global__ void __launch_bounds__(XC_THREADS) k_xcore(const XDesc* X, int dim, i
       *reinterpret_cast<__nv_bfloat16*>(im + um_off(cc, UM_KP + k, nrg)) = __float2bfloat16_rn(-qi[s]);
       *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, k, nrg)) = __float2bfloat16_rn(qi[s]);
       *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, UM_KP + k, nrg)) = __float2bfloat16_rn(qr[s]);
+    }
+  }
+}
+
+// acc += a * b for a double-float real a and an FP32 b: the product's high
+// part (exact with its FMA error term) enters acc.hi by a two-sum, the
+// rounding errors and a.lo * b go to acc.lo (not renormalised)
+__device__ __forceinline__ void df_mac_f(float& h, float& l, float ah, float al, float b) {
+  const float p = __fmul_rn(ah, b);
+  const float e = __fmaf_rn(ah, b, -p);
+  const df s = two_sum(h, p);
+  h = s.hi;
+  l = __fmaf_rn(al, b, __fadd_rn(l, __fadd_rn(s.lo, e)));
+}
+
+__global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim) {
+  __shared__ XDesc sd;
+  __shared__ int s_ce[XR_W];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ int s_fail;
+  extern __shared__ __align__(16) unsigned char xr_dyn[];
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    sd = X[blockIdx.y];
+    s_fail = 0;
+    mbar_init(&s_bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const XDesc& d = sd;
+  const int K = *d.kcount;
+  if (K == 0) return;
+  const int nb = K / dim;
+  const int j0 = blockIdx.x * XR_W;   // this CTA's columns j0 .. j0 + XR_W - 1 of M
+  float4* W = reinterpret_cast<float4*>(xr_dyn);                     // [K][XC_LD] double-float W
+  float4* s_dl = W + (size_t)XC_LD * XC_LD;                           // [n_acc][16]
+  float4* Rs = s_dl + 16 * UM_KP;                                     // [K][XR_W] residual, then V1, then M
+  float2* V = reinterpret_cast<float2*>(Rs + (size_t)UM_KP * XR_W);   // [K][XC_LD] V0
+  if (tid == 0) {   // the first K rows of W and V0 (contiguous) and the Delta records by bulk copies
+    const uint32_t bw = (uint32_t)(sizeof(float4) * XC_LD * K), bv = (uint32_t)(sizeof(float2) * XC_LD * K);
+    const uint32_t bd = (uint32_t)(sizeof(float4) * 16 * nb);
+    fence_proxy_async_global();
+    mbar_arrive_tx(&s_bar, bw + bv + bd);
+    bulk_g2s(W, d.wdf, bw, &s_bar);
+    bulk_g2s(V, d.v0, bv, &s_bar);
+    bulk_g2s(s_dl, d.acc_delta, bd, &s_bar);
+    if (!mbar_wait_bounded(&s_bar, 0)) {
+      s_fail = 1;
+      mbar_wait_bounded(&s_bar, 0);   // a second bounded wait for the copies in flight
+    }
+  }
+  __syncthreads();
+  if (s_fail) {
+    if (tid == 0) atomicExch(d.err, PQMC_ERR_TIMEOUT);
+    return;
+  }
+  // residual R = I - W V0 on this slab, one entry per thread (row ri, column cq)
+  const int ri = tid % UM_KP, cq = tid / UM_KP;
+  const int j = j0 + cq;
+  if (ri < K) {
+    float rh0 = 0.f, rl0 = 0.f, rh1 = 0.f, rl1 = 0.f;
+    for (int k = 0; k < K; ++k) {
+      const float4 w = W[ri * XC_LD + k];   // {re_hi, im_hi, re_lo, im_lo}
+      const float2 v = j < K ? V[k * XC_LD + j] : make_float2(0.f, 0.f);
+      df_mac_f(rh0, rl0, w.x, w.z, v.x);     // re += wr vr
+      df_mac_f(rh0, rl0, -w.y, -w.w, v.y);   //       - wi vi
+      df_mac_f(rh1, rl1, w.x, w.z, v.y);     // im += wr vi
+      df_mac_f(rh1, rl1, w.y, w.w, v.x);     //       + wi vr
+    }
+    const df wr = quick_two_sum(rh0, rl0), wi = quick_two_sum(rh1, rl1);
+    const df rr = df_sub(df{ri == j ? 1.f : 0.f, 0.f}, wr);   // I - W V0
+    Rs[ri * XR_W + cq] = make_float4(rr.hi, -wi.hi, rr.lo, -wi.lo);
+  }
+  __syncthreads();
+  // V1 = V0 + V0 R on the slab (R is small: its FP32 rounding suffices)
+  float4 v1 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (ri < K) {
+    float2 s = make_float2(0.f, 0.f);
+    for (int k = 0; k < K; ++k) s = fcfma(V[ri * XC_LD + k], hi2(Rs[k * XR_W + cq]), s);
+    const float2 v0 = j < K ? V[ri * XC_LD + j] : make_float2(0.f, 0.f);
+    const df a = two_sum(v0.x, s.x), b = two_sum(v0.y, s.y);
+    v1 = make_float4(a.hi, b.hi, a.lo, b.lo);
+  }
+  __syncthreads();
+  if (ri < K) Rs[ri * XR_W + cq] = v1;
+  __syncthreads();
+  // M = Delta_S V1 block row by block row
+  for (int it = tid; it < nb * XR_W; it += XR_THREADS) {
+    const int jb = it / XR_W, jl = it % XR_W;
+    dfc w[4], m[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+      if (a < dim) w[a] = dg_dfc(Rs[(jb * dim + a) * XR_W + jl]);
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      if (a >= dim) break;
+      m[a] = dfc_zero();
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if (b < dim) m[a] = dfc_mac(m[a], dg_dfc(s_dl[jb * 16 + a + dim * b]), w[b]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+      if (a < dim) Rs[(jb * dim + a) * XR_W + jl] = dfc_dg(m[a]);
+  }
+  __syncthreads();
+  // Ozaki slices of M's columns j0.. (output columns of X): B' re row c =
+  // [Mr | -Mi], im row 64 + c = [Mi | Mr]; columns at or past K are zero
+  if (tid < XR_W) {
+    float mx = 0.f;
+    if (j0 + tid < K)
+      for (int k = 0; k < K; ++k) {
+        const float4 v = Rs[k * XR_W + tid];
+        mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+      }
+    s_ce[tid] = oz_exp(mx);
+  }
+  __syncthreads();
+  const int K16 = (K + 15) & ~15, KG = K16 / 8;
+  const int ns = d.ns;
+  for (int it = tid; it < XR_W * KG; it += XR_THREADS) {
+    const int jl = it % XR_W, kg = it / XR_W, c = j0 + jl;
+    float rs[OZ_S][8], is[OZ_S][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = kg * 8 + u;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (c < K && k < K) v = Rs[k * XR_W + jl];
+      float qr[OZ_S], qi[OZ_S];
+      oz_split(v.x, v.z, s_ce[jl], qr);
+      oz_split(v.y, v.w, s_ce[jl], qi);
+#pragma unroll
+      for (int q = 0; q < OZ_S; ++q) {
+        rs[q][u] = qr[q];
+        is[q][u] = qi[q];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < OZ_S; ++q) {
+      unsigned char* im = d.img + (size_t)oz_slot_b1(ns, q) * UM_IMG;
+      float ni[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) ni[u] = -is[q][u];
+      *reinterpret_cast<uint4*>(im + um_off(c, kg * 8, 16)) = oz_pack8(rs[q]);
+      *reinterpret_cast<uint4*>(im + um_off(c, UM_KP + kg * 8, 16)) = oz_pack8(ni);
+      *reinterpret_cast<uint4*>(im + um_off(64 + c, kg * 8, 16)) = oz_pack8(is[q]);
+      *reinterpret_cast<uint4*>(im + um_off(64 + c, UM_KP + kg * 8, 16)) = oz_pack8(rs[q]);
     }
   }
 }
@@ -594,7 +623,8 @@ __global__ void __launch_bounds__(256, 1) k_xgemm(const XDesc* X, int parity) {
 }
 
 int exact_setup() {
-  PQMC_CUDA(raise_dyn_smem(k_xcore, (int)XC_SMEM));
+  PQMC_CUDA(raise_dyn_smem(k_xinv, (int)XI_SMEM));
+  PQMC_CUDA(raise_dyn_smem(k_xres, (int)XR_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xgemm<0>, XG_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xgemm<1>, XG_SMEM));
   return PQMC_OK;
@@ -602,8 +632,10 @@ int exact_setup() {
 
 int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi) {
   const int n_a = (ns + XC_THREADS - 1) / XC_THREADS, n_b = (ns + XC_THREADS / 32 - 1) / (XC_THREADS / 32);
-  PQMC_CUDA(launch_at(k_xcore, dim3(1 + n_a + n_b, C), dim3(XC_THREADS), XC_SMEM, st, prio, prio_hi, d_x, dim, parity,
+  PQMC_CUDA(launch_at(k_xinv, dim3(1 + n_a + n_b, C), dim3(XC_THREADS), XI_SMEM, st, prio, prio_hi, d_x, dim, parity,
                       n_a));
+  PQMC_LAUNCHED();
+  PQMC_CUDA(launch_at(k_xres, dim3(XR_CTAS, C), dim3(XR_THREADS), XR_SMEM, st, prio, prio_hi, d_x, dim));
   PQMC_LAUNCHED();
   return PQMC_OK;
 }
@@ -633,10 +665,9 @@ __global__ void k_x_from_df(const float4* a, cplx* b, long n) {
 }
 }  // namespace pqmc
 
-extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g,
-                                       double* lncw_out) {
+extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g) {
   using namespace pqmc;
-  if (!sites || !delta || !g || !lncw_out || dim < 1 || dim > 4 || k < dim || k > UM_KP || k % dim || ns < k ||
+  if (!sites || !delta || !g || dim < 1 || dim > 4 || k < dim || k > UM_KP || k % dim || ns < k ||
       ns > 4096) {
     set_error("exact_update_check: need 1 <= dim <= 4, dim <= k <= %d, k %% dim == 0, k <= ns <= 4096", UM_KP);
     return PQMC_ERR_ARG;
@@ -653,8 +684,8 @@ extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites,
   float4* d_g = nullptr;
   int* d_site = nullptr;
   float4* d_dl = nullptr;
-  float2* d_detf = nullptr;
-  double* d_thr = nullptr;
+  float4* d_w = nullptr;
+  float2* d_v0 = nullptr;
   int* d_k = nullptr;
   unsigned char* d_img = nullptr;
   DevScalars* d_sc = nullptr;
@@ -667,8 +698,8 @@ extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites,
     PQMC_CUDA(cudaMalloc((void**)&d_g, sizeof(float4) * n2));
     PQMC_CUDA(cudaMalloc((void**)&d_site, sizeof(int) * k));
     PQMC_CUDA(cudaMalloc((void**)&d_dl, sizeof(float4) * 16 * nb));
-    PQMC_CUDA(cudaMalloc((void**)&d_detf, sizeof(float2) * nb));
-    PQMC_CUDA(cudaMalloc((void**)&d_thr, sizeof(double) * nb));
+    PQMC_CUDA(cudaMalloc((void**)&d_w, sizeof(float4) * UM_KP * UM_KP));
+    PQMC_CUDA(cudaMalloc((void**)&d_v0, sizeof(float2) * UM_KP * UM_KP));
     PQMC_CUDA(cudaMalloc((void**)&d_k, sizeof(int)));
     PQMC_CUDA(cudaMalloc((void**)&d_img, oz_chain_bytes(ns)));
     PQMC_CUDA(cudaMalloc((void**)&d_sc, sizeof(DevScalars)));
@@ -679,8 +710,6 @@ extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites,
     PQMC_CUDA(cudaMemset(d_sc, 0, sizeof(DevScalars)));
     PQMC_CUDA(cudaMemset(d_err, 0, sizeof(int)));
     PQMC_CUDA(cudaMemset(d_nf, 0, sizeof(unsigned long long)));
-    PQMC_CUDA(cudaMemset(d_detf, 0, sizeof(float2) * nb));
-    PQMC_CUDA(cudaMemset(d_thr, 0, sizeof(double) * nb));
     PQMC_CUDA(cudaMemcpy(d_g64, g, sizeof(cplx) * n2, cudaMemcpyHostToDevice));
     PQMC_CUDA(cudaMemcpy(d_site, sites, sizeof(int) * k, cudaMemcpyHostToDevice));
     PQMC_CUDA(cudaMemcpy(d_k, &k, sizeof(int), cudaMemcpyHostToDevice));
@@ -707,8 +736,8 @@ extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites,
     x.kcount = d_k;
     x.acc_site = d_site;
     x.acc_delta = d_dl;
-    x.acc_detf = d_detf;
-    x.acc_thr = d_thr;
+    x.wdf = d_w;
+    x.v0 = d_v0;
     x.img = d_img;
     x.sc = d_sc;
     x.err = d_err;
@@ -727,9 +756,6 @@ extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites,
       return herr;
     }
     PQMC_CUDA(cudaMemcpy(g, d_g64, sizeof(cplx) * n2, cudaMemcpyDeviceToHost));
-    DevScalars hs;
-    PQMC_CUDA(cudaMemcpy(&hs, d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
-    *lncw_out = hs.ln_cw.x;
     return PQMC_OK;
   };
   st = run();
@@ -737,8 +763,8 @@ extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites,
   cudaFree(d_g);
   cudaFree(d_site);
   cudaFree(d_dl);
-  cudaFree(d_detf);
-  cudaFree(d_thr);
+  cudaFree(d_w);
+  cudaFree(d_v0);
   cudaFree(d_k);
   cudaFree(d_img);
   cudaFree(d_sc);

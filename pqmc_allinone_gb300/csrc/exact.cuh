@@ -8,13 +8,14 @@
 //
 //   G <- G + G(:,S) M (E_S - G(S,:)),   M = Delta_S W^-1,  W = I + G(S,S) Delta_S,
 //
-// with Delta_S block diagonal.  The block pivots of W in acceptance order
+// with Delta_S block diagonal.  (The block pivots of W in acceptance order
 // are the sequential ratio matrices R_j = I + Geff_j(S_j,S_j) Delta_j of the
-// reference, so det W = prod_j det R_j (the weight ln_cw).  The update is
-// evaluated from the double-float G, never from the scan's FP32 panels:
-//   k_xcore   W^-1 by Gauss-Jordan in double-float (pivots within each
-//             block), M, the exact per-move ratios and ln_cw; and the Ozaki
-//             slices of G(:,S), of M and of Z = E_S - G(S,:);
+// reference.)  The update is evaluated from the double-float G, never from
+// the scan's FP32 panels:
+//   k_xinv    W in double-float and the FP32 inverse V0 of its rounding; the
+//             Ozaki slices of G(:,S) and of Z = E_S - G(S,:);
+//   k_xres    one Newton step V1 = V0 + V0 (I - W V0) with a double-float
+//             residual, M = Delta_S V1 and the Ozaki slices of M;
 //   k_xgemm   X = G(:,S) M, then G += X Z, on the tensor cores: every
 //             operand is cut into OZ_S BF16 slices on a per-row (per-column)
 //             power-of-two grid, so that the products of one slice level
@@ -38,8 +39,8 @@ struct XDesc {
   const int* kcount;       // panel columns of the round (written by the scan)
   int* acc_site;           // (kmax) accepted sites, dim per move, in acceptance order
   float4* acc_delta;       // (kmax) 16 entries per accepted move: its Delta (double-float)
-  float2* acc_detf;        // (kmax) the scan's FP32 det R of each accepted move
-  double* acc_thr;         // (kmax) the Metropolis threshold of |det R|^2 of each move
+  float4* wdf;             // (kmax x kmax) W in double-float, row i at wdf + i*kmax
+  float2* v0;              // (kmax x kmax) FP32 inverse of W
   unsigned char* img;      // slice images (oz_chain_bytes)
   DevScalars* sc;
   int* err;
@@ -58,9 +59,9 @@ __host__ __device__ __forceinline__ size_t oz_chain_bytes(int ns) {
   return (size_t)(2 * um_rtiles(ns) + 1 + um_ctiles(ns)) * OZ_S * UM_IMG;
 }
 
-// The exact update of one round for C chains, in two launches on `st`:
-// exact_core (W^-1, M, ln_cw and the operand slices) and exact_products (the
-// two tensor-core products).  `prio` marks the launches with priority
+// The exact update of one round for C chains: exact_core (two launches:
+// W^-1, M and the operand slices) and exact_products (two launches: the
+// tensor-core products).  `prio` marks the launches with priority
 // `prio_hi` (kept as node priorities when the stream is being captured).
 int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi);
 int exact_products(const XDesc* d_x, int C, int ns, int parity, cudaStream_t st, bool prio, int prio_hi);

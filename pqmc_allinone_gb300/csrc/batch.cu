@@ -964,40 +964,52 @@ __global__ void __launch_bounds__(256, 2) k_bflush_um(const BDesc* D, const unsi
 constexpr int WRAP_R = 32, WRAP_C = 4;
 
 // the wrap of one DIM x DIM block of G (rows of one cover item, columns of
-// another) in double-float: corr = (A - I)(G + G(B - I)) + G(B - I), every
-// product formed error-free, added to G.  am(a, k) and bm(k, b) read the
-// double-float (A - I) and (B - I) entries; out(a, b, v) stores entry (a, b).
-template <int DIM, typename AM, typename BM, typename OUT>
-__device__ __forceinline__ void wrap_block_df(const float4 (&gd)[DIM][DIM], int dr, int dc, AM am, BM bm, OUT out) {
-  // one column b of the block at a time: G (B - I) of column b, then the
-  // correction of column b
+// another) in double-float, in two one-sided passes: T = G B row by row,
+// then G' = A T column by column, with A = I + am, B = I + bm; every entry
+// starts from its identity term and takes DIM error-free products.  get(a,
+// b) / put(a, b, v) read and write entry (a, b) of the block (in place);
+// am(a, k), bm(k, b) read the double-float (A - I), (B - I).  The outer
+// loops are not unrolled: the fully unrolled form overflowed the
+// instruction cache.
+template <int DIM, typename GET, typename PUT, typename AM, typename BM>
+__device__ __forceinline__ void wrap2_df(int dr, int dc, GET get, PUT put, AM am, BM bm) {
+#pragma unroll 1
+  for (int a = 0; a < dr; ++a) {
+    float4 g[DIM], t[DIM];
 #pragma unroll
-  for (int b = 0; b < DIM; ++b) {
-    if (b >= dc) break;
-    dfc gb[DIM];
+    for (int k = 0; k < DIM; ++k) g[k] = k < dc ? get(a, k) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int a = 0; a < DIM; ++a) {
-      dfc acc = dfc_zero();
+    for (int b = 0; b < DIM; ++b) {
+      dfc acc = dfc_from_dg(g[b]);
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
         const float4 v = bm(k, b);
-        acc = dfc_fms(acc, dfc{df{-gd[a][k].x, -gd[a][k].z}, df{-gd[a][k].y, -gd[a][k].w}}, dfc{df{v.x, v.z}, df{v.y, v.w}});
+        acc = dfc_fms(acc, dfc{df{-g[k].x, -g[k].z}, df{-g[k].y, -g[k].w}}, dfc_from_dg(v));
       }
-      gb[a] = acc;
+      t[b] = dg_from_dfc(acc);
     }
 #pragma unroll
+    for (int b = 0; b < DIM; ++b)
+      if (b < dc) put(a, b, t[b]);
+  }
+#pragma unroll 1
+  for (int b = 0; b < dc; ++b) {
+    float4 t[DIM], o[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) t[k] = k < dr ? get(k, b) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
     for (int a = 0; a < DIM; ++a) {
-      if (a >= dr) break;
-      dfc corr = gb[a];
+      dfc acc = dfc_from_dg(t[a]);
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
         const float4 v = am(a, k);
-        const dfc x = dfc_add(dfc{df{gd[k][b].x, gd[k][b].z}, df{gd[k][b].y, gd[k][b].w}}, gb[k]);
-        corr = dfc_fms(corr, dfc{df{-v.x, -v.z}, df{-v.y, -v.w}}, x);
+        acc = dfc_fms(acc, dfc{df{-v.x, -v.z}, df{-v.y, -v.w}}, dfc_from_dg(t[k]));
       }
-      const dfc n = dfc_add(dfc{df{gd[a][b].x, gd[a][b].z}, df{gd[a][b].y, gd[a][b].w}}, corr);
-      out(a, b, make_float4(n.re.hi, n.im.hi, n.re.lo, n.im.lo));
+      o[a] = dg_from_dfc(acc);
     }
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+      if (a < dr) put(a, b, o[a]);
   }
 }
 
@@ -1086,9 +1098,19 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
   __syncthreads();
   if (!live) return;
   if (DF) {
-    wrap_block_df<DIM>(gd, dr, dc, [&](int a, int k) { return s_am[a + DIM * k][lr]; },
-                       [&](int k, int b) { return s_bm[k + DIM * b][lc]; },
-                       [&](int a, int b, float4 v) { gout[Sr[a] + (size_t)ns * Sc[b]] = v; });
+    float4 blk[DIM * DIM];   // the block, entry (a, b) at a + DIM b
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) blk[a + DIM * b] = gd[a][b];
+    wrap2_df<DIM>(dr, dc, [&](int a, int b) { return blk[a + DIM * b]; },
+                  [&](int a, int b, float4 v) { blk[a + DIM * b] = v; },
+                  [&](int a, int k) { return s_am[a + DIM * k][lr]; }, [&](int k, int b) { return s_bm[k + DIM * b][lc]; });
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int a = 0; a < DIM; ++a)
+        if (a < dr && b < dc) gout[Sr[a] + (size_t)ns * Sc[b]] = blk[a + DIM * b];
     return;
   }
   // corr = (A - I) (G B) + G (B - I) = (A - I) G + (A - I) G (B - I) + G (B - I)
@@ -1242,18 +1264,19 @@ __global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, i
 #pragma unroll
     for (int k = 0; k < DIM; ++k) Sr[k] = k < dr ? s_site[4 * ir + k] : 0;
     float4* col = s_col + (size_t)icl * DIM * ns;
+    if (DF) {
+      wrap2_df<DIM>(dr, dc, [&](int a, int b) { return col[(size_t)b * ns + Sr[a]]; },
+                    [&](int a, int b, float4 v) { col[(size_t)b * ns + Sr[a]] = v; },
+                    [&](int a, int k) { return s_am[(size_t)(a + DIM * k) * n_items + ir]; },
+                    [&](int k, int b) { return s_bm[(size_t)(k + DIM * b) * WRAPC_C + icl]; });
+      continue;
+    }
     float4 gd[DIM][DIM];
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
 #pragma unroll
       for (int a = 0; a < DIM; ++a)
         gd[a][b] = (a < dr && b < dc) ? col[(size_t)b * ns + Sr[a]] : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (DF) {
-      wrap_block_df<DIM>(gd, dr, dc, [&](int a, int k) { return s_am[(size_t)(a + DIM * k) * n_items + ir]; },
-                         [&](int k, int b) { return s_bm[(size_t)(k + DIM * b) * WRAPC_C + icl]; },
-                         [&](int a, int b, float4 v) { col[(size_t)b * ns + Sr[a]] = v; });
-      continue;
-    }
     // corr = (A - I) (G B) + G (B - I), as in k_bwrap
     float2 gb[DIM][DIM];   // G (B - I)
 #pragma unroll

@@ -67,7 +67,7 @@ __device__ __forceinline__ dfc dfc_inv(dfc a) {
 
 // ---------------------------------------------------------------------------
 // M = Delta_S W^-1, W = I + G(S,S) Delta_S, in two launches:
-//   k_xinv  (CTA 0 of each chain) forms W in double-float and inverts its
+//   k_xinv  (one CTA per chain) forms W in double-float and inverts its
 //           FP32 rounding by Gauss-Jordan over the moves' dim x dim blocks
 //           (the block pivots are the moves' ratio matrices R_j, each
 //           inverted by its adjugate): V0 = W^-1 to ~1e-6;
@@ -76,10 +76,10 @@ __device__ __forceinline__ dfc dfc_inv(dfc a) {
 //           double-float from every product's exact parts, so V1 = W^-1 to
 //           ~|I - W V0|^2; then M = Delta_S V1 and the Ozaki slices of M's
 //           columns (the B operand of X = G(:,S) M).
-// The other CTAs of k_xinv cut the rows of G(:,S) (the A operand of X) and
-// the columns of Z = E_S - G(S,:) (the B operand of the flush, a warp per
-// column); these depend on G and S only.
-constexpr int XC_THREADS = 512;
+// The CTAs of k_xres past the slabs cut the rows of G(:,S) (the A operand of
+// X) and the columns of Z = E_S - G(S,:) (the B operand of the flush, a warp
+// per column); these depend on G and S only.
+constexpr int XC_THREADS = 1024;
 constexpr int XC_LD = UM_KP;   // leading dimension of the K x K matrices
 constexpr int XR_CTAS = 8;     // column slabs of the Newton step per chain
 constexpr int XR_W = UM_KP / XR_CTAS;
@@ -89,7 +89,7 @@ constexpr size_t XI_SMEM = sizeof(float4) * 16 * UM_KP + sizeof(float2) * ((size
 constexpr size_t XR_SMEM = sizeof(float4) * ((size_t)XC_LD * XC_LD + 16 * UM_KP + (size_t)UM_KP * XR_W) +
                            sizeof(float2) * (size_t)XC_LD * XC_LD;
 
-__global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim, int parity, int n_a) {
+__global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim, int parity) {
   __shared__ XDesc sd;
   __shared__ float2 s_pb[16];
   extern __shared__ __align__(16) unsigned char xc_dyn[];
@@ -101,8 +101,7 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
   if (K == 0) return;
   const int ns = d.ns;
   const float4* G = parity ? d.g_alt : d.g;
-  const int K16 = (K + 15) & ~15;
-  if (blockIdx.x == 0) {
+  {
     float4* s_dl = reinterpret_cast<float4*>(xc_dyn);                 // [n_acc][16] Delta blocks
     float2* Wf = reinterpret_cast<float2*>(s_dl + 16 * UM_KP);        // [K][XC_LD] FP32 W, inverted in place
     float2* s_row = Wf + (size_t)XC_LD * XC_LD;                       // [dim][UM_KP] pivot rows
@@ -135,7 +134,8 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
     // FP32 Gauss-Jordan in place by blocks of the moves: the pivot block P is
     // inverted by its adjugate on 16 lanes, the multipliers F_i = W(i, bb)
     // P^-1 are formed once per row
-    const int ri = tid / 8, cg = tid % 8;   // row ri, columns cg, cg + 8, ...
+    constexpr int CG = XC_THREADS / UM_KP;      // threads per row
+    const int ri = tid / CG, cg = tid % CG;   // row ri, columns cg, cg + CG, ...
     for (int b = 0; b < nb; ++b) {
       const int b0 = b * dim;
       if (warp == 0) {
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
               if (m < dim) f[n] = fcfma(s_col[m * UM_KP + ri], s_pb[m + dim * n], f[n]);
           }
         }
-        for (int j = cg; j < K; j += 8) {
+        for (int j = cg; j < K; j += CG) {
           float2 v;
           if (j >= b0 && j < b0 + dim) {
             v = piv_row ? f[j - b0] : make_float2(-f[j - b0].x, -f[j - b0].y);
@@ -187,9 +187,17 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
     for (int e = tid; e < K * K; e += XC_THREADS) d.v0[(e / K) * XC_LD + e % K] = Wf[(e / K) * XC_LD + e % K];
     return;
   }
-  if ((int)blockIdx.x <= n_a) {
+}
+
+// the Ozaki slices of G(:,S) (the A operand of X = G(:,S) M; CTA index
+// cta <= n_a, a thread per row) and of Z = E_S - G(S,:) (the B operand of
+// the flush; a warp per column); they depend on G and S only
+__device__ __forceinline__ void x_slice_gz(const XDesc& d, const float4* G, int K, int cta, int n_a, int tid) {
+  const int ns = d.ns, lane = tid & 31, warp = tid >> 5;
+  const int K16 = (K + 15) & ~15;
+  if (cta <= n_a) {
     // ---- rows of G(:,S): A operand of X = G(:,S) M ------------------------
-    const int r = ((int)blockIdx.x - 1) * XC_THREADS + tid;
+    const int r = (cta - 1) * XR_THREADS + tid;
     if (r >= ns) return;
     const int* S = d.acc_site;
     float m = 0.f;
@@ -224,7 +232,7 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
     return;
   }
   // ---- columns of Z = E_S - G(S,:): B operand of the flush, a warp each ----
-  const int c = ((int)blockIdx.x - 1 - n_a) * (XC_THREADS / 32) + warp;
+  const int c = (cta - 1 - n_a) * (XR_THREADS / 32) + warp;
   if (c >= ns) return;
   dfc z[2];
   float m = 0.f;
@@ -272,7 +280,7 @@ __device__ __forceinline__ void df_mac_f(float& h, float& l, float ah, float al,
   l = __fmaf_rn(al, b, __fadd_rn(l, __fadd_rn(s.lo, e)));
 }
 
-__global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim) {
+__global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim, int parity, int n_a) {
   __shared__ XDesc sd;
   __shared__ int s_ce[XR_W];
   __shared__ __align__(8) uint64_t s_bar;
@@ -289,6 +297,10 @@ __global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim)
   const XDesc& d = sd;
   const int K = *d.kcount;
   if (K == 0) return;
+  if ((int)blockIdx.x >= XR_CTAS) {
+    x_slice_gz(d, parity ? d.g_alt : d.g, K, (int)blockIdx.x - XR_CTAS + 1, n_a, tid);
+    return;
+  }
   const int nb = K / dim;
   const int j0 = blockIdx.x * XR_W;   // this CTA's columns j0 .. j0 + XR_W - 1 of M
   float4* W = reinterpret_cast<float4*>(xr_dyn);                     // [K][XC_LD] double-float W
@@ -631,11 +643,11 @@ int exact_setup() {
 }
 
 int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi) {
-  const int n_a = (ns + XC_THREADS - 1) / XC_THREADS, n_b = (ns + XC_THREADS / 32 - 1) / (XC_THREADS / 32);
-  PQMC_CUDA(launch_at(k_xinv, dim3(1 + n_a + n_b, C), dim3(XC_THREADS), XI_SMEM, st, prio, prio_hi, d_x, dim, parity,
-                      n_a));
+  const int n_a = (ns + XR_THREADS - 1) / XR_THREADS, n_b = (ns + XR_THREADS / 32 - 1) / (XR_THREADS / 32);
+  PQMC_CUDA(launch_at(k_xinv, dim3(1, C), dim3(XC_THREADS), XI_SMEM, st, prio, prio_hi, d_x, dim, parity));
   PQMC_LAUNCHED();
-  PQMC_CUDA(launch_at(k_xres, dim3(XR_CTAS, C), dim3(XR_THREADS), XR_SMEM, st, prio, prio_hi, d_x, dim));
+  PQMC_CUDA(launch_at(k_xres, dim3(XR_CTAS + n_a + n_b, C), dim3(XR_THREADS), XR_SMEM, st, prio, prio_hi, d_x, dim,
+                      parity, n_a));
   PQMC_LAUNCHED();
   return PQMC_OK;
 }

@@ -28,9 +28,9 @@ _i32p = ctypes.POINTER(ctypes.c_int32)
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (no external libraries)."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    hdr = os.path.join(HERE, "..", "include", "pqmc_gb300.h")
+    hdrs = [os.path.join(HERE, "..", "include", h) for h in ("pqmc_gb300.h", "pqmc_boxmuller.h")]
     if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) > os.path.getmtime(SRC)
-            and os.path.getmtime(LIB) > os.path.getmtime(hdr)):
+            and all(os.path.getmtime(LIB) > os.path.getmtime(h) for h in hdrs)):
         return LIB
     cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB + ".tmp",
            SRC, "-lpthread"]
@@ -52,6 +52,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_time_parallel.restype = ctypes.c_double
         L.oracle_time_parallel.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_record_width.argtypes = [_vp]
+        L.oracle_gauss_parts.argtypes = [_f64p, _f64p, ctypes.c_int, _f64p]
         _LIB = L
     return _LIB
 
@@ -210,3 +211,13 @@ def rng_draw(words, n):
     out = (ctypes.c_float * n)()
     lib().oracle_rng_draw(st, n, out)
     return np.array(out[:], dtype=np.float32), list(st)
+
+
+def gauss_parts(u1: np.ndarray, u2: np.ndarray) -> np.ndarray:
+    """(log u1, cos 2 pi u2, Gaussian jump of width 1) per pair, by the
+    fixed-order Box-Muller arithmetic the CUDA kernels share (n x 3)."""
+    a = np.ascontiguousarray(u1, dtype=np.float64)
+    b = np.ascontiguousarray(u2, dtype=np.float64)
+    out = np.zeros((a.size, 3))
+    lib().oracle_gauss_parts(a.ctypes.data_as(_f64p), b.ctypes.data_as(_f64p), a.size, out.ctypes.data_as(_f64p))
+    return out

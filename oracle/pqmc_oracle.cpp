@@ -25,6 +25,7 @@
 #include <thread>
 #include <chrono>
 #include "../include/pqmc_gb300.h"
+#include "../include/pqmc_boxmuller.h"
 
 namespace {
 
@@ -551,10 +552,11 @@ static double cal_prob(const Chain& c, cd w) {
 
 static double draw_jump(Chain& c) {
   if (c.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
-    // Box-Muller on two ran2 draws (u1 in (0,1), so log is finite)
+    // Box-Muller on two ran2 draws (u1 in (0,1), so log is finite), with the
+    // fixed-order arithmetic the CUDA kernels use (bit-identical jumps)
     double u1 = (double)c.rng.rands();
     double u2 = (double)c.rng.rands();
-    return c.jump * (std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+    return pqmc_bm_gauss_jump(c.jump, u1, u2);
   }
   return c.jump * (double)c.rng.ran_sysm();
 }
@@ -1344,6 +1346,15 @@ void oracle_rng_seed_words(int seed, int32_t* out) {
   for (int k = 0; k < 3; ++k) if (out[k] < 0) out[k] = ~out[k];
   for (int k = 3; k < 5; ++k) if (out[k] == 0) out[k] = 1;
 }
+// the fixed-order Box-Muller pieces (log u1, cos 2 pi u2, jump of width 1)
+void oracle_gauss_parts(const double* u1, const double* u2, int n, double* out) {
+  for (int i = 0; i < n; ++i) {
+    out[3 * i] = pqmc_bm_log(u1[i]);
+    out[3 * i + 1] = pqmc_bm_cos2pi(u2[i]);
+    out[3 * i + 2] = pqmc_bm_gauss_jump(1.0, u1[i], u2[i]);
+  }
+}
+
 void oracle_rng_draw(int32_t* state, int n, float* out) {
   Ran2 r{state[0], state[1], state[2], state[3], state[4]};
   for (int k = 0; k < n; ++k) out[k] = r.next();

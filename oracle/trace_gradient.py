@@ -93,3 +93,66 @@ def logweight_grad_trace(m, field: np.ndarray, seed_words=None):
     lndet = logabs + np.log(sign) + 2.0 * np.sum(np.log(d))
     W = c * np.real(lndet)
     return W, grad, dets
+
+
+def logweight_grad_trace_stable(m, field: np.ndarray, seed_words=None, block: int | None = None):
+    """grad[b, t] = dW/dx_{b,t} by the same trace formula, stabilised for long
+    Lt: the right factor R and the left factor X are re-orthonormalised after
+    every slice (g = R (X R)^-1 X does not change when R is multiplied on the
+    right, or X on the left, by an invertible matrix), the right factors are
+    kept only at the first slice of every block of `block` slices (ngroup by
+    default) and rebuilt inside a block as the left factor passes through
+    it.  Memory: Lt/block + block*n_pf matrices of Ns x nelec."""
+    from oracle.oracle import OracleChain
+
+    o = OracleChain(m, field=np.asarray(field, dtype=np.float64), seed_words=seed_words, meas=False)
+    o.init_expkv()
+    _, ekv_inv = o.expkv()
+    npf, pd, mp, nt = len(m.pf), m.pdim, m.max_pla, m.ntime
+    ekv_inv = ekv_inv.reshape((pd, pd, mp, npf, nt), order="F")
+    P = np.asarray(m.slater_q, dtype=np.complex128).reshape((m.ns, m.nelec), order="F")
+    nb = int(block or m.ngroup)
+    c = float(m.spec.ncopy) * (2.0 if m.spec.tr_weight else 1.0)
+
+    def orth_cols(a):
+        return np.asfortranarray(np.linalg.qr(a)[0])
+
+    def orth_rows(a):
+        return np.asfortranarray(np.linalg.qr(a.conj().T)[0].conj().T)
+
+    ck = {}
+    r = orth_cols(P)
+    for t in range(1, nt + 1):
+        if (t - 1) % nb == 0:
+            ck[t] = r.copy(order="F")
+        for f in range(npf):
+            r = o.left_evolve(t, f + 1, r)
+        r = orth_cols(r)
+    grad = np.zeros((m.n_bf, nt))
+    x = orth_rows(P.conj().T)
+    for t0 in sorted(ck, reverse=True):
+        t1 = min(t0 + nb - 1, nt)
+        R = {}
+        r = ck[t0]
+        for t in range(t0, t1 + 1):
+            for f in range(npf):
+                r = o.left_evolve(t, f + 1, r)
+                R[(t, f)] = r
+            r = orth_cols(r)
+        for t in range(t1, t0 - 1, -1):
+            for f in range(npf - 1, -1, -1):
+                tab = m.pf[f]
+                if m.spec.pfs[f].v_exist:
+                    r = R[(t, f)]
+                    y = np.linalg.solve(x @ r, x)   # g = r y
+                    dim = tab.dim
+                    for p in range(tab.n_pla):
+                        S = np.asarray(tab.site_list[p][:dim])
+                        b = int(tab.bf_list[p])
+                        de = _dexp(o, m.expkv_kind, f, p, float(field[b, t - 1]))
+                        einv = ekv_inv[:dim, :dim, p, f, t - 1]
+                        gb = r[S, :] @ y[:, S]
+                        grad[b, t - 1] += c * np.real(np.trace(gb @ (de @ einv)))
+                x = o.right_evolve(t, f + 1, x)
+            x = orth_rows(x)
+    return grad

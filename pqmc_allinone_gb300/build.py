@@ -39,8 +39,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    hdrs = sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + [
-        os.path.join(HERE, "..", "include", "pqmc_gb300.h")]
+    hdrs = sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + sorted(
+        glob.glob(os.path.join(HERE, "..", "include", "*.h")))
     objs = [os.path.join(OUT, os.path.basename(s)[:-3] + ".o") for s in srcs]
     nv = nvcc()
 

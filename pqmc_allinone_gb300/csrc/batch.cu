@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(256) k_bprep(const BDesc* D, int pf_first, int
     double jump;
     if (M.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
       double u1 = pre[p].xnew, u2 = pre[p].dE;
-      jump = M.jump * (sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+      jump = pqmc_bm_gauss_jump(M.jump, u1, u2);   // bit-identical with the oracle
     } else {
       jump = M.jump * pre[p].xnew;
     }

@@ -6,6 +6,7 @@
 #include <stdio.h>
 #include <atomic>
 #include "../../include/pqmc_gb300.h"
+#include "../../include/pqmc_boxmuller.h"
 
 typedef double2 cplx;
 

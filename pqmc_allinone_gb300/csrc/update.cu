@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(256) k_update(DevModel M, DevScalars* sc, UpdC
       double jump;
       if (M.proposal_kind == PQMC_PROPOSAL_GAUSSIAN) {
         double u1 = __ldcg(&pre[p].xnew), u2 = __ldcg(&pre[p].dE);
-        jump = M.jump * (sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+        jump = pqmc_bm_gauss_jump(M.jump, u1, u2);   // bit-identical with the oracle
       } else {
         jump = M.jump * __ldcg(&pre[p].xnew);
       }

@@ -148,3 +148,37 @@ def test_autograd_gradcheck():
     chains = [PqmcChain(m, field=f, rng_words=SEED_WORDS)]
     x = torch.tensor(f[None], dtype=torch.float64, device="cuda", requires_grad=True)
     assert torch.autograd.gradcheck(lambda y: LogWeight.apply(y, chains), (x,), eps=H, atol=1e-5, rtol=1e-4)
+
+
+def test_c5_full_size_fd_and_trace_formula():
+    """The differentiable configuration at its size: 10x10 spin-orbit lattice
+    (Ns = 200, Nup = 100, 200 bonds), Lt = 400, dtau = 0.1, x ~ N(0, 0.5^2)
+    from seeds 5000 + i, checkpoints every ngroup = 10 slices.  For two
+    chains: central finite differences (h = 1e-6, FP64 weights of the
+    device) on 64 random entries each, and every entry against the FP64
+    trace formula on the CPU (stabilised form, oracle/trace_gradient.py).
+    The gradient is formed in FP64 throughout (no FP32 accumulation).  At
+    this size |W| is large, so the difference's roundoff, ~ a few eps |W| / h,
+    sets its tolerance: 1e-6 + 1e-6 |fd| + 50 eps |W| / h; the trace formula
+    carries no such noise and keeps 1e-9 + 1e-7 of the largest entry."""
+    from oracle.trace_gradient import logweight_grad_trace_stable
+    from pqmc_allinone_gb300 import model as M
+    spec = M.epsocz_spec(10, lam=0.8, alpha=0.3, ntime=400, ngroup=10, filling=0.5, jump_distance=0.5)
+    m = M.build_model(spec, twist_seed=11, twist=1e-3)
+    assert (m.ns, m.nelec, m.n_bf, m.ntime) == (200, 100, 200, 400)
+    for i in range(2):
+        f = M.field_gaussian(m, 5000 + i)
+        ch = _chain(m, f)
+        w, g = _grad(ch, m)
+        assert abs(w.real - _weight(ch, f)) <= 1e-9 * abs(w.real)
+        gt = logweight_grad_trace_stable(m, f, SEED_WORDS)
+        assert np.abs(g - gt).max() <= 1e-9 + 1e-7 * np.abs(gt).max(), np.abs(g - gt).max()
+        rng = np.random.default_rng(5000 + i)
+        fd_noise = 50.0 * np.finfo(np.float64).eps * abs(w.real) / H
+        for _ in range(64):
+            b, t = int(rng.integers(m.n_bf)), int(rng.integers(m.ntime))
+            fp = f.copy(); fp[b, t] += H
+            fm = f.copy(); fm[b, t] -= H
+            fd = (_weight(ch, fp) - _weight(ch, fm)) / (2 * H)
+            assert abs(g[b, t] - fd) <= ATOL + RTOL * abs(fd) + fd_noise, (b, t, g[b, t], fd, w.real)
+        ch.close()

@@ -61,3 +61,34 @@ def test_uneven_batch_resume(tmp_path):
         assert rel_fro(cb.g(), ca.g()) < 1e-12
     a.close()
     b.close()
+
+
+def test_chain_resume_matches_uninterrupted_oracle(tmp_path):
+    """A GPU chain checkpointed after sweep 2, restored into a fresh handle
+    and run for sweeps 3-4 against the FP64 oracle run for sweeps 1-4 with
+    no interruption (src/Main_PQMC.f90:355-369 reads the field back; the
+    saved ran2 state and counters continue the stream): the same
+    accept/reject sequence (field, counters, ran2 state) and G within 1e-10."""
+    from oracle.oracle import OracleChain
+    from pqmc_allinone_gb300.engine import PqmcChain
+    m, f = epsocz_small(L=4, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=33)
+    w = seed_words(330)
+    a = PqmcChain(m, field=f, rng_words=w)
+    a.init_expkv()
+    a.init_g(1)
+    a.sweep(1, 2)
+    p = str(tmp_path / "chain.npz")
+    ck.save_checkpoint(p, [a], 2)
+    a.close()
+    b = PqmcChain(m, field=np.zeros_like(f), rng_words=seed_words(999))
+    nxt = ck.restore_chain(b, ck.load_checkpoint(p))
+    b.sweep(nxt, 2)
+    o = OracleChain(m, field=f, seed_words=w, meas=False)
+    o.init_expkv()
+    o.init_g(1)
+    o.sweep(1, 4)
+    so, sb = o.state(), b.state()
+    assert np.array_equal(b.field(), o.field())
+    assert (sb["positive_accept"], sb["negative_accept"]) == (so["positive_accept"], so["negative_accept"])
+    assert sb["rng"] == so["rng"]
+    assert rel_fro(b.g(), o.g()) < 1e-10

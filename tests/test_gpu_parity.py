@@ -132,3 +132,98 @@ def test_measurement(engine):
     rg = g.sweep(1, 2, warmup=0, meas_number=1, cap=4)
     assert ro.shape == rg.shape and ro.shape[0] == 2
     assert np.allclose(rg, ro, rtol=1e-10, atol=1e-12)
+
+
+def _c1_model():
+    """The 4x4 configuration with phonon-modulated bonds t(1 - lambda x_b),
+    lambda = 0.8, 32 bonds, spin 1/2 as ncopy = 2 (weight det^ncopy,
+    src/mod_update.f90:104), Nup = Ndn = 8, Lt = 80, dtau = 0.1, ngroup = 10,
+    the Gaussian proposal with sigma = 0.3 and x ~ N(0, 0.5^2) from seed 1."""
+    import dataclasses
+    from pqmc_allinone_gb300 import model as M
+    m1, f = general_bond_model(L=4, ntime=80, ngroup=10, lam=0.8, seed=1)
+    spec = dataclasses.replace(m1.spec, ncopy=2, proposal_kind=M.PROPOSAL_GAUSSIAN, jump_distance=0.3)
+    m = M.build_model(spec, twist_seed=3, twist=1e-3)
+    assert m.n_bf == 32 and m.nelec == 8 and m.ntime == 80
+    return m, f
+
+
+def test_spin_half_gaussian_20_sweeps_bit_identical(engine):
+    """The spin-1/2 bond-model configuration with the Gaussian proposal: 20
+    sweeps from one seed give the oracle's accept/reject sequence bit for bit
+    (ran2 state, counters and field after every sweep), G within 1e-10.  The
+    Box-Muller jumps use the fixed-order arithmetic both sides share."""
+    from oracle.oracle import OracleChain
+    from pqmc_allinone_gb300.engine import PqmcChain
+    m, f = _c1_model()
+    o = OracleChain(m, field=f, seed_words=SEED_WORDS)
+    g = PqmcChain(m, field=f, rng_words=SEED_WORDS)
+    for c in (o, g):
+        c.init_expkv()
+        c.init_g(1)
+    for loop in range(1, 21):
+        o.sweep(loop, 1)
+        g.sweep(loop, 1)
+        so, sg = o.state(), g.state()
+        assert sg["rng"] == so["rng"], loop
+        assert (sg["positive_accept"], sg["negative_accept"]) == (so["positive_accept"], so["negative_accept"]), loop
+        assert np.array_equal(g.field(), o.field()), loop
+        assert rel_fro(g.g(), o.g()) < G_TOL, loop
+    assert so["positive_accept"] > 0 and so["negative_accept"] > 0
+
+
+def test_spin_half_gaussian_mixed_batch(engine):
+    """The same configuration through the mixed batch (exact round update,
+    dim-2 plaquettes, Gaussian proposals formed on the device): the fast
+    path stays within 1e-8 of the recompute, and the G a sweep ends with
+    matches the oracle's on the chain's own field."""
+    from oracle.oracle import OracleChain
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    from pqmc_allinone_gb300.rng import seed_words
+    m, f = _c1_model()
+    words = [seed_words(20 + i) for i in range(4)]
+    b = PqmcBatch([m] * 4, [f] * 4, words, precision=1)
+    b.init()
+    for loop in (1, 2):
+        b.sweep(loop)
+    for ch, w in zip(b.chains, words):
+        s = ch.state()
+        assert 0.0 < s["err_g_rel_max"] < 1e-8, s
+        assert s["positive_accept"] > 0
+        o = OracleChain(m, field=ch.field(), seed_words=w, meas=False)
+        o.init_expkv()
+        o.init_g(1)
+        assert rel_fro(ch.g(), o.g()) < 1e-10
+    b.close()
+
+
+def test_c2_full_size_plain_fp64():
+    """The production-size configuration (14x14 spin-orbit lattice, Ns = 392,
+    Nup = 196, Lt = 1000, dtau = 0.1, lambda = 0.8, static alpha = 0.3,
+    ngroup = 10, x ~ N(0, 0.5^2) from seed 2) on the plain FP64 path against
+    the oracle: G of init_g_T0 within 1e-10, then one stabilisation block of
+    the first sweep (ten slices of updates and wraps closed by the
+    recompute, src/Main_PQMC.f90:99-154) with the same accept/reject sequence
+    and G within 1e-10 (err_fast, src/mod_evolution.f90:179-193, on both)."""
+    from oracle.oracle import OracleChain
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.engine import PqmcChain
+    spec = M.epsocz_spec(14, lam=0.8, alpha=0.3, ntime=1000, ngroup=10, filling=0.5, jump_distance=0.5)
+    m = M.build_model(spec, twist_seed=11, twist=1e-3)
+    assert (m.ns, m.nelec, m.ntime, m.n_bf) == (392, 196, 1000, 392)
+    f = M.field_gaussian(m, 2)
+    o = OracleChain(m, field=f, seed_words=SEED_WORDS, meas=False)
+    g = PqmcChain(m, field=f, rng_words=SEED_WORDS)
+    for c in (o, g):
+        c.init_expkv()
+        c.init_g(1)
+    assert rel_fro(g.g(), o.g()) < G_TOL
+    o.sweep(1, 1, max_slices=m.ngroup)
+    g.sweep_slices(1, 1, m.ngroup)
+    so, sg = o.state(), g.state()
+    assert sg["rng"] == so["rng"]
+    assert (sg["positive_accept"], sg["negative_accept"]) == (so["positive_accept"], so["negative_accept"])
+    assert sg["positive_accept"] > 1000
+    assert np.array_equal(g.field(), o.field())
+    assert rel_fro(g.g(), o.g()) < G_TOL
+    assert abs(sg["ln_cw"].real - so["ln_cw"].real) <= 1e-9 * abs(so["ln_cw"].real)

@@ -284,3 +284,29 @@ def test_spin_half_gaussian_bond_model():
         s = o2.state()
         assert s["err_fast_max"] <= 1e-6 + 1e-15
     assert s["positive_accept"] > 0 and s["negative_accept"] > 0
+
+
+def test_boxmuller_fixed_order_arithmetic():
+    """The Gaussian proposal's logarithm and cosine (include/pqmc_boxmuller.h,
+    shared by the CUDA kernels and the oracle so that Gaussian jumps agree
+    bit for bit) against the library functions: within 4 units in the last
+    place over ran2 draws, the grid ends and the reduction boundaries of
+    cos 2 pi t (1/8, 1/4, 3/8, 1/2, ...)."""
+    import math
+    from oracle.oracle import gauss_parts
+    draws, _ = rng_draw(seed_words(7), 20000)
+    u = draws.astype(np.float64)
+    edges = np.array([2.0 ** -24, 1e-7, 0.125, 0.25, 0.375, 0.5, 0.625, 0.75, 0.875, 1.0 - 2.0 ** -24,
+                      0.70710677, 0.70710683, 1.0], dtype=np.float32).astype(np.float64)
+    u1 = np.concatenate([u[: u.size // 2], edges])
+    u2 = np.concatenate([u[u.size // 2:], edges])
+    out = gauss_parts(u1, u2)
+    lg = np.array([math.log(x) for x in u1])
+    cs = np.array([math.cos(2.0 * math.pi * x) for x in u2])
+    jp = np.sqrt(-2.0 * lg) * cs
+    ulp = np.spacing(1.0)
+    assert np.all(np.abs(out[:, 0] - lg) <= 4 * ulp * np.maximum(np.abs(lg), 1e-300) + 1e-300)
+    # the cosine: absolute error against an argument rounded to 2 pi * t
+    assert np.all(np.abs(out[:, 1] - cs) <= 4 * ulp)
+    assert np.all(np.abs(out[:, 2] - jp) <= 1e-14 * (1 + np.abs(jp)))
+    assert np.all(out[u2 == 0.25, 1] == 0.0) and np.all(out[u2 == 0.5, 1] == -1.0) and out[-1, 1] == 1.0

@@ -61,6 +61,11 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--graphs", type=int, default=1, choices=[0, 1],
                    help="replay each slice's family steps from a captured CUDA graph (mixed batches)")
+    p.add_argument("--profile-block", type=int, default=0, metavar="C",
+                   help="profiling run instead of the benchmark: C chains of the workload's model in one "
+                        "group (delay depth 64, no graphs, the --flush round update), one warm-up block of "
+                        "ngroup slices, then one block inside an NVTX range named 'block' (for ncu "
+                        "--nvtx-include block/); prints the chains' largest drift")
     return p.parse_args()
 
 
@@ -256,37 +261,105 @@ class Cursor:
         return out
 
 
-def g_error_full_size(m, rank: int) -> dict:
-    """Green's-function error of the mixed form at full size: two chains run
-    the first block of sweep 1 (slices Lt..Lt-9, the stabilised recompute at
-    its end) in a mixed batch; the plain FP64 chain then recomputes G at the
-    same slice from the mixed chain's own field (init_g_T0 + get_g_scratch_T0)
-    and the two G are compared (relative Frobenius), with ln_cw beside."""
+def g_error_full_size(m, rank: int, flush: int) -> dict:
+    """Green's-function and observable error of the mixed form at full size
+    on identical phonon fields: the benchmark's first two chains (seeds 3000,
+    3001) run the first block of sweep 1 (slices Lt..Lt-9, the stabilised
+    recompute at its end) in a mixed batch; the plain FP64 chain then
+    recomputes G at the same slice from the mixed chain's own field
+    (init_g_T0 + get_g_scratch_T0) and the two G are compared (relative
+    Frobenius), with ln_cw beside, and one equal-time measurement record
+    (every observable of ms_take_measurement with its k-space part) taken
+    from each G at slice Lt/2 of that field."""
     from pqmc_allinone_gb300 import model as M
     from pqmc_allinone_gb300.engine import PqmcBatch, PqmcChain
     from pqmc_allinone_gb300.rng import seed_words
-    seeds = [3900 + i + 1000 * rank for i in range(2)]
-    b = PqmcBatch([m] * 2, [M.field_gaussian(m, s) for s in seeds], [seed_words(s) for s in seeds], precision=1)
+    seeds = [3000 + i + 1000 * rank for i in range(2)]
+    b = PqmcBatch([m] * 2, [M.field_gaussian(m, s) for s in seeds], [seed_words(s) for s in seeds], precision=1,
+                  meas=True)
+    b.set_flush(flush)
     b.init()
     b.sweep_slices(1, 1, m.ngroup)
     t = m.ntime - m.ngroup + 1
-    errs, dl = [], []
+    errs, dl, obs, obs_max = [], [], [], []
     for c in b.chains:
-        p = PqmcChain(m, field=c.field(), rng_words=seed_words(1))
+        p = PqmcChain(m, field=c.field(), rng_words=seed_words(1), meas=True)
         p.init_expkv()
         p.init_g(1)
         p.get_g_scratch(t, False, 1)
         g0, g1 = p.g(), c.g()
         errs.append(float(np.linalg.norm(g1 - g0) / np.linalg.norm(g0)))
         dl.append(abs(c.state()["ln_cw"].real - p.state()["ln_cw"].real))
+        r0 = p.begin_measure(False, m.ntime // 2, 0)
+        r1 = c.begin_measure(False, m.ntime // 2, 0)
+        obs.append(float(np.linalg.norm(r1 - r0) / np.linalg.norm(r0)))
+        big = np.abs(r0) > 1e-6 * np.abs(r0).max()
+        obs_max.append(float(np.max(np.abs(r1 - r0)[big] / np.abs(r0)[big])))
         p.close()
     drift = max(c.state()["err_g_rel_max"] for c in b.chains)
     b.close()
     return {"recompute_vs_fp64_rel_max": max(errs), "re_ln_cw_abs_diff_max": max(dl),
-            "fast_path_drift_in_block_rel_max": drift,
+            "observables_rel_fro_max": max(obs), "observables_componentwise_rel_max": max(obs_max),
+            "fast_path_drift_in_block_rel_max": drift, "seeds": seeds,
             "definition": "||G_mixed - G_fp64||_F / ||G_fp64||_F at the recompute closing the first block of "
-                          f"sweep 1 (slice {t}), same phonon field, 2 chains at full size; the FP64 G from the "
-                          "plain single-chain path (parity-tested against the oracle)"}
+                          f"sweep 1 (slice {t}), same phonon field, the benchmark's chains 0 and 1; the FP64 G from "
+                          "the plain single-chain path (parity-tested against the oracle at this size); observables: "
+                          "one measurement record (all observables and their k-space parts) from each G at slice "
+                          "Lt/2, relative Frobenius and the largest relative error of components above 1e-6 of "
+                          "the largest"}
+
+
+def run_profile_block(args) -> None:
+    """A short, self-contained run for kernel captures: one chain group, no
+    CUDA graphs (each kernel is its own launch), a warm-up block and one
+    block inside the NVTX range 'block'."""
+    import torch
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    from pqmc_allinone_gb300.rng import seed_words
+    m = workload_model("small" if args.workload == "small" else "c4_mixed")
+    c = args.profile_block
+    seeds = [3000 + i for i in range(c)]
+    b = PqmcBatch([m] * c, [M.field_gaussian(m, s) for s in seeds], [seed_words(s) for s in seeds], precision=1)
+    b.set_graphs(False)
+    b.set_flush(args.flush)
+    b.set_delay(args.delay or 64)
+    b.init()
+    b.sweep_slices(1, 1, m.ngroup)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("block")
+    b.sweep_slices(1, 1 + m.ngroup, m.ngroup)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    drift = max(ch.state()["err_g_rel_max"] for ch in b.chains)
+    b.close()
+    print(json.dumps({"profile_block": c, "flush": args.flush, "ns": m.ns, "ntime": m.ntime,
+                      "drift_rel_max": drift}))
+
+
+def flush_standalone(m, depth: int, flush: int) -> dict:
+    """The round update's products timed alone: one chain group of 8 chains
+    (nothing else on the GPU), phase timers over one block of 10 slices."""
+    from pqmc_allinone_gb300 import model as M
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    from pqmc_allinone_gb300.rng import seed_words
+    seeds = [3000 + i for i in range(8)]
+    b = PqmcBatch([m] * 8, [M.field_gaussian(m, s) for s in seeds], [seed_words(s) for s in seeds], precision=1)
+    b.set_flush(flush)
+    b.set_delay(depth)
+    b.init()
+    b.sweep_slices(1, 1, m.ngroup)   # warm-up block
+    b.set_timing(True)
+    b.sweep_slices(1, 1 + m.ngroup, m.ngroup)
+    ph = b.timing()
+    rounds = sum(b.flush_rounds())
+    b.set_timing(False)
+    b.close()
+    ms, n = ph["flush"]
+    bytes_alg = 32.0 * m.ns * m.ns * rounds
+    return {"chains": 8, "flush_ms_per_launch_pair": ms / max(1, n), "rounds_with_columns": rounds,
+            "launches": n, "achieved_gbs": bytes_alg / (ms * 1e-3) / 1e9 if ms > 0 else 0.0,
+            "algorithmic_bytes_per_round": 32.0 * m.ns * m.ns * 8}
 
 
 def run_plain(m, steps: int, rank: int) -> dict:
@@ -387,20 +460,23 @@ def run_mixed(args, world, rank, local):
     torch.cuda.synchronize()
     phases = b.timing()
     rounds = b.flush_rounds()
+    scanprof = b.scan_profile()
     b.set_timing(False)
     st2 = [c.state() for c in b.chains]
     # the phase timers follow chain group 0 (the first C/groups chains)
     g0 = C // max(1, binfo["groups"])
     acc_ph = sum(s2["positive_accept"] - s1["positive_accept"] for s1, s2 in zip(st1[:g0], st2[:g0]))
 
-    # the delayed-update contraction G += A B (rank-K flush, k_bflush_um).  At
-    # delay depth K it does 8*Ns^2*K flop against 32*Ns^2 bytes of G
-    # (double-float read and write): 2K/8 = 16 flop/B at K=64, under the HBM
-    # roof (6.8 TB/s measured copy bandwidth x 16 = 109 TFLOP/s), far below
-    # the tensor roof.
-    # Algorithmic bytes: 32*Ns^2 per flush that had columns to fold in
-    # (counted on the device per chain), over the flush kernel's own event
-    # time (the BF16 split kernel is timed apart).
+    # The contraction the delayed update reduces to, per round with columns:
+    # G += X Z (exact update, k_xgemm<1>; X = G(:,S) M by k_xgemm<0> first)
+    # or G += A B (FP32 panels, k_bflush_um / k_bflush).  At delay depth K it
+    # does 8*Ns^2*K flop (counted once, not the slice products) against
+    # 32*Ns^2 bytes of the double-float G (read and write): 16 flop/B at
+    # K = 64, under the HBM roof (x16 the measured copy bandwidth), far below
+    # the tensor roof.  Algorithmic bytes: 32*Ns^2 per round with columns
+    # (counted on the device per chain) over the flush phase's own event
+    # time on chain group 0's stream (the other groups' kernels run beside
+    # it); the same figure with nothing else on the GPU is reported apart.
     pk = peaks()
     dim = 4
     flush_ms, flush_n = phases["flush"]
@@ -409,36 +485,49 @@ def run_mixed(args, world, rank, local):
     flops = 8.0 * m.ns * m.ns * dim * acc_ph
     secs = flush_ms * 1e-3
     achieved = bytes_alg / secs / 1e9 if secs > 0 else 0.0
-    traffic = None
+    key = {2: "k_xgemm_flush", 1: "k_bflush_um"}.get(args.flush)
+    traffic, traffic_note = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            tj = json.load(f).get("k_bflush_um")
+            tj = json.load(f).get(key) if key else None
             if tj and tj.get("ns") == m.ns:
-                # DRAM bytes of one full-depth launch, scaled to group 0's chains
+                # DRAM bytes of one launch, scaled to group 0's chains
                 traffic = tj["bytes_per_launch"] * g0 / tj["chains"]
+                traffic_note = tj.get("note")
     except Exception:
         pass
+    kname = {2: "k_xgemm<1> (round update G += X Z from G: Ozaki-split BF16 tcgen05 products, exact level sums "
+                "in tensor memory, double-float epilogue; after k_xgemm<0>, X = G(:,S) M)",
+             1: "k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator in tensor memory)",
+             0: "k_bflush (rank-K flush G += A B, mma.sync BF16x3 products, FP32 accumulate)"}[args.flush]
+    sc_cyc = sum(x[0] for x in scanprof)
+    sc_acc = sum(x[1] for x in scanprof)
+    sc_rej = sum(x[2] for x in scanprof)
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
             "per_launch_bytes_algorithmic": bytes_alg / max(1, flush_n),
-            "traffic_note": "ncu dram__bytes_read+write of one full-depth flush launch (profiles/traffic.json, "
-                            "captured on the one-CTA-per-SM form of the kernel), scaled to the chains of one launch "
-                            "(chain group 0)",
+            "per_launch_bytes_algorithmic_all_columns": 32.0 * m.ns * m.ns * g0,
+            "traffic_note": traffic_note,
             "tensor_achieved_tflops": flops / secs / 1e12 if secs > 0 else 0.0,
             "tensor_peak_tflops": pk["bf16_tflops_sustained"],
-            "kernel": ("k_bflush_um (rank-K flush G += A B, tcgen05 BF16x3 products, FP32 accumulator "
-                       "in tensor memory)" if (depth <= 64 and (args.flush or tune)) else
-                       "k_bflush (rank-K flush G += A B, mma.sync BF16x3 products, FP32 accumulate)"),
-            "algorithmic": "32*Ns^2 bytes (G read + write, double-float) per flush with panel columns (device "
-                           "count, chain group 0) and 8*Ns^2*dim flop per accepted move, over the flush kernel's "
-                           "event time during two blocks (the other groups' kernels share the GPU meanwhile; "
-                           "launches of empty rounds included)",
+            "kernel": kname,
+            "algorithmic": "32*Ns^2 bytes (G read + write, double-float) per round with columns (device count, "
+                           "chain group 0) and 8*Ns^2*dim flop per accepted move, over the flush phase's event time "
+                           "during two blocks (the other groups' kernels share the GPU meanwhile; launches of empty "
+                           "rounds included)",
             "flush_rounds_group0": rounds_g0,
             "peak_source": f"{pk['source']} HBM copy bandwidth; bf16 sustained for the tensor figure",
-            "dominant_by_time": "k_bscan (59% of the serialised kernel time in the committed launch list of "
-                                "two 16-chain blocks): the sequential ratio scan, one CTA per "
-                                "chain, latency-bound by the Markov order (FMA pipe 33% active), neither an HBM nor "
-                                "a tensor-pipe kernel"}
+            "scan": {"kernel": "k_bscan (sequential ratio scan, one CTA per chain)",
+                     "sm_cycles_per_accepted_move": sc_cyc / max(1, sc_acc),
+                     "sm_cycles_per_proposal": sc_cyc / max(1, sc_acc + sc_rej),
+                     "accepted": sc_acc, "rejected": sc_rej,
+                     "definition": "device clock64 of every scan CTA from its start to its last bookkeeping, "
+                                   "summed over the two phase-timed blocks of all chains, over the moves it "
+                                   "accepted (the scan's cost model: ~17k cycles per accepted move, 11k of them the "
+                                   "panel stream)"},
+            "dominant_by_time": "k_bscan: the sequential ratio scan, one CTA per chain, latency-bound by the "
+                                "Markov order, neither an HBM nor a tensor-pipe kernel (its cycles per accepted "
+                                "move are under scan)"}
     total_ms = sum(v[0] for v in phases.values())
     phase_out = {k: {"ms_per_step": v[0] / 2, "share": v[0] / total_ms if total_ms else None,
                      "launch_groups": v[1]} for k, v in phases.items()}
@@ -448,7 +537,10 @@ def run_mixed(args, world, rank, local):
     # runs, the updated block and each chain's state come back
     e2e = run_e2e_mixed(b, m, cur, min(args.steps, 5))
     b.close()
-    gerr = g_error_full_size(m, rank)
+    gerr = g_error_full_size(m, rank, args.flush)
+    standalone = flush_standalone(m, depth, args.flush) if rank == 0 else None
+    roof["standalone"] = standalone
+    roof["standalone_frac"] = (standalone["achieved_gbs"] / pk["hbm_gbs"]) if standalone else None
 
     plain = None if args.no_plain else run_plain(m, args.plain_steps, rank)
     cb = None
@@ -462,16 +554,21 @@ def run_mixed(args, world, rank, local):
            "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None,
-           "dtype": "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute",
+           "dtype": ("double-float (48-bit) G, wraps and recompute; fp32 scan ratios; round update from G: "
+                     "fp32 inverse + double-float Newton step, bf16 Ozaki slices x5 with exact level sums"
+                     if args.flush == 2 else
+                     "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute"),
            "data": "synthetic (x ~ N(0,0.5^2), seeds 3000+i)",
            "config": config_of(args.workload, m, world, C, {"autotune": tune, **binfo}),
            "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "clocks": clocks,
            "cpu_baseline": cb, "plain_fp64": plain,
            "speedup_vs_plain_fp64": (per_gpu / plain["value"]) if plain else None,
            "g_error": {"fast_path_drift_rel_max": drift,
+                       "gate": 1e-8,
+                       "meets_gate": bool(drift <= 1e-8 and gerr["recompute_vs_fp64_rel_max"] <= 1e-8),
                        "definition": "max over chains and recomputes in the timed region of "
-                                     "||G_fast - G_recomputed||_F / ||G_recomputed||_F (drift of the FP32 "
-                                     "fast path over one ngroup block; the recompute is FP64-class)",
+                                     "||G_fast - G_recomputed||_F / ||G_recomputed||_F (drift of the fast "
+                                     "path over one ngroup block; the recompute is FP64-class)",
                        "recompute_vs_fp64": gerr},
            "accept_ratio": acc / max(1, acc + rej), "phases": phase_out, "init_s": t_init}
     print(json.dumps(out))
@@ -656,7 +753,10 @@ def run_uneven(args, world, rank, local):
            "value": world * C / t_step, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None,
-           "dtype": "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute",
+           "dtype": ("double-float (48-bit) G, wraps and recompute; fp32 scan ratios; round update from G: "
+                     "fp32 inverse + double-float Newton step, bf16 Ozaki slices x5 with exact level sums"
+                     if args.flush == 2 else
+                     "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute"),
            "data": "synthetic (per chain i: seed 1000+i draws L, Lt, lambda~U(0.5,1); x ~ N(0,0.5^2))",
            "config": {"workload": f"{C} chains of uneven size, mixed precision, one batch per GPU",
                       "chains_by_L": {L: Ls.count(L) for L in (8, 10, 12)},
@@ -723,6 +823,9 @@ def main():
     if args.impl == "reference":
         world, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
         run_reference(args, world, rank)
+        return
+    if args.profile_block:
+        run_profile_block(args)
         return
     world, rank, local = dist_setup()
     if args.workload == "c2_fp64":

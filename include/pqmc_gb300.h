@@ -424,6 +424,13 @@ int pqmc_batch_get_timing(pqmc_batch* batch, double* ms, long long* launches);
  * to fold in since the last pqmc_batch_set_timing, i.e. the number of
  * read-modify-writes of the chain's G by the flush. */
 int pqmc_batch_flush_rounds(pqmc_batch* batch, long long* rounds);
+/* Per chain (no reference counterpart), since the last
+ * pqmc_batch_set_timing(batch, 1): out[3i] the SM cycles the chain's
+ * sequential scan CTA ran (device clock64 from its start to its last
+ * bookkeeping, summed over the scan rounds), out[3i+1] the moves it
+ * accepted and out[3i+2] the proposals it rejected.  Counted only while
+ * phase timing is on. */
+int pqmc_batch_scan_profile(pqmc_batch* batch, long long* out);
 /* Slice graphs (mixed batches, on by default; no reference counterpart):
  * the family steps of a slice (draws, proposals, scan rounds, flushes,
  * wraps) are captured once per chain group, direction and G-buffer parity

@@ -247,6 +247,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_set_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_get_timing": ([vp, _f64p, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "pqmc_batch_flush_rounds": ([vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "pqmc_batch_scan_profile": ([vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "pqmc_batch_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_classes": ([vp, _i32p], ctypes.c_int),
         "pqmc_batch_field_slices": ([vp, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int], ctypes.c_int),

@@ -64,6 +64,9 @@ struct BDesc {
   // the round's accepted moves for the exact update (exact.cuh)
   int* acc_site;
   float4* acc_delta;
+  // scan profile while phase timing is on: SM cycles of the chain's scan
+  // CTA, accepted moves, rejected proposals
+  unsigned long long* scan_prof;
 };
 
 // ---------------------------------------------------------------------------
@@ -261,7 +264,8 @@ __device__ __forceinline__ void scan_issue(float2* s_stage, uint64_t* s_full, co
 
 template <int DIM, int RPT>
 __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, int parity, int kd, int qc,
-                                                         int* next_p, int exact) {
+                                                         int* next_p, int exact, int prof) {
+  const long long t_start = prof ? clock64() : 0;
   constexpr int NW = SCAN_THREADS / 32;
   __shared__ BDesc sd;
   __shared__ float2 s_R[NW][16];
@@ -592,6 +596,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_bscan(const BDesc* D, int pf, 
       }
       d.sc->pos_acc += n_acc;
       d.sc->neg_acc += na;
+      if (prof) {
+        atomicAdd(d.scan_prof, (unsigned long long)(clock64() - t_start));
+        atomicAdd(d.scan_prof + 1, (unsigned long long)n_acc);
+        atomicAdd(d.scan_prof + 2, (unsigned long long)na);
+      }
     }
   }
 }
@@ -1397,6 +1406,7 @@ struct pqmc_batch {
   bool slice_prep = false;
   pqmc::DevScalars* h_states = nullptr;   // pinned staging of pqmc_batch_states
   unsigned long long* d_nflush = nullptr;  // per chain: flush rounds with work
+  unsigned long long* d_scanprof = nullptr;  // per chain: scan cycles, accepted moves, rejected proposals
   // equal-time measurement inside batched sweeps (ms_begin_measure semantics)
   int meas_on = 0, meas_warmup = 0, meas_interval = 1, meas_number = 0;
   std::vector<std::vector<double>> records;   // finished records per chain
@@ -1603,7 +1613,7 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     const bool one = ns <= SCAN_THREADS;
 #define PQMC_SCAN(DM, R)                                                                                         \
   PQMC_CUDA(launch_at(k_bscan<DM, R>, dim3(C), dim3(SCAN_THREADS), smem, st, (b->prio_mask & 1) != 0, b->prio_hi, Dg, \
-                      pf, parity, kd, b->qc, next, exact ? 1 : 0))
+                      pf, parity, kd, b->qc, next, exact ? 1 : 0, b->timing ? 1 : 0))
     switch (dim) {
       case 1: if (one) PQMC_SCAN(1, 1); else PQMC_SCAN(1, 2); break;
       case 2: if (one) PQMC_SCAN(2, 1); else PQMC_SCAN(2, 2); break;
@@ -2097,6 +2107,9 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
   PQMC_CUDA(cudaMalloc((void**)&b->d_nflush, sizeof(unsigned long long) * n_chains));
   PQMC_CUDA(cudaMemset(b->d_nflush, 0, sizeof(unsigned long long) * n_chains));
   for (int i = 0; i < n_chains; ++i) b->h_desc[i].nflush = b->d_nflush + i;
+  PQMC_CUDA(cudaMalloc((void**)&b->d_scanprof, sizeof(unsigned long long) * 3 * n_chains));
+  PQMC_CUDA(cudaMemset(b->d_scanprof, 0, sizeof(unsigned long long) * 3 * n_chains));
+  for (int i = 0; i < n_chains; ++i) b->h_desc[i].scan_prof = b->d_scanprof + 3 * i;
   if (precision == PQMC_PREC_MIXED) {
     // the exact round update: accepted-move records and slice images per
     // chain (images zero outside the rows and columns of G)
@@ -2196,6 +2209,7 @@ int pqmc_batch_destroy(pqmc_batch* b) {
     if (pa) cudaFree(pa);
   if (b->h_states) cudaFreeHost(b->h_states);
   if (b->d_nflush) cudaFree(b->d_nflush);
+  if (b->d_scanprof) cudaFree(b->d_scanprof);
   if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_next) cudaFree(b->d_next);
   if (b->d_err) cudaFree(b->d_err);
@@ -2287,6 +2301,31 @@ int pqmc_batch_set_timing(pqmc_batch* b, int enable) {
     b->phase_n[k] = 0;
   }
   if (b->d_nflush) PQMC_CUDA(cudaMemset(b->d_nflush, 0, sizeof(unsigned long long) * b->chains.size()));
+  if (b->d_scanprof)
+    PQMC_CUDA(cudaMemset(b->d_scanprof, 0, sizeof(unsigned long long) * 3 * b->chains.size()));
+  return PQMC_OK;
+}
+
+int pqmc_batch_scan_profile(pqmc_batch* b, long long* out) {
+  if (!b || !out) { set_error("batch_scan_profile: null argument"); return PQMC_ERR_ARG; }
+  if (!b->parts.empty()) {
+    for (size_t k = 0; k < b->parts.size(); ++k) {
+      std::vector<long long> pr(3 * b->parts[k]->chains.size());
+      PQMC_TRY(pqmc_batch_scan_profile(b->parts[k], pr.data()));
+      for (size_t i = 0; i < b->chains.size(); ++i)
+        if (b->part_of[i] == (int)k)
+          for (int q = 0; q < 3; ++q) out[3 * i + q] = pr[3 * b->index_in_part[i] + q];
+    }
+    return PQMC_OK;
+  }
+  const size_t n = b->chains.size();
+  std::vector<unsigned long long> h(3 * n, 0ull);
+  if (b->d_scanprof) {
+    PQMC_CUDA(cudaStreamSynchronize(b->stream));
+    for (int g = 1; g < b->n_groups; ++g) PQMC_CUDA(cudaStreamSynchronize(b->g_stream[g]));
+    PQMC_CUDA(cudaMemcpy(h.data(), b->d_scanprof, sizeof(unsigned long long) * 3 * n, cudaMemcpyDeviceToHost));
+  }
+  for (size_t i = 0; i < 3 * n; ++i) out[i] = (long long)h[i];
   return PQMC_OK;
 }
 

@@ -332,9 +332,10 @@ def run_profile_block(args) -> None:
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     drift = max(ch.state()["err_g_rel_max"] for ch in b.chains)
+    free, total = torch.cuda.mem_get_info()
     b.close()
     print(json.dumps({"profile_block": c, "flush": args.flush, "ns": m.ns, "ntime": m.ntime,
-                      "drift_rel_max": drift}))
+                      "drift_rel_max": drift, "device_gb_in_use": (total - free) / 1e9}))
 
 
 def flush_standalone(m, depth: int, flush: int) -> dict:

@@ -334,19 +334,29 @@ int pqmc_logweight_grad(pqmc_chain* chain, double* logw_out, double* grad_dev);
 /* ---- batched, mixed precision --------------------------------------- */
 typedef struct pqmc_batch pqmc_batch; /* many chains in one device context */
 #define PQMC_PREC_FP64 0   /* every product in FP64                        */
-#define PQMC_PREC_MIXED 1  /* split-BF16 tensor-core delayed-update and
-                              B-string products, FP32 accumulation; FP64
-                              QR, recompute and log-det                    */
+#define PQMC_PREC_MIXED 1  /* G held in double-float (two FP32 values,
+                              48-bit significand); accept/reject from FP32
+                              ratios; round update of G in double-float
+                              with Ozaki-split BF16 tensor-core products
+                              (exact level sums); double-float wraps, QR
+                              (CholeskyQR2), recompute and log-det; ln_cw
+                              accumulated in FP64                         */
 int pqmc_batch_create(const pqmc_model* const* models, int n_chains,
                       int precision, pqmc_batch** out);
 int pqmc_batch_destroy(pqmc_batch* batch);
 int pqmc_batch_chain(pqmc_batch* batch, int i, pqmc_chain** chain);
-/* delay depth of the mixed-precision update: panel columns folded into G
- * per tensor-core flush (default 64, at most 512) */
+/* delay depth of the mixed-precision update: accepted-move columns per
+ * scan round, applied to G by one round update (default 64, at most 512;
+ * the exact round update takes at most 64 and clamps deeper settings) */
 int pqmc_batch_set_delay(pqmc_batch* batch, int depth);
-/* rank-K flush engine of the mixed batch: 1 (default) = tcgen05 tensor
- * cores with the accumulator in tensor memory (delay depth <= 64; deeper
- * delays use 0), 0 = mma.sync split-BF16 tiles */
+/* round update of the mixed batch: 2 (default) = the exact update of G
+ * from G itself (W^-1 by an FP32 inverse refined by a double-float Newton
+ * step, Ozaki-split BF16 tcgen05 products with exact level sums, drift of
+ * the fast-updated G ~1e-9 per block), with double-float wraps;
+ * 1 = the scan's FP32 panels added by tcgen05 3xBF16 products (delay depth
+ * <= 64; deeper delays use 0), FP32 wrap corrections (drift ~1e-5 per
+ * block); 0 = the same with mma.sync split-BF16 tiles.  PQMC_WRAP_DF=0/1
+ * forces the FP32 / double-float wrap in any mode. */
 int pqmc_batch_set_flush(pqmc_batch* batch, int mode);
 /* one sweep of every chain (Main_PQMC.f90:99-154); equal-time
  * measurements only after pqmc_batch_set_measure; chains with global moves

@@ -217,7 +217,9 @@ int pqmc_get_qd(pqmc_chain* chain, int block, double* q, double* d);
 /* init_expKV for every family + set_pf_expKV_mat
  * (mod_phonon_field.f90:423-450, 605-636). */
 int pqmc_init_expkv(pqmc_chain* chain);
-/* init_g_T0(start_time) (mod_evolution.f90:46-111). */
+/* init_g(start_time): init_g_T0 (mod_evolution.f90:46-111), or init_g_FT
+ * on a chain set to finite temperature (the procedure pointer of
+ * set_temperature, :30-45). */
 int pqmc_init_g(pqmc_chain* chain, int start_time);
 /* update_phonon_field(ppf_list(pf_id), time) (mod_update.f90:13-201). */
 int pqmc_update_phonon_field(pqmc_chain* chain, int pf_id, int time);
@@ -231,12 +233,43 @@ int pqmc_left_evolve(pqmc_chain* chain, int time, int pf_id, double* mat,
 /* right_evolve(time, mat(n,Ns), n, pf_id, .false.) on a caller matrix. */
 int pqmc_right_evolve(pqmc_chain* chain, int time, int pf_id, double* mat,
                       int n);
-/* get_g_scratch_T0(time, forward, loop) (mod_evolution.f90:113-195);
- * err_out (may be NULL) receives max|gfast-g| and |Re(dln_cw)|. */
+/* get_g_scratch_T0(time, forward, loop) (mod_evolution.f90:113-195), or
+ * get_g_scratch_FT at finite temperature; err_out (may be NULL) receives
+ * max|gfast-g| and |Re(dln_cw)|. */
 int pqmc_get_g_scratch(pqmc_chain* chain, int time, int forward, int loop,
                        double* err_out);
-/* cal_new_weight_T0() (mod_evolution.f90:359-408); ln_cw_out complex. */
+/* cal_new_weight_T0() (mod_evolution.f90:359-408), or cal_new_weight_FT
+ * at finite temperature; ln_cw_out complex. */
 int pqmc_cal_new_weight(pqmc_chain* chain, double* ln_cw_out);
+
+/* ---- finite temperature (mod_evolution.f90:409-785) ------------------ */
+/* set_temperature (mod_evolution.f90:30-45): proj = 1 selects the
+ * projector path (the default), proj = 0 the finite-temperature one for
+ * init_g, get_g_scratch, cal_new_weight and the sweep.  Finite temperature
+ * needs ntime to be a multiple of ngroup and allocates the Ns x Ns Q and R
+ * strings (2 x 16 Ns^2 (ntime/ngroup + 2) bytes); chains of a batch stay on
+ * the projector path (PQMC_ERR_STATE).  Either switch drops G: call
+ * pqmc_init_g next.  The weight is ln det(1 + B(beta,0)) (x2 Re under
+ * TR_weight, x ncopy) and g_h = 1 - (1 + B(beta,0))^-1 at the slice in
+ * progress.  Four departures from the reference's unfinished branch, each a
+ * correction: the strings use a column-pre-pivoted Householder QR instead of
+ * the SVD (which loses the small scales of the graded products); init_g_FT
+ * closes with B(beta,beta) = 1 as the left factor; the left string's unitary
+ * factor is its Q; cal_new_weight_FT scales column i by D(i) alone. */
+int pqmc_set_temperature(pqmc_chain* chain, int proj);
+int pqmc_get_temperature(pqmc_chain* chain, int* proj);
+/* init_g_FT(start_time) (mod_evolution.f90:411-489). */
+int pqmc_init_g_ft(pqmc_chain* chain, int start_time);
+/* get_g_scratch_FT(time, forward, loop) (mod_evolution.f90:631-745). */
+int pqmc_get_g_scratch_ft(pqmc_chain* chain, int time, int forward, int loop,
+                          double* err_out);
+/* cal_new_weight_FT() (mod_evolution.f90:748-785); strings and G intact. */
+int pqmc_cal_new_weight_ft(pqmc_chain* chain, double* ln_cw_out);
+/* One block of the finite-temperature strings: q, r (Ns x Ns) and d (Ns)
+ * complex, any of them NULL.  Blocks below the current time hold
+ * B(t_b,0) = Q D R; blocks above it hold B(beta,t_b)^H = Q D R. */
+int pqmc_get_qdr_ft(pqmc_chain* chain, int block, double* q, double* d,
+                    double* r);
 /* Meas_sys%take_measurement(time) (mod_meas.f90:210-544): adds one
  * record into the device accumulator. */
 int pqmc_take_measurement(pqmc_chain* chain, int time);

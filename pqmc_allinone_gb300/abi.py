@@ -219,6 +219,12 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_right_evolve": ([vp, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int], ctypes.c_int),
         "pqmc_get_g_scratch": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p], ctypes.c_int),
         "pqmc_cal_new_weight": ([vp, _f64p], ctypes.c_int),
+        "pqmc_set_temperature": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_get_temperature": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "pqmc_init_g_ft": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_get_g_scratch_ft": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p], ctypes.c_int),
+        "pqmc_cal_new_weight_ft": ([vp, _f64p], ctypes.c_int),
+        "pqmc_get_qdr_ft": ([vp, ctypes.c_int, _f64p, _f64p, _f64p], ctypes.c_int),
         "pqmc_take_measurement": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_begin_measure": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p,
                                 ctypes.POINTER(ctypes.c_int)], ctypes.c_int),

@@ -122,6 +122,7 @@ extern "C" int pqmc_set_field_device(pqmc_chain* c, const double* dfield) {
 // grad_dev: device, (n_bf, ntime) doubles (gradient of Re logw).
 extern "C" int pqmc_logweight_grad(pqmc_chain* c, double* logw_out, double* grad_dev) {
   if (!c || !grad_dev) { set_error("logweight_grad: null argument"); return PQMC_ERR_ARG; }
+  if (c->finite_t) { set_error("logweight_grad: the projector log-weight only (the chain is at finite temperature)"); return PQMC_ERR_STATE; }
   const int ns = c->ns, ne = c->nelec, nt = c->ntime, ng = c->ngroup;
   cudaStream_t s = c->stream;
   const size_t qb = sizeof(cplx) * (size_t)ns * ne;

@@ -1925,6 +1925,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       delete b;
       return st;
     }
+    c->in_batch = true;
     b->chains.push_back(c);
   }
   pqmc_chain* c0 = b->chains[0];

@@ -343,8 +343,11 @@ static inline cplx* Qblk(pqmc_chain* c, int blk1) {  // 1-based block
 }
 static inline cplx* Dblk(pqmc_chain* c, int blk1) { return c->d_string + (size_t)c->nelec * (blk1 - 1); }
 
-// init_g_T0(start_time), src/mod_evolution.f90:46-111
+// init_g_T0(start_time), src/mod_evolution.f90:46-111; a chain set to
+// finite temperature takes init_g_FT instead (the procedure pointer of
+// set_temperature, :30-45)
 int do_init_g(pqmc_chain* c, int start_time) {
+  if (c->finite_t) return do_init_g_ft(c, start_time);
   const int ns = c->ns, ne = c->nelec, nb = c->nblock;
   cudaStream_t s = c->stream;
   size_t qb = sizeof(cplx) * (size_t)ns * ne;
@@ -383,6 +386,7 @@ int do_init_g(pqmc_chain* c, int start_time) {
 // get_g_scratch_T0(time, forward, loop), src/mod_evolution.f90:113-195
 int do_g_scratch(pqmc_chain* c, int time, bool forward, int loop) {
   (void)loop;
+  if (c->finite_t) return do_g_scratch_ft(c, time, forward);
   const int ns = c->ns, ne = c->nelec;
   if (forward ? (time - c->ngroup < 1 || time - 1 > c->ntime) : (time < 1 || time + c->ngroup - 1 > c->ntime)) {
     set_error("g_scratch: slices of time %d outside 1..%d", time, c->ntime);
@@ -413,6 +417,7 @@ int do_g_scratch(pqmc_chain* c, int time, bool forward, int loop) {
 
 // cal_new_weight_T0, src/mod_evolution.f90:359-408
 int do_new_weight(pqmc_chain* c) {
+  if (c->finite_t) return do_new_weight_ft(c);
   const int ns = c->ns, ne = c->nelec, nb = c->nblock;
   cudaStream_t s = c->stream;
   size_t qb = sizeof(cplx) * (size_t)ns * ne;
@@ -645,6 +650,7 @@ int chain_alloc(pqmc_chain* c, const pqmc_model* m, cudaStream_t s) {
 }
 
 int chain_free(pqmc_chain* c) {
+  ft_free(c);
   void* ptrs[] = {c->d_logsum, c->pre, c->d_model_blob, c->field, c->expkv, c->expkv_inv, c->g, c->g_alt, c->q_string, c->d_string,
                   c->slater_q, c->slater_d, c->rmat, c->xmat, c->lmat, c->pbp, c->tau, c->dtmp, c->lcol,
                   c->ipiv, c->ctl, c->sc, c->m_cell_sites, c->m_cell_bf, c->m_cell_xnb, c->m_cell_ynb,

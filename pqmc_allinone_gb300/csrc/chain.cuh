@@ -52,6 +52,8 @@ struct PlaqPre {
   double thr;       // accept iff |det R|^2 >= thr (the Metropolis test of cal_prob)
 };
 
+struct FtState;           // finite-temperature strings (finite_t.cu)
+
 struct WrapItems {        // cover of all sites by one family: plaquettes + singletons
   int n_items;
   int* d_pla;             // (n_items) plaquette index or -1
@@ -114,9 +116,23 @@ struct pqmc_chain {
   pqmc_global_params gp;
   std::vector<double> g_rpos;
   long long g_acc = 0, g_rej = 0;
+  // finite temperature (pqmc_set_temperature): the Q/D/R strings of
+  // init_g_FT and its work buffers, finite_t.cu
+  bool finite_t = false;
+  pqmc::FtState* ft = nullptr;
+  bool in_batch = false;            // owned by a pqmc_batch (projector path only)
 };
 
 namespace pqmc {
+// weight and error bookkeeping kernels of chain.cu, shared with finite_t.cu
+__global__ void k_scalars_zero(DevScalars* sc);
+__global__ void k_finish_weight(DevScalars* sc, int tr_weight, int ncopy, int compare);
+__global__ void k_maxdiff(long n, const cplx* __restrict__ a, const cplx* __restrict__ b, double* out);
+__global__ void k_set_errg(DevScalars* sc, const double* e);
+int do_init_g_ft(pqmc_chain* c, int start_time);
+int do_g_scratch_ft(pqmc_chain* c, int time, bool forward);
+int do_new_weight_ft(pqmc_chain* c);
+int ft_free(pqmc_chain* c);
 int chain_alloc(pqmc_chain* c, const pqmc_model* m, cudaStream_t s);
 int chain_free(pqmc_chain* c);
 int launch_init_expkv(pqmc_chain* c, int t0, int nt);

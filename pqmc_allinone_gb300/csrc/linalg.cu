@@ -106,8 +106,12 @@ __device__ __forceinline__ cplx block_csum(cplx v, double* red) {
 // block applies H_i^H to its share of the trailing columns.  Then Q formation
 // (zung2r).  A is m x n (lda = m), m >= n.  d receives diag(R) (real in the
 // LAPACK convention).  Matches zqdr (src/mod_matrixlib.f90:323-334) with the
-// unit-diagonal R discarded as the reference does for the hot path.
-__global__ void __launch_bounds__(256) k_house_qr(int m, int n, cplx* A, cplx* tau, cplx* d) {
+// unit-diagonal R discarded as the reference does for the hot path.  With
+// Rout the upper triangle of R (n x n, diagonal = d) is copied out before Q
+// is formed, and with lndet ln det Q = sum over the reflectors of
+// ln det(I - tau v v^H) = ln(-tau / conj(tau)) (a phase; 0 for tau = 0).
+__global__ void __launch_bounds__(256) k_house_qr(int m, int n, cplx* A, cplx* tau, cplx* d, cplx* Rout,
+                                                  cplx* lndet) {
   cg::grid_group grid = cg::this_grid();
   __shared__ double red[33];
   for (int i = 0; i < n; ++i) {
@@ -163,6 +167,22 @@ __global__ void __launch_bounds__(256) k_house_qr(int m, int n, cplx* A, cplx* t
       }
     }
     grid.sync();
+  }
+  if (Rout) {
+    for (int j = blockIdx.x; j < n; j += gridDim.x)
+      for (int k = threadIdx.x; k < n; k += blockDim.x) Rout[k + (size_t)n * j] = k <= j ? A[k + (size_t)m * j] : mk(0.0);
+    grid.sync();
+  }
+  if (lndet && blockIdx.x == 0 && threadIdx.x == 0) {
+    double ph = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const cplx t = tau[i];
+      if (t.x != 0.0 || t.y != 0.0) {
+        const cplx z = cdiv(cneg(t), cconj(t));
+        ph += atan2(z.y, z.x);
+      }
+    }
+    lndet[0] = mk(0.0, ph);
   }
   // zung2r: Q = H_1 ... H_n applied to the first n unit columns
   for (int i = n - 1; i >= 0; --i) {
@@ -333,8 +353,12 @@ int coop_grid(const void* fn, int threads, int want) {
 }
 
 int house_qr(cudaStream_t s, int m, int n, cplx* A, cplx* tau, cplx* d) {
+  return house_qr_r(s, m, n, A, tau, d, nullptr, nullptr);
+}
+
+int house_qr_r(cudaStream_t s, int m, int n, cplx* A, cplx* tau, cplx* d, cplx* R, cplx* lndet) {
   int nb = coop_grid((const void*)k_house_qr, 256, n);
-  void* args[] = {&m, &n, &A, &tau, &d};
+  void* args[] = {&m, &n, &A, &tau, &d, &R, &lndet};
   PQMC_CUDA(cudaLaunchCooperativeKernel((const void*)k_house_qr, nb, 256, args, 0, s));
   PQMC_LAUNCHED();
   return PQMC_OK;

@@ -168,7 +168,42 @@ class PqmcChain:
         self._chk(self.lib.pqmc_init_expkv(self.h), "init_expKV")
 
     def init_g(self, start_time: int = 1):
-        self._chk(self.lib.pqmc_init_g(self.h, start_time), "init_g_T0")
+        self._chk(self.lib.pqmc_init_g(self.h, start_time), "init_g")
+
+    # ---- finite temperature (src/mod_evolution.f90:409-785) -------------
+    def set_temperature(self, proj: bool):
+        """set_temperature: True for the projector path (the default), False
+        for finite temperature; G is dropped, call init_g next."""
+        self._chk(self.lib.pqmc_set_temperature(self.h, int(bool(proj))), "set_temperature")
+
+    def proj(self) -> bool:
+        v = ctypes.c_int(0)
+        self._chk(self.lib.pqmc_get_temperature(self.h, ctypes.byref(v)), "get_temperature")
+        return bool(v.value)
+
+    def init_g_ft(self, start_time: int = 1):
+        self._chk(self.lib.pqmc_init_g_ft(self.h, start_time), "init_g_FT")
+
+    def get_g_scratch_ft(self, time: int, forward: bool, loop: int = 1) -> np.ndarray:
+        e = np.zeros(2)
+        self._chk(self.lib.pqmc_get_g_scratch_ft(self.h, time, int(forward), loop, e.ctypes.data_as(_f64p)),
+                  "get_g_scratch_FT")
+        return e
+
+    def cal_new_weight_ft(self) -> complex:
+        o = np.zeros(2)
+        self._chk(self.lib.pqmc_cal_new_weight_ft(self.h, o.ctypes.data_as(_f64p)), "cal_new_weight_FT")
+        return complex(o[0], o[1])
+
+    def qdr_ft(self, blk: int):
+        """(Q, D, R) of one block of the finite-temperature strings."""
+        n = self.m.ns
+        q = np.zeros((n, n), dtype=np.complex128, order="F")
+        r = np.zeros((n, n), dtype=np.complex128, order="F")
+        d = np.zeros(n, dtype=np.complex128)
+        self._chk(self.lib.pqmc_get_qdr_ft(self.h, blk, q.ctypes.data_as(_f64p), d.ctypes.data_as(_f64p),
+                                           r.ctypes.data_as(_f64p)), "get_qdr_FT")
+        return q, d, r
 
     def update_phonon_field(self, pf_id: int, time: int):
         self._chk(self.lib.pqmc_update_phonon_field(self.h, pf_id, time), "update_phonon_field")
@@ -194,12 +229,12 @@ class PqmcChain:
     def get_g_scratch(self, time: int, forward: bool, loop: int = 1) -> np.ndarray:
         e = np.zeros(2)
         self._chk(self.lib.pqmc_get_g_scratch(self.h, time, int(forward), loop, e.ctypes.data_as(_f64p)),
-                  "get_g_scratch_T0")
+                  "get_g_scratch")
         return e
 
     def cal_new_weight(self) -> complex:
         o = np.zeros(2)
-        self._chk(self.lib.pqmc_cal_new_weight(self.h, o.ctypes.data_as(_f64p)), "cal_new_weight_T0")
+        self._chk(self.lib.pqmc_cal_new_weight(self.h, o.ctypes.data_as(_f64p)), "cal_new_weight")
         return complex(o[0], o[1])
 
     def set_field_device(self, ptr: int):

@@ -70,25 +70,41 @@ __global__ void k_ft_fill(int n, cplx* v, cplx val) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = val;
 }
 
-// X(:, j) *= d(j), and norm(j) = |X(:, j)| after the scaling; one CTA per column
+// X(:, j) *= d(j), and norm(j) = |X(:, j)| after the scaling, taken as
+// max |x| * |x / max| (the entries of a graded string pass 1e154, where
+// the plain sum of squares overflows); one CTA of 256 threads per column
 __global__ void k_ft_colscale_norm(int n, cplx* X, const cplx* __restrict__ d, double* norm) {
   __shared__ double red[256];
   const int j = blockIdx.x;
   const cplx dj = d[j];
   cplx* x = X + (size_t)n * j;
-  double s = 0.0;
+  double mx = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const cplx v = cmul(x[i], dj);
     x[i] = v;
-    s += cabs2(v);
+    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
   }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  mx = red[0];
+  __syncthreads();
+  double s = 0.0;
+  if (mx > 0.0)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double a = x[i].x / mx, b = x[i].y / mx;
+      s += a * a + b * b;
+    }
   red[threadIdx.x] = s;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) norm[j] = sqrt(red[0]);
+  if (threadIdx.x == 0) norm[j] = mx * sqrt(red[0]);
 }
 
 // perm(rank) = j with columns ranked by decreasing norm, ties by index; a

@@ -16,6 +16,11 @@ pytestmark = pytest.mark.gpu
 
 G_TOL = 1e-10
 W_TOL = 1e-9
+# Im ln_cw is reduced modulo 2 pi in single precision, as the reference
+# reduces it (mod(aimag, 2*pi), src/mod_evolution.f90:626); two evaluations
+# whose phases differ by k whole turns before the reduction differ by
+# k (2 pi_sp - 2 pi) = k * 1.75e-7 after it.  The phase check allows 50 turns.
+PHASE_TOL = 50 * 1.75e-7 + 1e-9
 
 
 def _pair(builder, **kw):
@@ -50,7 +55,7 @@ def test_init_g_ft_matches_oracle_and_dense(name, builder, kw):
     assert rel_fro(g.g(), gd) < G_TOL
     w = g.state()["ln_cw"]
     assert abs(w.real - lo.real) <= W_TOL * abs(lo.real) + 1e-9
-    assert abs(np.exp(1j * w.imag) - np.exp(1j * lo.imag)) < 1e-8
+    assert abs(np.exp(1j * w.imag) - np.exp(1j * lo.imag)) < PHASE_TOL
     wn = g.cal_new_weight()                       # cal_new_weight_FT
     assert abs(wn.real - lo.real) <= W_TOL * abs(lo.real) + 1e-9
     assert rel_fro(g.g(), go) < G_TOL             # G untouched by the weight

@@ -1152,14 +1152,14 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
 // item x column item) in place with the arithmetic of k_bwrap, entry for
 // entry, and writes the columns back with bulk stores.  Every entry of G is
 // read and written once, in whole columns.
-constexpr int WRAPC_C = 2;
+constexpr int WRAPC_C = 1;
 constexpr size_t WRAPC_MAX_SMEM = 200 * 1024;   // dynamic shared memory of k_bwrap_cols at most
 __host__ __device__ inline size_t wrapc_smem(int ns, int n_items, int dim) {
   return (size_t)WRAPC_C * dim * ns * 16 + (size_t)dim * dim * (n_items + WRAPC_C) * 16 + (size_t)n_items * 6 * 4;
 }
 
 template <int DIM, int DF>
-__global__ void __launch_bounds__(128, 3) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
+__global__ void __launch_bounds__(128, 4) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
                                                     const int* __restrict__ wpla, const int* __restrict__ wsites,
                                                     const int* __restrict__ wdim, const float4* __restrict__ tab_all) {
   __shared__ BDesc sd;

@@ -76,9 +76,9 @@ __device__ __forceinline__ dfc dfc_inv(dfc a) {
 //           double-float from every product's exact parts, so V1 = W^-1 to
 //           ~|I - W V0|^2; then M = Delta_S V1 and the Ozaki slices of M's
 //           columns (the B operand of X = G(:,S) M).
-// The CTAs of k_xres past the slabs cut the rows of G(:,S) (the A operand of
-// X) and the columns of Z = E_S - G(S,:) (the B operand of the flush, a warp
-// per column); these depend on G and S only.
+// The rows of G(:,S) (the A operand of X) and the columns of Z = E_S - G(S,:)
+// (the B operand of the flush) depend on G and S only and are cut by
+// k_xslice, launched before both.
 constexpr int XC_THREADS = 1024;
 constexpr int XC_LD = UM_KP;   // leading dimension of the K x K matrices
 constexpr int XR_CTAS = 8;     // column slabs of the Newton step per chain
@@ -189,50 +189,68 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
   }
 }
 
-// the Ozaki slices of G(:,S) (the A operand of X = G(:,S) M; CTA index
-// cta <= n_a, a thread per row) and of Z = E_S - G(S,:) (the B operand of
-// the flush; a warp per column); they depend on G and S only
-__device__ __forceinline__ void x_slice_gz(const XDesc& d, const float4* G, int K, int cta, int n_a, int tid) {
-  const int ns = d.ns, lane = tid & 31, warp = tid >> 5;
+// k_xslice: the Ozaki slices of G(:,S) (the A operand of X = G(:,S) M) and
+// of Z = E_S - G(S,:) (the B operand of the flush).  They depend on G and S
+// only, so they run in their own light launch (256 threads, no dynamic
+// shared memory, several CTAs per SM beside the other kernels) instead of
+// inside the Newton step's 512-thread CTAs.
+//   CTAs 0 .. XS_RCTAS-1 (per 16 rows): 16 threads per row, 4 k each; the
+//   row's exponent from the largest |hi| over its K entries (a max over the
+//   16 lanes of the row), then 8-byte stores of 4 BF16 per slice.
+//   CTAs past them (per 8 columns): a warp per column of Z, 2 k per lane.
+constexpr int XS_THREADS = 256;
+constexpr int XS_ROWS = XS_THREADS / 16;   // rows of G(:,S) per CTA
+constexpr int XS_COLS = XS_THREADS / 32;   // columns of Z per CTA
+__global__ void __launch_bounds__(XS_THREADS, 4) k_xslice(const XDesc* X, int parity, int n_rcta) {
+  const XDesc& d = X[blockIdx.y];
+  const int K = *d.kcount;
+  if (K == 0) return;
+  const float4* G = parity ? d.g_alt : d.g;
+  const int ns = d.ns, tid = threadIdx.x, lane = tid & 31;
   const int K16 = (K + 15) & ~15;
-  if (cta <= n_a) {
+  const int* S = d.acc_site;
+  if ((int)blockIdx.x < n_rcta) {
     // ---- rows of G(:,S): A operand of X = G(:,S) M ------------------------
-    const int r = (cta - 1) * XR_THREADS + tid;
-    if (r >= ns) return;
-    const int* S = d.acc_site;
+    const int r = blockIdx.x * XS_ROWS + tid / 16, q = tid % 16;   // k = 4q .. 4q+3
+    const bool row_ok = r < ns;
+    float4 v[4];
     float m = 0.f;
-    for (int k = 0; k < K; ++k) {
-      const float4 v = G[r + (size_t)ns * S[k]];
-      m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = 4 * q + u;
+      v[u] = (row_ok && k < K) ? G[r + (size_t)ns * S[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+      m = fmaxf(m, fmaxf(fabsf(v[u].x), fabsf(v[u].y)));
     }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));   // the row's 16 lanes
+    if (!row_ok || 4 * q >= K16) return;
     const int e = oz_exp(m);
     const int t = r / 128, row = r % 128, nrg = um_rg(ns, t);
-    for (int kg = 0; kg < K16 / 8; ++kg) {
-      float rs[OZ_S][8], is[OZ_S][8];
+    uint32_t wr[OZ_S][2], wi[OZ_S][2];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int k = kg * 8 + u;
-        const float4 v = k < K ? G[r + (size_t)ns * S[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float qr[OZ_S], qi[OZ_S];
-        oz_split(v.x, v.z, e, qr);
-        oz_split(v.y, v.w, e, qi);
+    for (int h = 0; h < 2; ++h) {
+      float r0[OZ_S], r1[OZ_S], i0[OZ_S], i1[OZ_S];
+      oz_split(v[2 * h].x, v[2 * h].z, e, r0);
+      oz_split(v[2 * h + 1].x, v[2 * h + 1].z, e, r1);
+      oz_split(v[2 * h].y, v[2 * h].w, e, i0);
+      oz_split(v[2 * h + 1].y, v[2 * h + 1].w, e, i1);
 #pragma unroll
-        for (int s = 0; s < OZ_S; ++s) {
-          rs[s][u] = qr[s];
-          is[s][u] = qi[s];
-        }
+      for (int sl = 0; sl < OZ_S; ++sl) {
+        wr[sl][h] = oz_pack2(r0[sl], r1[sl]);
+        wi[sl][h] = oz_pack2(i0[sl], i1[sl]);
       }
+    }
+    const int kg = q / 2, half = (q & 1) * 8;
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) {   // A' row = [Gr | Gi]
-        unsigned char* im = d.img + (size_t)oz_slot_a1(ns, t, s) * UM_IMG;
-        *reinterpret_cast<uint4*>(im + um_off(row, kg * 8, nrg)) = oz_pack8(rs[s]);
-        *reinterpret_cast<uint4*>(im + um_off(row, UM_KP + kg * 8, nrg)) = oz_pack8(is[s]);
-      }
+    for (int sl = 0; sl < OZ_S; ++sl) {   // A' row = [Gr | Gi]
+      unsigned char* im = d.img + (size_t)oz_slot_a1(ns, t, sl) * UM_IMG;
+      *reinterpret_cast<uint2*>(im + um_off(row, kg * 8, nrg) + half) = make_uint2(wr[sl][0], wr[sl][1]);
+      *reinterpret_cast<uint2*>(im + um_off(row, UM_KP + kg * 8, nrg) + half) = make_uint2(wi[sl][0], wi[sl][1]);
     }
     return;
   }
   // ---- columns of Z = E_S - G(S,:): B operand of the flush, a warp each ----
-  const int c = (cta - 1 - n_a) * (XR_THREADS / 32) + warp;
+  const int c = ((int)blockIdx.x - n_rcta) * XS_COLS + (tid >> 5);
   if (c >= ns) return;
   dfc z[2];
   float m = 0.f;
@@ -241,7 +259,7 @@ __device__ __forceinline__ void x_slice_gz(const XDesc& d, const float4* G, int 
     const int k = lane + 32 * h;
     z[h] = dfc_zero();
     if (k < K) {
-      const int sk = d.acc_site[k];
+      const int sk = S[k];
       const dfc g = dg_dfc(G[sk + (size_t)ns * c]);
       z[h] = dfc{sk == c ? df_sub(df{1.f, 0.f}, g.re) : df_neg(g.re), df_neg(g.im)};
       m = fmaxf(m, fmaxf(fabsf(z[h].re.hi), fabsf(z[h].im.hi)));
@@ -258,13 +276,13 @@ __device__ __forceinline__ void x_slice_gz(const XDesc& d, const float4* G, int 
     oz_split(z[h].re.hi, z[h].re.lo, e, qr);
     oz_split(z[h].im.hi, z[h].im.lo, e, qi);
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) {
+    for (int sl = 0; sl < OZ_S; ++sl) {
       // B' re row cc = [Zr | -Zi], im row 8 ncg + cc = [Zi | Zr]
-      unsigned char* im = d.img + (size_t)oz_slot_b2(ns, tj, s) * UM_IMG;
-      *reinterpret_cast<__nv_bfloat16*>(im + um_off(cc, k, nrg)) = __float2bfloat16_rn(qr[s]);
-      *reinterpret_cast<__nv_bfloat16*>(im + um_off(cc, UM_KP + k, nrg)) = __float2bfloat16_rn(-qi[s]);
-      *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, k, nrg)) = __float2bfloat16_rn(qi[s]);
-      *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, UM_KP + k, nrg)) = __float2bfloat16_rn(qr[s]);
+      unsigned char* im = d.img + (size_t)oz_slot_b2(ns, tj, sl) * UM_IMG;
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(cc, k, nrg)) = __float2bfloat16_rn(qr[sl]);
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(cc, UM_KP + k, nrg)) = __float2bfloat16_rn(-qi[sl]);
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, k, nrg)) = __float2bfloat16_rn(qi[sl]);
+      *reinterpret_cast<__nv_bfloat16*>(im + um_off(8 * ncg + cc, UM_KP + k, nrg)) = __float2bfloat16_rn(qr[sl]);
     }
   }
 }
@@ -280,7 +298,7 @@ __device__ __forceinline__ void df_mac_f(float& h, float& l, float ah, float al,
   l = __fmaf_rn(al, b, __fadd_rn(l, __fadd_rn(s.lo, e)));
 }
 
-__global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim, int parity, int n_a) {
+__global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim, int parity) {
   __shared__ XDesc sd;
   __shared__ int s_ce[XR_W];
   __shared__ __align__(8) uint64_t s_bar;
@@ -297,10 +315,6 @@ __global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim,
   const XDesc& d = sd;
   const int K = *d.kcount;
   if (K == 0) return;
-  if ((int)blockIdx.x >= XR_CTAS) {
-    x_slice_gz(d, parity ? d.g_alt : d.g, K, (int)blockIdx.x - XR_CTAS + 1, n_a, tid);
-    return;
-  }
   const int nb = K / dim;
   const int j0 = blockIdx.x * XR_W;   // this CTA's columns j0 .. j0 + XR_W - 1 of M
   float4* W = reinterpret_cast<float4*>(xr_dyn);                     // [K][XC_LD] double-float W
@@ -536,6 +550,15 @@ __global__ void __launch_bounds__(256, 1) k_xgemm(const XDesc* X, int parity) {
   }
   const int q = warp & 3, hf = warp >> 2;
   const int r = ti * 128 + q * 32 + lane;
+  if (MODE == 1 && r < ns) {
+    // the epilogue's G entries into L2 while thread 0 runs the copies and
+    // products (a prefetch holds no registers and cannot fault: every
+    // address is inside the chain's Ns x Ns tile)
+    const float4* G = parity ? d.g_alt : d.g;
+    const int col0 = tj * 64 + hf * 32, ncol = min(32, ns - col0);
+    for (int c = 0; c < ncol; ++c)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(G + r + (size_t)ns * (col0 + c)));
+  }
   __syncthreads();
   const int last = s_last;
   if (last >= 0) {   // every exit path waits for the last commit (it tracks all earlier products)
@@ -643,11 +666,12 @@ int exact_setup() {
 }
 
 int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi) {
-  const int n_a = (ns + XR_THREADS - 1) / XR_THREADS, n_b = (ns + XR_THREADS / 32 - 1) / (XR_THREADS / 32);
+  const int n_r = (ns + XS_ROWS - 1) / XS_ROWS, n_c = (ns + XS_COLS - 1) / XS_COLS;
+  PQMC_CUDA(launch_at(k_xslice, dim3(n_r + n_c, C), dim3(XS_THREADS), 0, st, prio, prio_hi, d_x, parity, n_r));
+  PQMC_LAUNCHED();
   PQMC_CUDA(launch_at(k_xinv, dim3(1, C), dim3(XC_THREADS), XI_SMEM, st, prio, prio_hi, d_x, dim, parity));
   PQMC_LAUNCHED();
-  PQMC_CUDA(launch_at(k_xres, dim3(XR_CTAS + n_a + n_b, C), dim3(XR_THREADS), XR_SMEM, st, prio, prio_hi, d_x, dim,
-                      parity, n_a));
+  PQMC_CUDA(launch_at(k_xres, dim3(XR_CTAS, C), dim3(XR_THREADS), XR_SMEM, st, prio, prio_hi, d_x, dim, parity));
   PQMC_LAUNCHED();
   return PQMC_OK;
 }

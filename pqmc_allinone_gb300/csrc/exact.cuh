@@ -12,8 +12,8 @@
 // are the sequential ratio matrices R_j = I + Geff_j(S_j,S_j) Delta_j of the
 // reference.)  The update is evaluated from the double-float G, never from
 // the scan's FP32 panels:
-//   k_xinv    W in double-float and the FP32 inverse V0 of its rounding; the
-//             Ozaki slices of G(:,S) and of Z = E_S - G(S,:);
+//   k_xslice  the Ozaki slices of G(:,S) and of Z = E_S - G(S,:);
+//   k_xinv    W in double-float and the FP32 inverse V0 of its rounding;
 //   k_xres    one Newton step V1 = V0 + V0 (I - W V0) with a double-float
 //             residual, M = Delta_S V1 and the Ozaki slices of M;
 //   k_xgemm   X = G(:,S) M, then G += X Z, on the tensor cores: every
@@ -59,8 +59,8 @@ __host__ __device__ __forceinline__ size_t oz_chain_bytes(int ns) {
   return (size_t)(2 * um_rtiles(ns) + 1 + um_ctiles(ns)) * OZ_S * UM_IMG;
 }
 
-// The exact update of one round for C chains: exact_core (two launches:
-// W^-1, M and the operand slices) and exact_products (two launches: the
+// The exact update of one round for C chains: exact_core (three launches:
+// the operand slices, W^-1, M) and exact_products (two launches: the
 // tensor-core products).  `prio` marks the launches with priority
 // `prio_hi` (kept as node priorities when the stream is being captured).
 int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi);

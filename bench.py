@@ -423,7 +423,12 @@ def run_mixed(args, world, rank, local):
         depth, table = b.autotune(cur.loop, cur.tc, m.ngroup, cands)
         for _ in cands:
             cur.next()
-        tune = {"candidates_ms_per_slice": table, "chosen": depth}
+        tile, ttable = b.autotune_tiles(cur.loop, cur.tc, m.ngroup)
+        for _ in range(sum(v is not None for v in ttable.values())):   # the blocks the timed tiles ran
+            cur.next()
+        tune = {"candidates_ms_per_slice": table, "chosen": depth,
+                "wrap_tile_ms_per_slice": {b.WRAP_TILES[k]: v for k, v in ttable.items()},
+                "wrap_tile_chosen": b.WRAP_TILES[tile]}
     for _ in range(args.warmup):
         b.sweep_slices(*cur.next(), m.ngroup)
     torch.cuda.synchronize()

@@ -414,6 +414,23 @@ int pqmc_batch_records(pqmc_batch* batch, int i, double* records, int cap, int* 
 int pqmc_batch_autotune(pqmc_batch* batch, int loop, int first_tc, int n_slices,
                         const int* candidates, int n_candidates, int* best,
                         double* ms_out);
+/* Tile shape of the mixed batch's two-way wrap: 1 or 2 column items per
+ * k_bwrap_cols CTA (whole columns of G staged in shared memory; fewer items
+ * let more CTAs share an SM, more items share the row items' tables), or 0
+ * for the gathered form (32 x 4 blocks per CTA).  The same arithmetic for
+ * every entry in every shape: the chains are bit-identical whichever runs.
+ * Shapes whose columns do not fit in shared memory fall back to the largest
+ * that fits.  Default 1 (0 with PQMC_WRAP_COLS=0). */
+int pqmc_batch_set_wrap_tile(pqmc_batch* batch, int ci);
+int pqmc_batch_get_wrap_tile(pqmc_batch* batch, int* ci);
+/* Autotune the tile shapes at the batch's delay depth: every wrap tile
+ * (0, 1, 2) is timed over n_slices slices of sweep `loop` from first_tc
+ * with plain launches (CUDA events on the batch stream; the chains advance
+ * meanwhile), the fastest is kept and written to *best; ms_out (3 entries,
+ * may be NULL) receives the ms per slice of each, -1 where the shape does
+ * not fit.  Uneven batches tune each class; *best is the first class's. */
+int pqmc_batch_autotune_tiles(pqmc_batch* batch, int loop, int first_tc, int n_slices,
+                              int* best, double* ms_out);
 /* slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain */
 int pqmc_batch_sweep_slices(pqmc_batch* batch, int loop, int first_tc, int n_slices);
 /* init_expKV and init_g_T0(1) (mod_evolution.f90:46-111) of every chain

@@ -243,6 +243,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_records": ([vp, ctypes.c_int, _f64p, ctypes.c_int, _i32p], ctypes.c_int),
         "pqmc_batch_autotune": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, ctypes.c_int, _i32p, _f64p],
                                 ctypes.c_int),
+        "pqmc_batch_set_wrap_tile": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_get_wrap_tile": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "pqmc_batch_autotune_tiles": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _f64p],
+                                      ctypes.c_int),
         "pqmc_batch_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "pqmc_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "pqmc_set_field_slices": ([vp, ctypes.c_int, ctypes.c_int, _f64p], ctypes.c_int),

@@ -1151,14 +1151,17 @@ __global__ void __launch_bounds__(128, 3) k_bwrap(const BDesc* D, int pf, int le
 // (B - I) of its column items (FP64, rounded once), updates each block (row
 // item x column item) in place with the arithmetic of k_bwrap, entry for
 // entry, and writes the columns back with bulk stores.  Every entry of G is
-// read and written once, in whole columns.
-constexpr int WRAPC_C = 1;
+// read and written once, in whole columns.  The number of column items per
+// CTA (CI, 1 or 2) is a tile shape chosen by pqmc_batch_autotune_tiles:
+// one item halves the staged columns, so more CTAs share an SM; two items
+// share the row items' (A - I) table between more blocks.
+constexpr int WRAPC_C_DEFAULT = 1;
 constexpr size_t WRAPC_MAX_SMEM = 200 * 1024;   // dynamic shared memory of k_bwrap_cols at most
-__host__ __device__ inline size_t wrapc_smem(int ns, int n_items, int dim) {
-  return (size_t)WRAPC_C * dim * ns * 16 + (size_t)dim * dim * (n_items + WRAPC_C) * 16 + (size_t)n_items * 6 * 4;
+__host__ __device__ inline size_t wrapc_smem(int ns, int n_items, int dim, int ci) {
+  return (size_t)ci * dim * ns * 16 + (size_t)dim * dim * (n_items + ci) * 16 + (size_t)n_items * 6 * 4;
 }
 
-template <int DIM, int DF>
+template <int DIM, int DF, int WRAPC_C>
 __global__ void __launch_bounds__(128, 4) k_bwrap_cols(const BDesc* D, int pf, int left, int n_items, int parity,
                                                     const int* __restrict__ wpla, const int* __restrict__ wsites,
                                                     const int* __restrict__ wdim, const float4* __restrict__ tab_all) {
@@ -1397,7 +1400,8 @@ struct pqmc_batch {
     int kernels;  // kernel nodes per replay
   };
   bool graphs = false;
-  std::vector<char> wrap_cols;   // per family: k_bwrap_cols (columns of G fit in shared memory) or k_bwrap
+  std::vector<char> wrap_cols;   // per family: the most column items per k_bwrap_cols CTA whose columns fit (0: k_bwrap)
+  int wrap_ci = 1;               // wrap tile: column items per k_bwrap_cols CTA (1, 2), 0 for the gather form k_bwrap
   std::deque<SliceGraph> gcache;
   // proposal records of every family per chain (n_pf x max_pla); when the
   // families' bosons are disjoint, a slice's draws and proposals of all
@@ -1505,6 +1509,23 @@ static void gphase_end(pqmc_batch* b, int g, int phase, cudaEvent_t a) {
   if (g == 0) phase_end(b, phase, a);
 }
 
+// the dynamic shared-memory limit of every k_bwrap_cols variant of one
+// family dimension and column-item count
+template <int DM>
+static cudaError_t raise_wrapc_dm(int ci, int sm) {
+  cudaError_t e = ci == 1 ? raise_dyn_smem(k_bwrap_cols<DM, 0, 1>, sm) : raise_dyn_smem(k_bwrap_cols<DM, 0, 2>, sm);
+  if (e != cudaSuccess) return e;
+  return ci == 1 ? raise_dyn_smem(k_bwrap_cols<DM, 1, 1>, sm) : raise_dyn_smem(k_bwrap_cols<DM, 1, 2>, sm);
+}
+static cudaError_t raise_wrapc(int dim, int ci, int sm) {
+  switch (dim) {
+    case 1: return raise_wrapc_dm<1>(ci, sm);
+    case 2: return raise_wrapc_dm<2>(ci, sm);
+    case 3: return raise_wrapc_dm<3>(ci, sm);
+    default: return raise_wrapc_dm<4>(ci, sm);
+  }
+}
+
 // two-way wrap of group g's chains by family pf at the group's slice (the
 // caller flips the parity)
 static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
@@ -1531,11 +1552,17 @@ static int bwrap(pqmc_batch* b, int g, int pf, bool left, int parity) {
     }
     PQMC_LAUNCHED();
   }
-  if (pf < (int)b->wrap_cols.size() && b->wrap_cols[pf]) {
-    const dim3 gc((unsigned)((w.n_items + WRAPC_C - 1) / WRAPC_C), (unsigned)C);
-    const size_t sm = wrapc_smem(c0->ns, w.n_items, c0->h_pf_dim[pf]);
-#define PQMC_WC(DM, F) \
-  k_bwrap_cols<DM, F><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim, tab)
+  const int ci = pf < (int)b->wrap_cols.size() ? std::min(b->wrap_ci, (int)b->wrap_cols[pf]) : 0;
+  if (ci > 0) {   // columns staged, ci column items per CTA
+    const dim3 gc((unsigned)((w.n_items + ci - 1) / ci), (unsigned)C);
+    const size_t sm = wrapc_smem(c0->ns, w.n_items, c0->h_pf_dim[pf], ci);
+#define PQMC_WC(DM, F)                                                                                          \
+  do {                                                                                                          \
+    if (ci == 1)                                                                                                \
+      k_bwrap_cols<DM, F, 1><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim, tab); \
+    else                                                                                                        \
+      k_bwrap_cols<DM, F, 2><<<gc, 128, sm, st>>>(D, pf, l, w.n_items, parity, w.d_pla, w.d_sites, w.d_dim, tab); \
+  } while (0)
     switch (c0->h_pf_dim[pf] + (df ? 4 : 0)) {
       case 1: PQMC_WC(1, 0); break;
       case 2: PQMC_WC(2, 0); break;
@@ -2054,19 +2081,16 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
     const char* wenv = getenv("PQMC_WRAP_COLS");
     const bool wc_on = !(wenv && atoi(wenv) == 0);
     b->wrap_cols.assign(c0->n_pf, 0);
+    b->wrap_ci = wc_on ? WRAPC_C_DEFAULT : 0;
     for (int f = 0; f < c0->n_pf && wc_on; ++f) {
       const int dim = c0->h_pf_dim[f];
-      const size_t sm = wrapc_smem(c0->ns, c0->wrap[f].n_items, dim);
-      if (dim < 1 || dim > 4 || sm > WRAPC_MAX_SMEM) continue;
-      cudaError_t e;
-      switch (dim) {
-        case 1: e = raise_dyn_smem(k_bwrap_cols<1, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<1, 1>, (int)sm); break;
-        case 2: e = raise_dyn_smem(k_bwrap_cols<2, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<2, 1>, (int)sm); break;
-        case 3: e = raise_dyn_smem(k_bwrap_cols<3, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<3, 1>, (int)sm); break;
-        default: e = raise_dyn_smem(k_bwrap_cols<4, 0>, (int)sm); if (e == cudaSuccess) e = raise_dyn_smem(k_bwrap_cols<4, 1>, (int)sm); break;
+      if (dim < 1 || dim > 4) continue;
+      for (int ci = 1; ci <= 2; ++ci) {   // the staged tiles whose columns fit
+        const size_t sm = wrapc_smem(c0->ns, c0->wrap[f].n_items, dim, ci);
+        if (sm > WRAPC_MAX_SMEM) break;
+        PQMC_CUDA(raise_wrapc(dim, ci, (int)sm));
+        b->wrap_cols[f] = (char)ci;
       }
-      PQMC_CUDA(e);
-      b->wrap_cols[f] = 1;
     }
   }
   b->h_desc.resize(n_chains);
@@ -2240,6 +2264,82 @@ int pqmc_batch_set_flush(pqmc_batch* b, int mode) {
   }
   for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_flush(p, mode));
   b->flush_mode = mode;
+  return PQMC_OK;
+}
+
+int pqmc_batch_set_wrap_tile(pqmc_batch* b, int ci) {
+  if (!b || ci < 0 || ci > 2) {
+    set_error("batch_set_wrap_tile: 0 (gathered blocks), 1 or 2 (column items per CTA)");
+    return PQMC_ERR_ARG;
+  }
+  for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_wrap_tile(p, ci));
+  if (b->wrap_ci != ci) {   // the slice graphs hold the old wrap launches
+    PQMC_CUDA(cudaStreamSynchronize(b->stream));
+    drop_graphs(b);
+  }
+  b->wrap_ci = ci;
+  return PQMC_OK;
+}
+
+int pqmc_batch_get_wrap_tile(pqmc_batch* b, int* ci) {
+  if (!b || !ci) { set_error("null argument"); return PQMC_ERR_ARG; }
+  *ci = b->parts.empty() ? b->wrap_ci : b->parts[0]->wrap_ci;
+  return PQMC_OK;
+}
+
+int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slices, int* best, double* ms_out) {
+  if (!b || n_slices < 1 || !best) { set_error("batch_autotune_tiles: bad arguments"); return PQMC_ERR_ARG; }
+  if (b->precision != PQMC_PREC_MIXED) { set_error("batch_autotune_tiles: mixed batches only"); return PQMC_ERR_ARG; }
+  if (!b->parts.empty()) {   // every class tunes its own tile; ms_out sums the classes
+    double part_ms[3];
+    if (ms_out)
+      for (int i = 0; i < 3; ++i) ms_out[i] = 0.0;
+    for (size_t k = 0; k < b->parts.size(); ++k) {
+      int bk = 0;
+      PQMC_TRY(pqmc_batch_autotune_tiles(b->parts[k], loop, first_tc, n_slices, &bk, part_ms));
+      if (k == 0) *best = bk;
+      if (ms_out)
+        for (int i = 0; i < 3; ++i) ms_out[i] = (ms_out[i] < 0.0 || part_ms[i] < 0.0) ? -1.0 : ms_out[i] + part_ms[i];
+    }
+    return PQMC_OK;
+  }
+  const int nt = b->chains[0]->ntime;
+  int max_ci = 0;
+  for (char v : b->wrap_cols) max_ci = std::max(max_ci, (int)v);
+  cudaEvent_t e0, e1;
+  PQMC_CUDA(cudaEventCreate(&e0));
+  PQMC_CUDA(cudaEventCreate(&e1));
+  const bool graphs = b->graphs;
+  b->graphs = false;   // plain launches for every candidate, as in pqmc_batch_autotune
+  double best_ms = 1e300;
+  int best_ci = b->wrap_ci, lp = loop, tc = first_tc, st = PQMC_OK;
+  for (int ci = 0; ci <= 2 && st == PQMC_OK; ++ci) {
+    if (ci > max_ci) {
+      if (ms_out) ms_out[ci] = -1.0;
+      continue;
+    }
+    b->wrap_ci = ci;
+    const int n = std::min(n_slices, nt - tc + 1);
+    cudaEventRecord(e0, b->stream);
+    st = pqmc_batch_sweep_slices(b, lp, tc, n);
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per_slice = ms / n;
+    if (ms_out) ms_out[ci] = per_slice;
+    if (per_slice < best_ms) { best_ms = per_slice; best_ci = ci; }
+    tc += n;
+    if (tc > nt) { tc = 1; ++lp; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->graphs = graphs;
+  if (st != PQMC_OK) return st;
+  PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  drop_graphs(b);
+  b->wrap_ci = best_ci;
+  *best = best_ci;
   return PQMC_OK;
 }
 

@@ -387,6 +387,28 @@ class PqmcBatch:
                                                       ms.ctypes.data_as(_f64p)), "pqmc_batch_autotune")
         return int(best[0]), {int(k): float(v) for k, v in zip(cand, ms)}
 
+    WRAP_TILES = {0: "gathered blocks", 1: "1 column item per CTA", 2: "2 column items per CTA"}
+
+    def set_wrap_tile(self, ci: int):
+        """Tile shape of the two-way wrap: 1 or 2 column items per staged CTA,
+        0 for the gathered form (bit-identical results in every shape)."""
+        check(self.lib, self.lib.pqmc_batch_set_wrap_tile(self.h, ci), "pqmc_batch_set_wrap_tile")
+
+    def wrap_tile(self) -> int:
+        v = ctypes.c_int(0)
+        check(self.lib, self.lib.pqmc_batch_get_wrap_tile(self.h, ctypes.byref(v)), "pqmc_batch_get_wrap_tile")
+        return int(v.value)
+
+    def autotune_tiles(self, loop: int, first_tc: int, n_slices: int):
+        """Tile-shape autotuner at the current delay depth: every wrap tile
+        timed over n_slices slices from (loop, first_tc); keeps the fastest.
+        Returns (best tile, {tile: ms per slice or None where it does not fit})."""
+        ms = np.zeros(3)
+        best = ctypes.c_int(0)
+        check(self.lib, self.lib.pqmc_batch_autotune_tiles(self.h, loop, first_tc, n_slices, ctypes.byref(best),
+                                                            ms.ctypes.data_as(_f64p)), "pqmc_batch_autotune_tiles")
+        return int(best.value), {k: (float(v) if v >= 0 else None) for k, v in enumerate(ms)}
+
     def set_measure(self, warmup: int, meas_interval: int = 1, meas_number: int = 0):
         """Equal-time measurements in batched sweeps (chains built with meas=True)."""
         check(self.lib, self.lib.pqmc_batch_set_measure(self.h, warmup, meas_interval, meas_number),

@@ -236,6 +236,41 @@ def test_wrap_column_staging_bit_identical(monkeypatch):
         assert s0["positive_accept"] > 0
 
 
+def test_wrap_tiles_bit_identical_and_autotuned():
+    """Every tile shape of the wrap (gathered blocks, 1 or 2 column items per
+    staged CTA) gives the same chains bit for bit, graphs included; the tile
+    autotuner times each, keeps the fastest and the run continues from it."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(3):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=150 + i)
+        ms.append((m, f, seed_words(1500 + i)))
+    runs = []
+    for ci in (0, 1, 2):
+        b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+        b.set_wrap_tile(ci)
+        assert b.wrap_tile() == ci
+        b.init()
+        for loop in (1, 2):
+            b.sweep(loop)
+        runs.append([(c.field(), c.g(), c.state()) for c in b.chains])
+        b.close()
+    for other in runs[1:]:
+        for (f0, g0, s0), (f1, g1, s1) in zip(runs[0], other):
+            assert np.array_equal(f0, f1) and np.array_equal(g0, g1)
+            assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    b.init()
+    best, table = b.autotune_tiles(1, 1, 5)
+    assert best in (0, 1, 2) and b.wrap_tile() == best
+    assert all(v is not None and v > 0 for v in table.values())
+    assert table[best] == min(table.values())
+    b.sweep_slices(1, 16, 5)
+    b.sweep(2)
+    assert all(0.0 < c.state()["err_g_rel_max"] < 1e-8 for c in b.chains)
+    b.close()
+
+
 def test_launch_priorities_bit_identical(monkeypatch):
     """The family-step kernels launched at the highest stream priority (node
     priorities in the slice graphs) and every kernel at the default priority:

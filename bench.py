@@ -676,16 +676,25 @@ def run_uneven(args, world, rank, local):
     t0 = time.perf_counter()
     b.init()
     t_init = time.perf_counter() - t0
-    # autotune on the first blocks of sweep 1, then finish sweep 1
-    cands = (32, 64, 96) if args.delay == 0 else (args.delay,)
+    # autotune on the first blocks of sweep 1 (depth, then the wrap tile),
+    # then finish sweep 1 from the slice the timed candidates reached (a
+    # candidate the round update cannot take is skipped and runs no slices)
+    if args.delay:
+        cands = (args.delay,)
+    else:
+        cands = (16, 32, 48, 64) if args.flush in (1, 2) else (32, 64, 96)
     best, table = b.autotune(1, 1, 10, cands)
-    b.sweep_slices(1, 1 + 10 * len(cands), max(m.ntime for m, _, _ in ms))
+    tc = 1 + 10 * sum(1 for v in table.values() if v >= 0)
+    tile, ttable = b.autotune_tiles(1, tc, 10)
+    tc += 10 * sum(1 for v in ttable.values() if v is not None)
+    b.sweep_slices(1, tc, max(m.ntime for m, _, _ in ms))
     loop = 2
     for _ in range(args.warmup):
         b.sweep(loop)
         loop += 1
     torch.cuda.synchronize()
     st0 = [c.state() for c in b.chains]
+    rounds0 = b.flush_rounds()
     n0 = kernel_launches()
     stream = torch.cuda.ExternalStream(b.stream())
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -708,9 +717,40 @@ def run_uneven(args, world, rank, local):
     acc = sum(s1["positive_accept"] - s0["positive_accept"] for s0, s1 in zip(st0, st1))
     rej = sum(s1["negative_accept"] - s0["negative_accept"] for s0, s1 in zip(st0, st1))
     drift = max(s["err_g_rel_max"] for s in st1)
+    rounds = [r1 - r0 for r0, r1 in zip(rounds0, b.flush_rounds())]
     classes = b.classes()
     n_graphs = b.graph_count()
     b.close()
+    # step-level roofline: the round updates' and the wraps' algorithmic G
+    # traffic (double-float G read + write, 32 Ns^2 bytes per pass) over the
+    # step time; the scan and the recompute share the GPU meanwhile
+    pk = peaks()
+    g_bytes = sum(32.0 * m.ns * m.ns * (r + len(m.pf) * m.ntime * args.steps) for (m, _, _), r in zip(ms, rounds))
+    achieved = g_bytes / (t_step * args.steps) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": None,
+            "kernel": "whole step: k_xgemm<1> (round updates, one G pass per round with columns, device-counted) "
+                      "and the wraps (one G pass per family and slice)",
+            "algorithmic": "32*Ns^2 bytes per G pass (double-float read + write), summed over chains, over the "
+                           "timed steps' event time; not a per-kernel figure (no phase timers in this mode)",
+            "rounds_with_columns": int(sum(rounds)), "peak_source": f"{pk['source']} HBM copy bandwidth"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        # the oracle on the host cores for one chain of each L of the mix
+        # (20 slices each), scaled to the mix: core-seconds of one sweep of
+        # every chain = sum_i Lt_i * (seconds per slice per core for L_i)
+        per_slice, samples = {}, []
+        for L in (8, 10, 12):
+            x = next((x for x in ms if int(x[0].lat.dlength[0]) == L), None)
+            if x is None:
+                continue
+            cb = cpu_baseline(x[0], x[1], x[2], 20)
+            per_slice[L] = 1.0 / (cb["per_core"] * x[0].ntime)
+            samples.append(f"L={L} (Lt={x[0].ntime}): {cb['sample']}")
+        cores = os.cpu_count() or 1
+        core_s = sum(m.ntime * per_slice[int(m.lat.dlength[0])] for m, _, _ in ms)
+        cpu = {"value": C / (core_s / cores), "unit": "chain-sweeps/s", "cores": cores, "kind": "port",
+               "sample": "; ".join(samples) + f"; scaled to the {C}-chain mix by Lt, {cores} chains at a time"}
     # plain FP64 single chains on a sample (one chain per L at Lt=200, one
     # sweep each), scaled to the batch's mix by Lt: the sequential FP64 form
     plain = None
@@ -768,7 +808,10 @@ def run_uneven(args, world, rank, local):
                       "chains_by_L": {L: Ls.count(L) for L in (8, 10, 12)},
                       "chains_by_Lt": {t: Lts.count(t) for t in (200, 400, 600)},
                       "classes": classes, "graphs": bool(args.graphs), "slice_graphs_held": n_graphs,
-                      "autotune": {"candidates_ms_per_slice_summed_over_classes": table, "class0_depth": best},
+                      "autotune": {"candidates_ms_per_slice_summed_over_classes": table, "class0_depth": best,
+                                   "wrap_tile_ms_per_slice_summed_over_classes":
+                                       {b.WRAP_TILES[k]: v for k, v in ttable.items()},
+                                   "class0_wrap_tile": b.WRAP_TILES[tile]},
                       "step": "one sweep of every chain (its own Lt slices, one recompute per 10 slices)",
                       "l2": "no flush: the batch's G, expKV and Q strings (tens of GB) far exceed the 129 MB L2",
                       "parallelism": f"replicas x{world}"},
@@ -776,7 +819,7 @@ def run_uneven(args, world, rank, local):
            "speedup_vs_plain_fp64": (C / t_step / plain["value"]) if plain else None,
            "g_error": {"fast_path_drift_rel_max": drift},
            "accept_ratio": acc / max(1, acc + rej), "models_s": t_models, "init_s": t_init,
-           "roofline": None, "cpu_baseline": None, "e2e": None}
+           "roofline": roof, "cpu_baseline": cpu, "e2e": None}
     print(json.dumps(out))
 
 
@@ -814,13 +857,44 @@ def run_adjoint(args, world, rank, local):
     dt = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
     if rank != 0:
         return
+    # FP64 roofline: complex multiply-adds per gradient, counted from the
+    # algorithm (8 flop each): the right-to-left pass propagates P (Ns x
+    # nelec) through every family of every slice (dim Ns nelec each); the
+    # left-to-right pass propagates the running right factor the same way and
+    # wraps G (Ns x Ns) through every family (2 dim Ns^2 each); the
+    # Householder QR of each block and the G rebuild per block are ignored
+    dims = [t.dim for t in m.pf]
+    cmac = m.ntime * sum(2 * d * m.ns * m.nelec + 2 * d * m.ns * m.ns for d in dims)
+    flops = 8.0 * cmac
+    achieved = B * flops / dt / 1e9
+    roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
+            "frac": achieved / FP64_PEAK_GFLOPS, "traffic": None,
+            "algorithmic": f"{flops / 1e9:.2f} GFLOP per gradient: 8 flop x Lt x sum over families of "
+                           "(2 dim Ns nelec + 2 dim Ns^2) complex multiply-adds (both passes' propagation and "
+                           "the G wraps; QR and per-block G rebuilds not counted)",
+            "peak_source": "FP64 FMA loop over all SMs measured on this GPU (1010.8 GFLOP/s)"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the reference has no gradient: its route is central differences of
+        # cal_new_weight_T0, 2 n_bf Lt weight evaluations per gradient
+        from oracle.oracle import OracleChain
+        o = OracleChain(m, field=fields[0], seed_words=seed_words(5000), meas=False)
+        o.init_expkv()
+        o.init_g(1)
+        ta = time.perf_counter()
+        o.cal_new_weight()
+        tw = time.perf_counter() - ta
+        n_eval = 2 * m.n_bf * m.ntime
+        cpu = {"value": 1.0 / (tw * n_eval), "unit": "chain-gradients/s", "cores": 1, "kind": "port",
+               "sample": f"one oracle cal_new_weight_T0 at 10x10, Lt=400 ({tw:.3f} s on one core); a gradient by "
+                         f"central differences needs 2 n_bf Lt = {n_eval} of them (the reference has no adjoint)"}
     out = {"metric": "log-weight gradients/s (forward + adjoint) @10x10 Lt=400", "value": world * B / dt,
            "unit": "chain-gradients/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": dt * 1000.0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "c128", "data": "synthetic (x ~ N(0,0.5^2), seeds 5000+i)",
            "config": {"workload": f"10x10 SOC EPSOCZ, Lt=400, {B} chains, checkpoint every ngroup=10 slices",
                       "ns": m.ns, "nelec": m.nelec, "ntime": m.ntime, "chains": B},
-           "gpu_launches": int(kernel_launches() - n0), "roofline": None, "cpu_baseline": None, "e2e": None}
+           "gpu_launches": int(kernel_launches() - n0), "roofline": roof, "cpu_baseline": cpu, "e2e": None}
     print(json.dumps(out))
 
 

@@ -29,7 +29,30 @@ struct GemmArgs {
   int out_df;   // C is written in the double-float float4 form (not accumulated)
   int shape;    // 0 general; 1 only the lower triangle of C is needed (Gram
                 // matrix for a Cholesky factor); 2 B is upper triangular
+  // A and B already split into double-float (re.hi, re.lo, im.hi, im.lo),
+  // same layout and leading dimension (set by BatchRecompute::gemm)
+  const float4* Adf = nullptr;
+  const float4* Bdf = nullptr;
 };
+
+// one operand of one chain split into double-float once per GEMM, so that
+// the k-tiles of every CTA that reads it stage it without FP64 instructions
+// (a double -> float pair conversion issues on the FP64 pipe, 1/64 of the
+// FP32 rate on this GPU, and each element is staged by every CTA of its
+// row or column of tiles)
+struct ConvArgs {
+  const cplx* src;
+  float4* dst;
+  long n;
+};
+__global__ void k_gemm_split(const ConvArgs* args) {
+  const ConvArgs a = args[blockIdx.y];
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.n; e += (long)gridDim.x * blockDim.x) {
+    const cplx v = a.src[e];
+    const df vr = df_make(v.x), vi = df_make(v.y);
+    a.dst[e] = make_float4(vr.hi, vr.lo, vi.hi, vi.lo);
+  }
+}
 
 // Batched complex GEMM with FP64-class accuracy on the FP32 pipe: the
 // operands are split into double-float (hi + lo), every real product is
@@ -80,6 +103,15 @@ __global__ void __launch_bounds__(256) k_dfgemm2(const GemmArgs* args, int m, in
       int r, q;
       if (TA) { q = e % DG_BK; r = e / DG_BK; } else { r = e % DG_BM; q = e / DG_BM; }
       const int gr = row0 + r, gk = kk + q;
+      if (g.Adf) {   // the split of df_make, bit for bit (conj negates both parts)
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gr < m && gk < k) {
+          v = TA ? g.Adf[gk + (size_t)g.lda * gr] : g.Adf[gr + (size_t)g.lda * gk];
+          if (TA) v = make_float4(v.x, v.y, -v.z, -v.w);
+        }
+        sA[q][r] = v;
+        continue;
+      }
       cplx v = mk(0.0);
       if (gr < m && gk < k) v = TA ? cconj(g.A[gk + (size_t)g.lda * gr]) : g.A[gr + (size_t)g.lda * gk];
       const df vr = df_make(v.x), vi = df_make(v.y);
@@ -89,6 +121,15 @@ __global__ void __launch_bounds__(256) k_dfgemm2(const GemmArgs* args, int m, in
       int q, c;
       if (TB) { c = e % DG_BN; q = e / DG_BN; } else { q = e % DG_BK; c = e / DG_BK; }
       const int gc = col0 + c, gk = kk + q;
+      if (g.Bdf) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gc < n && gk < k) {
+          v = TB ? g.Bdf[gc + (size_t)g.ldb * gk] : g.Bdf[gk + (size_t)g.ldb * gc];
+          if (TB) v = make_float4(v.x, v.y, -v.z, -v.w);
+        }
+        sB[q][c] = v;
+        continue;
+      }
       cplx v = mk(0.0);
       if (gc < n && gk < k) v = TB ? cconj(g.B[gc + (size_t)g.ldb * gk]) : g.B[gk + (size_t)g.ldb * gc];
       const df vr = df_make(v.x), vi = df_make(v.y);
@@ -890,7 +931,7 @@ __global__ void k_bweight(const WeightArgs* args, int ndcount, long ng, int comp
 // ---------------------------------------------------------------------------
 BatchRecompute::~BatchRecompute() {
   void* ps[] = {d_gemm, d_chol, d_gj, d_prop, d_weight, work_df, tmpX, gram, rinv, pbp, wmat, logdet, piv, perm,
-                status, ekv_df};
+                status, ekv_df, d_conv, split_a, split_b};
   for (void* p : ps)
     if (p) cudaFree(p);
 }
@@ -907,6 +948,9 @@ int BatchRecompute::setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s
     return PQMC_OK;
   };
   PQMC_TRY(al((void**)&d_gemm, sizeof(GemmArgs) * C * 8));
+  PQMC_TRY(al((void**)&d_conv, sizeof(ConvArgs) * C * 2 * 8));
+  PQMC_TRY(al((void**)&split_a, sizeof(float4) * (size_t)C * ns * ne));   // every operand fits in ns x ne
+  PQMC_TRY(al((void**)&split_b, sizeof(float4) * (size_t)C * ns * ne));
   PQMC_TRY(al((void**)&d_chol, sizeof(CholArgs) * C));
   PQMC_TRY(al((void**)&d_gj, sizeof(GJArgs) * C * 2));
   PQMC_TRY(al((void**)&d_prop, sizeof(PropArgs) * C * 2));
@@ -960,7 +1004,33 @@ static inline cplx* dblk(pqmc_chain* c, int b1) { return c->d_string + (size_t)c
 
 int BatchRecompute::gemm(char ta, char tb, int m, int n, int k, const std::vector<GemmArgs>& a, int slot,
                          int accumulate) {
-  PQMC_CUDA(cudaMemcpyAsync(d_gemm + slot * C, a.data(), sizeof(GemmArgs) * C, cudaMemcpyHostToDevice, stream));
+  // split A and B of every chain into double-float once (B shares A's split
+  // when they are the same matrix, as in the Gram matrix X^H X)
+  const long na = (long)a[0].lda * (ta == 'C' ? m : k), nb = (long)a[0].ldb * (tb == 'C' ? k : n);
+  const long cap = (long)ns * ne;
+  std::vector<GemmArgs> g(a);
+  std::vector<ConvArgs> cv;
+  cv.reserve(2 * C);
+  if (na <= cap && nb <= cap) {
+    for (int i = 0; i < C; ++i) {
+      float4* da = split_a + (size_t)i * cap;
+      float4* db = split_b + (size_t)i * cap;
+      cv.push_back(ConvArgs{a[i].A, da, na});
+      g[i].Adf = da;
+      if (a[i].B == a[i].A && na == nb) {
+        g[i].Bdf = da;
+      } else {
+        cv.push_back(ConvArgs{a[i].B, db, nb});
+        g[i].Bdf = db;
+      }
+    }
+    ConvArgs* dc = d_conv + (size_t)slot * 2 * C;
+    PQMC_CUDA(cudaMemcpyAsync(dc, cv.data(), sizeof(ConvArgs) * cv.size(), cudaMemcpyHostToDevice, stream));
+    const long mx = std::max(na, nb);
+    k_gemm_split<<<dim3((unsigned)std::min<long>((mx + 255) / 256, 256), (unsigned)cv.size()), 256, 0, stream>>>(dc);
+    PQMC_LAUNCHED();
+  }
+  PQMC_CUDA(cudaMemcpyAsync(d_gemm + slot * C, g.data(), sizeof(GemmArgs) * C, cudaMemcpyHostToDevice, stream));
   return dfgemm_batched(stream, ta, tb, m, n, k, d_gemm + slot * C, C, accumulate);
 }
 

@@ -7,6 +7,7 @@ struct dfc;
 
 namespace pqmc {
 struct GemmArgs;
+struct ConvArgs;
 struct CholArgs;
 struct GJArgs;
 struct PropArgs;
@@ -17,6 +18,9 @@ struct BatchRecompute {
   cudaStream_t stream = nullptr;
   std::vector<pqmc_chain*> cs;
   GemmArgs* d_gemm = nullptr;
+  ConvArgs* d_conv = nullptr;       // the operand splits of each GEMM slot
+  float4* split_a = nullptr;        // A and B of a GEMM in double-float, per chain (ns x ne each)
+  float4* split_b = nullptr;
   CholArgs* d_chol = nullptr;
   GJArgs* d_gj = nullptr;
   PropArgs* d_prop = nullptr;

@@ -318,10 +318,36 @@ def test_uneven_batch_matches_its_classes():
             assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
     for (m, _, w), (f, g, s) in zip(ms, mixed):
         assert s["positive_accept"] > 0 and s["negative_accept"] > 0
+        assert 0.0 < s["err_g_rel_max"] < MIXED_DRIFT_TOL[2], s   # the exact round update in every class
         o = OracleChain(m, field=f, seed_words=w, meas=False)
         o.init_expkv()
         o.init_g(1)
         assert rel_fro(g, o.g()) < MIXED_RECOMPUTE_TOL
+
+
+def test_uneven_batch_autotune_then_sweeps():
+    """Both autotuners on an uneven batch (every class tunes its own depth
+    and wrap tile on genuine slices), then the rest of the sweep from the
+    slice the timed candidates reached: the fast path stays within the
+    drift bound in every class."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    geo = [(4, 80), (6, 80), (4, 80), (6, 80)]
+    ms = []
+    for i, (L, nt) in enumerate(geo):
+        m, f = epsocz_small(L=L, ntime=nt, ngroup=10, lam=0.8, alpha=0.3, seed=1100 + i)
+        ms.append((m, f, seed_words(1100 + i)))
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    b.init()
+    best, table = b.autotune(1, 1, 10, (16, 32, 64, 96))
+    assert table[96] < 0 and best in (16, 32, 64)   # 96 columns exceed the exact round update
+    tc = 1 + 10 * sum(1 for v in table.values() if v >= 0)
+    tile, ttable = b.autotune_tiles(1, tc, 10)
+    tc += 10 * sum(1 for v in ttable.values() if v is not None)
+    assert tc <= 80
+    b.sweep_slices(1, tc, 80 - tc + 1)
+    b.sweep(2)
+    assert all(0.0 < c.state()["err_g_rel_max"] < MIXED_DRIFT_TOL[2] for c in b.chains)
+    b.close()
 
 
 def test_fp64_uneven_batch_matches_oracle():

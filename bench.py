@@ -423,12 +423,14 @@ def run_mixed(args, world, rank, local):
         depth, table = b.autotune(cur.loop, cur.tc, m.ngroup, cands)
         for _ in cands:
             cur.next()
-        tile, ttable = b.autotune_tiles(cur.loop, cur.tc, m.ngroup)
-        for _ in range(sum(v is not None for v in ttable.values())):   # the blocks the timed tiles ran
+        (tile, ftile), ttable, ftable = b.autotune_tiles(cur.loop, cur.tc, m.ngroup)
+        for _ in range(b.tiles_timed(ttable, ftable)):   # the blocks the timed tiles ran
             cur.next()
         tune = {"candidates_ms_per_slice": table, "chosen": depth,
                 "wrap_tile_ms_per_slice": {b.WRAP_TILES[k]: v for k, v in ttable.items()},
-                "wrap_tile_chosen": b.WRAP_TILES[tile]}
+                "wrap_tile_chosen": b.WRAP_TILES[tile],
+                "flush_tile_ms_per_slice": {f"{k} columns per CTA": v for k, v in ftable.items()},
+                "flush_tile_chosen": f"{ftile} columns per CTA"}
     for _ in range(args.warmup):
         b.sweep_slices(*cur.next(), m.ngroup)
     torch.cuda.synchronize()
@@ -685,8 +687,8 @@ def run_uneven(args, world, rank, local):
         cands = (16, 32, 48, 64) if args.flush in (1, 2) else (32, 64, 96)
     best, table = b.autotune(1, 1, 10, cands)
     tc = 1 + 10 * sum(1 for v in table.values() if v >= 0)
-    tile, ttable = b.autotune_tiles(1, tc, 10)
-    tc += 10 * sum(1 for v in ttable.values() if v is not None)
+    (tile, ftile), ttable, ftable = b.autotune_tiles(1, tc, 10)
+    tc += 10 * b.tiles_timed(ttable, ftable)
     b.sweep_slices(1, tc, max(m.ntime for m, _, _ in ms))
     loop = 2
     for _ in range(args.warmup):
@@ -811,7 +813,10 @@ def run_uneven(args, world, rank, local):
                       "autotune": {"candidates_ms_per_slice_summed_over_classes": table, "class0_depth": best,
                                    "wrap_tile_ms_per_slice_summed_over_classes":
                                        {b.WRAP_TILES[k]: v for k, v in ttable.items()},
-                                   "class0_wrap_tile": b.WRAP_TILES[tile]},
+                                   "class0_wrap_tile": b.WRAP_TILES[tile],
+                                   "flush_tile_ms_per_slice_summed_over_classes":
+                                       {f"{k} columns per CTA": v for k, v in ftable.items()},
+                                   "class0_flush_tile": f"{ftile} columns per CTA"},
                       "step": "one sweep of every chain (its own Lt slices, one recompute per 10 slices)",
                       "l2": "no flush: the batch's G, expKV and Q strings (tens of GB) far exceed the 129 MB L2",
                       "parallelism": f"replicas x{world}"},

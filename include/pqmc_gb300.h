@@ -423,12 +423,22 @@ int pqmc_batch_autotune(pqmc_batch* batch, int loop, int first_tc, int n_slices,
  * that fits.  Default 1 (0 with PQMC_WRAP_COLS=0). */
 int pqmc_batch_set_wrap_tile(pqmc_batch* batch, int ci);
 int pqmc_batch_get_wrap_tile(pqmc_batch* batch, int* ci);
+/* Flush tile of the exact round update: 64 columns of G per CTA (one CTA
+ * per SM: 3 x 128 tensor-memory columns, 160 KB of slice images in two
+ * stages) or 32 (two CTAs per SM: 3 x 64 columns, 60 KB stages of a quarter
+ * of the inner dimension).  Default 64.  The two sum the rounded level of
+ * the Ozaki products in another order, so chains agree to its rounding
+ * (~2^-40 of the update), not bit for bit. */
+int pqmc_batch_set_flush_tile(pqmc_batch* batch, int ct);
+int pqmc_batch_get_flush_tile(pqmc_batch* batch, int* ct);
 /* Autotune the tile shapes at the batch's delay depth: every wrap tile
- * (0, 1, 2) is timed over n_slices slices of sweep `loop` from first_tc
- * with plain launches (CUDA events on the batch stream; the chains advance
- * meanwhile), the fastest is kept and written to *best; ms_out (3 entries,
- * may be NULL) receives the ms per slice of each, -1 where the shape does
- * not fit.  Uneven batches tune each class; *best is the first class's. */
+ * (0, 1, 2), then, with the exact round update, every flush tile (64, 32),
+ * each timed over n_slices slices of sweep `loop` from first_tc with plain
+ * launches (CUDA events on the batch stream; the chains advance meanwhile);
+ * the fastest of each is kept.  best (2 entries) receives the wrap tile and
+ * the flush tile; ms_out (5 entries: wrap 0, 1, 2, flush 64, 32; may be
+ * NULL) the ms per slice of each, -1 where a shape does not fit or does not
+ * apply.  Uneven batches tune each class; best is the first class's. */
 int pqmc_batch_autotune_tiles(pqmc_batch* batch, int loop, int first_tc, int n_slices,
                               int* best, double* ms_out);
 /* slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain */
@@ -544,6 +554,9 @@ int pqmc_cal_g_and_det_noalloc(const double* x_left, const double* rmat, int ns,
  * Ozaki-split BF16 tensor-core products.
  * Limits: 1 <= dim <= 4, k <= 64, k % dim == 0, k <= ns <= 4096. */
 int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g);
+/* The same with the flush tile chosen: 64 (k_xgemm<1>) or 32 (k_xflush2). */
+int pqmc_exact_update_check_tile(int ns, int k, int dim, const int* sites, const double* delta, double* g,
+                                 int flush_tile);
 
 /* ---- introspection --------------------------------------------------- */
 const char* pqmc_version(void);

@@ -247,6 +247,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_get_wrap_tile": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "pqmc_batch_autotune_tiles": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _f64p],
                                       ctypes.c_int),
+        "pqmc_batch_set_flush_tile": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_get_flush_tile": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "pqmc_batch_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "pqmc_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "pqmc_set_field_slices": ([vp, ctypes.c_int, ctypes.c_int, _f64p], ctypes.c_int),
@@ -265,6 +267,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_batch_class_info": ([vp, ctypes.c_int, _i32p], ctypes.c_int),
         "pqmc_batch_graph_count": ([vp, _i32p], ctypes.c_int),
         "pqmc_exact_update_check": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _f64p, _f64p], ctypes.c_int),
+        "pqmc_exact_update_check_tile": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _f64p, _f64p, ctypes.c_int],
+                                         ctypes.c_int),
         "pqmc_version": ([], ctypes.c_char_p),
         "pqmc_last_error": ([], ctypes.c_char_p),
         "pqmc_kernel_launches": ([], ctypes.c_int64),

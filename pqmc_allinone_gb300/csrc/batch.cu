@@ -1402,6 +1402,7 @@ struct pqmc_batch {
   bool graphs = false;
   std::vector<char> wrap_cols;   // per family: the most column items per k_bwrap_cols CTA whose columns fit (0: k_bwrap)
   int wrap_ci = 1;               // wrap tile: column items per k_bwrap_cols CTA (1, 2), 0 for the gather form k_bwrap
+  int xflush_ct = 64;            // flush tile of the exact round update: 64 (k_xgemm<1>) or 32 (k_xflush2) columns
   std::deque<SliceGraph> gcache;
   // proposal records of every family per chain (n_pf x max_pla); when the
   // families' bosons are disjoint, a slice's draws and proposals of all
@@ -1660,12 +1661,14 @@ static int bupdate(pqmc_batch* b, int g, int pf, int parity) {
     }
     if (exact) {   // double-float core and operand slices (timed as the split phase)
       cudaEvent_t tsp = gphase_begin(b, g);
-      PQMC_TRY(exact_core(b->d_xdesc + c_first, C, ns, dim, parity, st, (b->prio_mask & 2) != 0, b->prio_hi));
+      PQMC_TRY(exact_core(b->d_xdesc + c_first, C, ns, dim, parity, b->xflush_ct, st, (b->prio_mask & 2) != 0,
+                          b->prio_hi));
       gphase_end(b, g, PQMC_PHASE_SPLIT, tsp);
     }
     cudaEvent_t tf = gphase_begin(b, g);
     if (exact) {
-      PQMC_TRY(exact_products(b->d_xdesc + c_first, C, ns, parity, st, (b->prio_mask & 2) != 0, b->prio_hi));
+      PQMC_TRY(exact_products(b->d_xdesc + c_first, C, ns, parity, b->xflush_ct, st, (b->prio_mask & 2) != 0,
+                              b->prio_hi));
     } else if (b->flush_mode == 1 && img && kd <= UM_KP) {
       PQMC_CUDA(launch_at(k_bflush_um, dim3(um_rtiles(ns) * um_ctiles(ns), C), dim3(256), (size_t)(6 * UM_HALF), st,
                           (b->prio_mask & 2) != 0, b->prio_hi, Dg, (const unsigned char*)img, parity));
@@ -2287,19 +2290,46 @@ int pqmc_batch_get_wrap_tile(pqmc_batch* b, int* ci) {
   return PQMC_OK;
 }
 
+int pqmc_batch_set_flush_tile(pqmc_batch* b, int ct) {
+  if (!b || (ct != 32 && ct != 64)) {
+    set_error("batch_set_flush_tile: 64 (one CTA per SM) or 32 (two CTAs per SM) columns");
+    return PQMC_ERR_ARG;
+  }
+  for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_flush_tile(p, ct));
+  if (b->xflush_ct != ct) {   // the slice graphs hold the old launches
+    PQMC_CUDA(cudaStreamSynchronize(b->stream));
+    drop_graphs(b);
+  }
+  b->xflush_ct = ct;
+  return PQMC_OK;
+}
+
+int pqmc_batch_get_flush_tile(pqmc_batch* b, int* ct) {
+  if (!b || !ct) { set_error("null argument"); return PQMC_ERR_ARG; }
+  *ct = b->parts.empty() ? b->xflush_ct : b->parts[0]->xflush_ct;
+  return PQMC_OK;
+}
+
+// candidates of pqmc_batch_autotune_tiles, in ms_out order
+static const int TILE_WRAP[3] = {0, 1, 2};
+static const int TILE_FLUSH[2] = {64, 32};
+
 int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slices, int* best, double* ms_out) {
   if (!b || n_slices < 1 || !best) { set_error("batch_autotune_tiles: bad arguments"); return PQMC_ERR_ARG; }
   if (b->precision != PQMC_PREC_MIXED) { set_error("batch_autotune_tiles: mixed batches only"); return PQMC_ERR_ARG; }
-  if (!b->parts.empty()) {   // every class tunes its own tile; ms_out sums the classes
-    double part_ms[3];
+  if (!b->parts.empty()) {   // every class tunes its own tiles; ms_out sums the classes
+    double part_ms[5];
     if (ms_out)
-      for (int i = 0; i < 3; ++i) ms_out[i] = 0.0;
+      for (int i = 0; i < 5; ++i) ms_out[i] = 0.0;
     for (size_t k = 0; k < b->parts.size(); ++k) {
-      int bk = 0;
-      PQMC_TRY(pqmc_batch_autotune_tiles(b->parts[k], loop, first_tc, n_slices, &bk, part_ms));
-      if (k == 0) *best = bk;
+      int bk[2] = {0, 0};
+      PQMC_TRY(pqmc_batch_autotune_tiles(b->parts[k], loop, first_tc, n_slices, bk, part_ms));
+      if (k == 0) {
+        best[0] = bk[0];
+        best[1] = bk[1];
+      }
       if (ms_out)
-        for (int i = 0; i < 3; ++i) ms_out[i] = (ms_out[i] < 0.0 || part_ms[i] < 0.0) ? -1.0 : ms_out[i] + part_ms[i];
+        for (int i = 0; i < 5; ++i) ms_out[i] = (ms_out[i] < 0.0 || part_ms[i] < 0.0) ? -1.0 : ms_out[i] + part_ms[i];
     }
     return PQMC_OK;
   }
@@ -2311,14 +2341,8 @@ int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slice
   PQMC_CUDA(cudaEventCreate(&e1));
   const bool graphs = b->graphs;
   b->graphs = false;   // plain launches for every candidate, as in pqmc_batch_autotune
-  double best_ms = 1e300;
-  int best_ci = b->wrap_ci, lp = loop, tc = first_tc, st = PQMC_OK;
-  for (int ci = 0; ci <= 2 && st == PQMC_OK; ++ci) {
-    if (ci > max_ci) {
-      if (ms_out) ms_out[ci] = -1.0;
-      continue;
-    }
-    b->wrap_ci = ci;
+  int lp = loop, tc = first_tc, st = PQMC_OK;
+  auto time_slices = [&](double* out) {
     const int n = std::min(n_slices, nt - tc + 1);
     cudaEventRecord(e0, b->stream);
     st = pqmc_batch_sweep_slices(b, lp, tc, n);
@@ -2326,20 +2350,43 @@ int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slice
     cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    const double per_slice = ms / n;
-    if (ms_out) ms_out[ci] = per_slice;
-    if (per_slice < best_ms) { best_ms = per_slice; best_ci = ci; }
+    *out = ms / n;
     tc += n;
     if (tc > nt) { tc = 1; ++lp; }
+  };
+  // the wrap tile, then the exact round update's flush tile at the best wrap
+  double best_ms = 1e300;
+  int best_ci = b->wrap_ci;
+  for (int i = 0; i < 3 && st == PQMC_OK; ++i) {
+    double v = -1.0;
+    if (TILE_WRAP[i] <= max_ci) {
+      b->wrap_ci = TILE_WRAP[i];
+      time_slices(&v);
+      if (v < best_ms) { best_ms = v; best_ci = TILE_WRAP[i]; }
+    }
+    if (ms_out) ms_out[i] = v;
   }
+  b->wrap_ci = best_ci;
+  best_ms = 1e300;
+  int best_ct = b->xflush_ct;
+  for (int i = 0; i < 2 && st == PQMC_OK; ++i) {
+    double v = -1.0;
+    if (b->flush_mode == 2) {
+      b->xflush_ct = TILE_FLUSH[i];
+      time_slices(&v);
+      if (v < best_ms) { best_ms = v; best_ct = TILE_FLUSH[i]; }
+    }
+    if (ms_out) ms_out[3 + i] = v;
+  }
+  b->xflush_ct = best_ct;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->graphs = graphs;
   if (st != PQMC_OK) return st;
   PQMC_CUDA(cudaStreamSynchronize(b->stream));
   drop_graphs(b);
-  b->wrap_ci = best_ci;
-  *best = best_ci;
+  best[0] = best_ci;
+  best[1] = best_ct;
   return PQMC_OK;
 }
 

@@ -197,11 +197,12 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
 //   CTAs 0 .. XS_RCTAS-1 (per 16 rows): 16 threads per row, 4 k each; the
 //   row's exponent from the largest |hi| over its K entries (a max over the
 //   16 lanes of the row), then 8-byte stores of 4 BF16 per slice.
-//   CTAs past them (per 8 columns): a warp per column of Z, 2 k per lane.
+//   CTAs past them (per 8 columns): a warp per column of Z, 2 k per lane,
+//   into the column tiles of the flush kernel in use (64 or 32 columns).
 constexpr int XS_THREADS = 256;
 constexpr int XS_ROWS = XS_THREADS / 16;   // rows of G(:,S) per CTA
 constexpr int XS_COLS = XS_THREADS / 32;   // columns of Z per CTA
-__global__ void __launch_bounds__(XS_THREADS, 4) k_xslice(const XDesc* X, int parity, int n_rcta) {
+__global__ void __launch_bounds__(XS_THREADS, 4) k_xslice(const XDesc* X, int parity, int n_rcta, int ct) {
   const XDesc& d = X[blockIdx.y];
   const int K = *d.kcount;
   if (K == 0) return;
@@ -267,7 +268,9 @@ __global__ void __launch_bounds__(XS_THREADS, 4) k_xslice(const XDesc* X, int pa
   }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   const int e = oz_exp(m);
-  const int tj = c / 64, cc = c % 64, ncg = um_cg(ns, tj), nrg = 2 * ncg;
+  // Z's column tiles are ct = 64 (k_xgemm<1>) or 32 (k_xflush2) columns wide,
+  // padded to 8 or 4 column groups (zeros past Ns)
+  const int tj = c / ct, cc = c % ct, ncg = ct == 64 ? um_cg(ns, tj) : 4, nrg = 2 * ncg;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int k = lane + 32 * h;
@@ -657,17 +660,175 @@ __global__ void __launch_bounds__(256, 1) k_xgemm(const XDesc* X, int parity) {
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(taddr) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// k_xflush2: the flush G += X Z over a 128 x 32 tile of G, two CTAs per SM.
+// The three level accumulators take 3 x 64 tensor-memory columns (re at
+// 0..31, im at 32..63 of each level), so one CTA allocates 256 and two share
+// an SM's 512; the images stream through a 60 KB stage a quarter of the
+// inner dimension at a time (4 k groups of A, 128 rows, and of B, 32 re + 32
+// im rows, five slices each), and the epilogue reads 8 columns at a time
+// (at most 128 registers).  One CTA's G read-modify-write then overlaps the
+// other's copies and products.  The same 15 slice pairs and levels as
+// k_xgemm<1>; level 2 sums in another order (stage by stage), so the two
+// agree to its rounding, not bit for bit.
+constexpr int XF_QK = 4;                          // k groups of 8 per stage
+constexpr int XF_A = XF_QK * 16 * 128;            // one A slice of a stage (16 row groups)
+constexpr int XF_B = XF_QK * 8 * 128;             // one B slice of a stage (8 row groups)
+constexpr int XF_SMEM = OZ_S * (XF_A + XF_B);     // 60 KB of stages
+// requested per CTA: 80 KB, so that at most two CTAs share an SM (three
+// would fit by registers and by 60 KB each, but 3 x 256 tensor-memory
+// columns exceed the SM's 512 and the third allocation would wait)
+constexpr int XF_SMEM_LAUNCH = 80 * 1024;
+
+__device__ __forceinline__ void um_ld8_nw(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(256, 2) k_xflush2(const XDesc* X, int parity) {
+  __shared__ XDesc sd;
+  __shared__ __align__(8) uint64_t s_load[4], s_mma[4];
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_fail, s_last;
+  extern __shared__ __align__(1024) unsigned char xf_dyn[];   // OZ_S A stages, then OZ_S B stages
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    sd = X[blockIdx.y];
+    s_fail = 0;
+    s_last = -1;
+    for (int p = 0; p < 4; ++p) {
+      mbar_init(&s_load[p], 1);
+      mbar_init(&s_mma[p], 1);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const XDesc& d = sd;
+  const int K = *d.kcount;
+  if (K == 0) return;   // uniform: no tensor memory taken
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_addr(&s_taddr))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  um_fence_before();
+  __syncthreads();
+  um_fence_after();
+  const uint32_t taddr = s_taddr;
+  const int ns = d.ns, RT = um_rtiles(ns);
+  const int ti = (int)blockIdx.x % RT, tj = (int)blockIdx.x / RT;
+  const int nrg_a = um_rg(ns, ti);
+  const int nkg = ((K + 15) & ~15) / 8;   // k groups of one half (even, <= 8)
+  if (tid == 0) {
+    if (blockIdx.x == 0) atomicAdd(d.nflush, 1ull);
+    const uint32_t ka = (uint32_t)nrg_a * 128, kb = 8u * 128u;   // bytes per k group
+    const uint32_t base = smem_addr(xf_dyn), idesc = um_idesc(64u);
+    uint32_t started = 0;
+    int phase = 0;
+    for (int half = 0; half < 2 && !s_fail; ++half)
+      for (int qk = 0; qk < 2 && !s_fail; ++qk) {
+        const int kg0 = XF_QK * qk, nk = min(XF_QK, nkg - kg0);
+        if (nk <= 0) continue;
+        if (phase > 0) {   // the products of the previous stage have read the buffer
+          if (!mbar_wait_bounded(&s_mma[phase - 1], 0)) {
+            s_fail = 1;
+            break;
+          }
+          um_fence_after();
+        }
+        const uint32_t ba = (uint32_t)nk * ka, bb = (uint32_t)nk * kb;
+        const size_t ga = (size_t)(half * (UM_KP / 8) + kg0) * ka, gb = (size_t)(half * (UM_KP / 8) + kg0) * kb;
+        mbar_arrive_tx(&s_load[phase], (uint32_t)OZ_S * (ba + bb));
+        for (int sl = 0; sl < OZ_S; ++sl) {
+          bulk_g2s(xf_dyn + (size_t)sl * XF_A, d.img + (size_t)oz_slot_a2(ns, ti, sl) * UM_IMG + ga, ba, &s_load[phase]);
+          bulk_g2s(xf_dyn + (size_t)OZ_S * XF_A + (size_t)sl * XF_B, d.img + (size_t)oz_slot_b2(ns, tj, sl) * UM_IMG + gb,
+                   bb, &s_load[phase]);
+        }
+        if (!mbar_wait_bounded(&s_load[phase], 0)) {
+          s_fail = 1;
+          mbar_wait_bounded(&s_load[phase], 0);   // a second bounded wait for the copies in flight
+          break;
+        }
+        um_fence_after();
+        for (int i = 0; i < OZ_S; ++i)
+          for (int j = 0; i + j < OZ_S; ++j) {
+            const int l = min(i + j, 2);
+            for (int kk = 0; kk < nk / 2; ++kk) {
+              const uint64_t ad = um_desc(base + i * XF_A + kk * 2 * ka, ka, 128);
+              const uint64_t bd = um_desc(base + OZ_S * XF_A + j * XF_B + kk * 2 * kb, kb, 128);
+              um_mma(taddr + (uint32_t)(l * 64), ad, bd, idesc, (started >> l) & 1u);
+              started |= 1u << l;
+            }
+          }
+        um_commit(&s_mma[phase]);   // also tracks every earlier product
+        s_last = phase;
+        ++phase;
+      }
+  }
+  const int q = warp & 3, hf = warp >> 2;
+  const int r = ti * 128 + q * 32 + lane;
+  const int col0 = tj * 32 + hf * 16, ncol = min(16, ns - col0);
+  float4* G = parity ? d.g_alt : d.g;
+  if (r < ns)   // the epilogue's G entries into L2 while the products run
+    for (int c = 0; c < ncol; ++c) asm volatile("prefetch.global.L2 [%0];" ::"l"(G + r + (size_t)ns * (col0 + c)));
+  __syncthreads();
+  const int last = s_last;
+  if (last >= 0) {   // every exit path waits for the last commit (it tracks all earlier products)
+    if (!mbar_wait_bounded(&s_mma[last], 0)) s_fail = 1;
+    um_fence_after();
+  }
+  __syncthreads();
+  const uint32_t tbase = taddr + ((uint32_t)(q * 32) << 16);
+  if (!s_fail) {
+#pragma unroll 1
+    for (int ch = 0; ch < 2; ++ch) {
+      const int c0 = ch * 8;
+      if (ncol <= c0) break;   // warp-uniform
+      float re[3][8], im[3][8];
+#pragma unroll
+      for (int l = 0; l < 3; ++l) {
+        um_ld8_nw(tbase + l * 64 + hf * 16 + c0, re[l]);
+        um_ld8_nw(tbase + l * 64 + 32 + hf * 16 + c0, im[l]);
+      }
+      um_wait_ld();
+      if (r < ns) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          if (c0 + c >= ncol) continue;
+          float4* p = G + r + (size_t)ns * (col0 + c0 + c);
+          const float4 g = *p;
+          const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
+          const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
+          const df nr = df_add(df{g.x, g.z}, vr), ni = df_add(df{g.y, g.w}, vi);
+          *p = make_float4(nr.hi, ni.hi, nr.lo, ni.lo);
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(d.err, PQMC_ERR_TIMEOUT);
+  }
+  um_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(taddr) : "memory");
+}
+
 int exact_setup() {
   PQMC_CUDA(raise_dyn_smem(k_xinv, (int)XI_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xres, (int)XR_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xgemm<0>, XG_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xgemm<1>, XG_SMEM));
+  PQMC_CUDA(raise_dyn_smem(k_xflush2, XF_SMEM_LAUNCH));
   return PQMC_OK;
 }
 
-int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi) {
+int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, int ct, cudaStream_t st, bool prio,
+               int prio_hi) {
   const int n_r = (ns + XS_ROWS - 1) / XS_ROWS, n_c = (ns + XS_COLS - 1) / XS_COLS;
-  PQMC_CUDA(launch_at(k_xslice, dim3(n_r + n_c, C), dim3(XS_THREADS), 0, st, prio, prio_hi, d_x, parity, n_r));
+  PQMC_CUDA(launch_at(k_xslice, dim3(n_r + n_c, C), dim3(XS_THREADS), 0, st, prio, prio_hi, d_x, parity, n_r, ct));
   PQMC_LAUNCHED();
   PQMC_CUDA(launch_at(k_xinv, dim3(1, C), dim3(XC_THREADS), XI_SMEM, st, prio, prio_hi, d_x, dim, parity));
   PQMC_LAUNCHED();
@@ -676,11 +837,16 @@ int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_
   return PQMC_OK;
 }
 
-int exact_products(const XDesc* d_x, int C, int ns, int parity, cudaStream_t st, bool prio, int prio_hi) {
-  const int RT = um_rtiles(ns), CT = um_ctiles(ns);
+int exact_products(const XDesc* d_x, int C, int ns, int parity, int ct, cudaStream_t st, bool prio, int prio_hi) {
+  const int RT = um_rtiles(ns);
   PQMC_CUDA(launch_at(k_xgemm<0>, dim3(RT, C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
   PQMC_LAUNCHED();
-  PQMC_CUDA(launch_at(k_xgemm<1>, dim3(RT * CT, C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
+  if (ct == 32)
+    PQMC_CUDA(launch_at(k_xflush2, dim3(RT * oz_ztiles(ns), C), dim3(256), (size_t)XF_SMEM_LAUNCH, st, prio, prio_hi,
+                        d_x, parity));
+  else
+    PQMC_CUDA(launch_at(k_xgemm<1>, dim3(RT * um_ctiles(ns), C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x,
+                        parity));
   PQMC_LAUNCHED();
   return PQMC_OK;
 }
@@ -702,10 +868,16 @@ __global__ void k_x_from_df(const float4* a, cplx* b, long n) {
 }  // namespace pqmc
 
 extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g) {
+  return pqmc_exact_update_check_tile(ns, k, dim, sites, delta, g, 64);
+}
+
+extern "C" int pqmc_exact_update_check_tile(int ns, int k, int dim, const int* sites, const double* delta, double* g,
+                                            int flush_tile) {
   using namespace pqmc;
   if (!sites || !delta || !g || dim < 1 || dim > 4 || k < dim || k > UM_KP || k % dim || ns < k ||
-      ns > 4096) {
-    set_error("exact_update_check: need 1 <= dim <= 4, dim <= k <= %d, k %% dim == 0, k <= ns <= 4096", UM_KP);
+      ns > 4096 || (flush_tile != 32 && flush_tile != 64)) {
+    set_error("exact_update_check: need 1 <= dim <= 4, dim <= k <= %d, k %% dim == 0, k <= ns <= 4096, "
+              "flush tile 32 or 64", UM_KP);
     return PQMC_ERR_ARG;
   }
   for (int i = 0; i < k; ++i)
@@ -779,8 +951,8 @@ extern "C" int pqmc_exact_update_check(int ns, int k, int dim, const int* sites,
     x.err = d_err;
     x.nflush = d_nf;
     PQMC_CUDA(cudaMemcpy(d_x, &x, sizeof(XDesc), cudaMemcpyHostToDevice));
-    PQMC_TRY(exact_core(d_x, 1, ns, dim, 0, 0, false, 0));
-    PQMC_TRY(exact_products(d_x, 1, ns, 0, 0, false, 0));
+    PQMC_TRY(exact_core(d_x, 1, ns, dim, 0, flush_tile, 0, false, 0));
+    PQMC_TRY(exact_products(d_x, 1, ns, 0, flush_tile, 0, false, 0));
     k_x_from_df<<<256, 256>>>(d_g, d_g64, (long)n2);
     PQMC_LAUNCHED();
     PQMC_CUDA(cudaDeviceSynchronize());

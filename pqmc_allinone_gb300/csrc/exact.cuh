@@ -55,16 +55,22 @@ __host__ __device__ __forceinline__ int oz_slot_b1(int ns, int s) { return 2 * u
 __host__ __device__ __forceinline__ int oz_slot_b2(int ns, int t, int s) {
   return (2 * um_rtiles(ns) + 1 + t) * OZ_S + s;
 }
+// Z's column tiles: 64 columns for k_xgemm<1>, 32 for k_xflush2; slots for
+// the narrower ones, which are more
+__host__ __device__ __forceinline__ int oz_ztiles(int ns) { return (ns + 31) / 32; }
 __host__ __device__ __forceinline__ size_t oz_chain_bytes(int ns) {
-  return (size_t)(2 * um_rtiles(ns) + 1 + um_ctiles(ns)) * OZ_S * UM_IMG;
+  return (size_t)(2 * um_rtiles(ns) + 1 + oz_ztiles(ns)) * OZ_S * UM_IMG;
 }
 
 // The exact update of one round for C chains: exact_core (three launches:
 // the operand slices, W^-1, M) and exact_products (two launches: the
 // tensor-core products).  `prio` marks the launches with priority
 // `prio_hi` (kept as node priorities when the stream is being captured).
-int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, cudaStream_t st, bool prio, int prio_hi);
-int exact_products(const XDesc* d_x, int C, int ns, int parity, cudaStream_t st, bool prio, int prio_hi);
+// ct: the flush tile's width, 64 (k_xgemm<1>, one CTA per SM) or 32
+// (k_xflush2, two CTAs per SM); exact_core cuts Z into tiles of that width
+int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, int ct, cudaStream_t st, bool prio,
+               int prio_hi);
+int exact_products(const XDesc* d_x, int C, int ns, int parity, int ct, cudaStream_t st, bool prio, int prio_hi);
 int exact_setup();   // raises the kernels' dynamic shared-memory limits
 
 }  // namespace pqmc

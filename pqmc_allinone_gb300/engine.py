@@ -399,15 +399,31 @@ class PqmcBatch:
         check(self.lib, self.lib.pqmc_batch_get_wrap_tile(self.h, ctypes.byref(v)), "pqmc_batch_get_wrap_tile")
         return int(v.value)
 
+    def set_flush_tile(self, ct: int):
+        """Flush tile of the exact round update: 64 or 32 columns of G per CTA."""
+        check(self.lib, self.lib.pqmc_batch_set_flush_tile(self.h, ct), "pqmc_batch_set_flush_tile")
+
+    def flush_tile(self) -> int:
+        v = ctypes.c_int(0)
+        check(self.lib, self.lib.pqmc_batch_get_flush_tile(self.h, ctypes.byref(v)), "pqmc_batch_get_flush_tile")
+        return int(v.value)
+
     def autotune_tiles(self, loop: int, first_tc: int, n_slices: int):
-        """Tile-shape autotuner at the current delay depth: every wrap tile
-        timed over n_slices slices from (loop, first_tc); keeps the fastest.
-        Returns (best tile, {tile: ms per slice or None where it does not fit})."""
-        ms = np.zeros(3)
-        best = ctypes.c_int(0)
-        check(self.lib, self.lib.pqmc_batch_autotune_tiles(self.h, loop, first_tc, n_slices, ctypes.byref(best),
+        """Tile-shape autotuner at the current delay depth: every wrap tile,
+        then (exact round update) every flush tile, each timed over n_slices
+        slices from (loop, first_tc); keeps the fastest of each.  Returns
+        ((best wrap tile, best flush tile), {wrap tile: ms}, {flush tile: ms})
+        with None where a shape does not fit or does not apply."""
+        ms = np.zeros(5)
+        best = (ctypes.c_int * 2)()
+        check(self.lib, self.lib.pqmc_batch_autotune_tiles(self.h, loop, first_tc, n_slices, best,
                                                             ms.ctypes.data_as(_f64p)), "pqmc_batch_autotune_tiles")
-        return int(best.value), {k: (float(v) if v >= 0 else None) for k, v in enumerate(ms)}
+        val = [float(v) if v >= 0 else None for v in ms]
+        return (int(best[0]), int(best[1])), dict(zip((0, 1, 2), val[:3])), dict(zip((64, 32), val[3:]))
+
+    def tiles_timed(self, wrap_table: dict, flush_table: dict) -> int:
+        """Blocks of slices an autotune_tiles call ran (one per timed shape)."""
+        return sum(v is not None for v in wrap_table.values()) + sum(v is not None for v in flush_table.values())
 
     def set_measure(self, warmup: int, meas_interval: int = 1, meas_number: int = 0):
         """Equal-time measurements in batched sweeps (chains built with meas=True)."""
@@ -481,10 +497,11 @@ class PqmcBatch:
             pass
 
 
-def exact_update_check(g: np.ndarray, sites, delta) -> np.ndarray:
+def exact_update_check(g: np.ndarray, sites, delta, flush_tile: int = 64) -> np.ndarray:
     """The batch's exact round update applied to a host G (validation):
     returns G + G(:,S) Delta_S W^-1 (E_S - G(S,:)), sites in acceptance
-    order (dim per move), delta (n_moves, dim, dim)."""
+    order (dim per move), delta (n_moves, dim, dim); flush_tile 64
+    (k_xgemm<1>) or 32 (k_xflush2)."""
     lib = load_library()
     ns = g.shape[0]
     d = np.asarray(delta, dtype=np.complex128)
@@ -492,8 +509,9 @@ def exact_update_check(g: np.ndarray, sites, delta) -> np.ndarray:
     s = np.ascontiguousarray(sites, dtype=np.int32)
     gg = np.asfortranarray(g, dtype=np.complex128).copy(order="F")
     dl = np.ascontiguousarray(np.stack([np.asfortranarray(x).ravel(order="F") for x in d]))
-    check(lib, lib.pqmc_exact_update_check(ns, len(s), dim, s.ctypes.data_as(_i32p),
-                                            dl.view(np.float64).ctypes.data_as(_f64p),
-                                            gg.ravel(order="K").view(np.float64).ctypes.data_as(_f64p)),
+    check(lib, lib.pqmc_exact_update_check_tile(ns, len(s), dim, s.ctypes.data_as(_i32p),
+                                                 dl.view(np.float64).ctypes.data_as(_f64p),
+                                                 gg.ravel(order="K").view(np.float64).ctypes.data_as(_f64p),
+                                                 int(flush_tile)),
           "pqmc_exact_update_check")
     return gg

@@ -261,14 +261,44 @@ def test_wrap_tiles_bit_identical_and_autotuned():
             assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
     b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
     b.init()
-    best, table = b.autotune_tiles(1, 1, 5)
+    (best, fbest), table, ftable = b.autotune_tiles(1, 1, 4)
     assert best in (0, 1, 2) and b.wrap_tile() == best
+    assert fbest in (64, 32) and b.flush_tile() == fbest
     assert all(v is not None and v > 0 for v in table.values())
-    assert table[best] == min(table.values())
-    b.sweep_slices(1, 16, 5)
+    assert all(v is not None and v > 0 for v in ftable.values())
+    assert table[best] == min(table.values()) and ftable[fbest] == min(ftable.values())
+    assert b.tiles_timed(table, ftable) == 5
+    b.sweep_slices(1, 21, 0)
     b.sweep(2)
     assert all(0.0 < c.state()["err_g_rel_max"] < 1e-8 for c in b.chains)
     b.close()
+
+
+def test_flush_tiles_agree():
+    """The two flush tiles of the exact round update (128 x 64 tiles, one CTA
+    per SM; 128 x 32, two CTAs per SM) sum the rounded level of the Ozaki
+    products in another order, so their chains agree to that rounding: the
+    same accept/reject sequence here, G within 1e-12, both within the drift
+    bound."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(3):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=160 + i)
+        ms.append((m, f, seed_words(1600 + i)))
+    runs = []
+    for ct in (64, 32):
+        b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+        b.set_flush_tile(ct)
+        assert b.flush_tile() == ct
+        b.init()
+        for loop in (1, 2):
+            b.sweep(loop)
+        runs.append([(c.field(), c.g(), c.state()) for c in b.chains])
+        b.close()
+    for (f0, g0, s0), (f1, g1, s1) in zip(*runs):
+        assert np.array_equal(f0, f1) and s0["positive_accept"] == s1["positive_accept"]
+        assert rel_fro(g1, g0) < 1e-12
+        assert 0.0 < s1["err_g_rel_max"] < MIXED_DRIFT_TOL[2]
 
 
 def test_launch_priorities_bit_identical(monkeypatch):
@@ -341,8 +371,8 @@ def test_uneven_batch_autotune_then_sweeps():
     best, table = b.autotune(1, 1, 10, (16, 32, 64, 96))
     assert table[96] < 0 and best in (16, 32, 64)   # 96 columns exceed the exact round update
     tc = 1 + 10 * sum(1 for v in table.values() if v >= 0)
-    tile, ttable = b.autotune_tiles(1, tc, 10)
-    tc += 10 * sum(1 for v in ttable.values() if v is not None)
+    (tile, ftile), ttable, ftable = b.autotune_tiles(1, tc, 5)
+    tc += 5 * b.tiles_timed(ttable, ftable)
     assert tc <= 80
     b.sweep_slices(1, tc, 80 - tc + 1)
     b.sweep(2)

@@ -55,14 +55,15 @@ def _case(ns, dim, nmoves, scale, seed):
     (130, 2, 13, 0.2),     # ragged row and column tiles (130 = 128 + 2)
     (77, 1, 40, 0.2),      # one site per move, one row tile
 ])
-def test_exact_update_matches_sequential_fp64(ns, dim, nmoves, scale):
+@pytest.mark.parametrize("flush_tile", [64, 32])
+def test_exact_update_matches_sequential_fp64(ns, dim, nmoves, scale, flush_tile):
     from pqmc_allinone_gb300.engine import exact_update_check
     g0, sites, deltas = _case(ns, dim, nmoves, scale, seed=ns + dim + nmoves)
     want = _sequential(g0, sites, deltas)
-    got = exact_update_check(g0, sites.reshape(-1), deltas)
+    got = exact_update_check(g0, sites.reshape(-1), deltas, flush_tile)
     upd = np.linalg.norm(want - g0)
     err = np.linalg.norm(got - want)
-    print(f"ns={ns} dim={dim} moves={nmoves} scale={scale}: |err|/|update| {err / upd:.3e}, "
+    print(f"ns={ns} dim={dim} moves={nmoves} scale={scale} tile={flush_tile}: |err|/|update| {err / upd:.3e}, "
           f"|err|/|G| {err / np.linalg.norm(want):.3e}")
     assert err <= UPDATE_TOL * upd + 1e-14 * np.linalg.norm(want), (err, upd)
     # FP32-accurate arithmetic would leave ~1e-7 of the update: the test

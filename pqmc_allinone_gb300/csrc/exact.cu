@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(XC_THREADS, 1) k_xinv(const XDesc* X, int dim,
 #pragma unroll
         for (int m = 0; m < 4; ++m)
           if (m < dim) a = dfc_mac(a, gs[m], dg_dfc(s_dl[jb * 16 + m + dim * jj]));
-        d.wdf[i * XC_LD + j] = dfc_dg(a);
+        d.wdf[j * XC_LD + i] = dfc_dg(a);   // column-major: k_xres reads W(i, k) for consecutive i
         Wf[i * XC_LD + j] = make_float2(a.re.hi, a.im.hi);
       }
     }
@@ -320,11 +320,11 @@ __global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim,
   if (K == 0) return;
   const int nb = K / dim;
   const int j0 = blockIdx.x * XR_W;   // this CTA's columns j0 .. j0 + XR_W - 1 of M
-  float4* W = reinterpret_cast<float4*>(xr_dyn);                     // [K][XC_LD] double-float W
+  float4* W = reinterpret_cast<float4*>(xr_dyn);                     // [K][XC_LD] double-float W, column-major
   float4* s_dl = W + (size_t)XC_LD * XC_LD;                           // [n_acc][16]
   float4* Rs = s_dl + 16 * UM_KP;                                     // [K][XR_W] residual, then V1, then M
   float2* V = reinterpret_cast<float2*>(Rs + (size_t)UM_KP * XR_W);   // [K][XC_LD] V0
-  if (tid == 0) {   // the first K rows of W and V0 (contiguous) and the Delta records by bulk copies
+  if (tid == 0) {   // the first K columns of W and rows of V0 (contiguous) and the Delta records by bulk copies
     const uint32_t bw = (uint32_t)(sizeof(float4) * XC_LD * K), bv = (uint32_t)(sizeof(float2) * XC_LD * K);
     const uint32_t bd = (uint32_t)(sizeof(float4) * 16 * nb);
     fence_proxy_async_global();
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim,
   if (ri < K) {
     float rh0 = 0.f, rl0 = 0.f, rh1 = 0.f, rl1 = 0.f;
     for (int k = 0; k < K; ++k) {
-      const float4 w = W[ri * XC_LD + k];   // {re_hi, im_hi, re_lo, im_lo}
+      const float4 w = W[k * XC_LD + ri];   // {re_hi, im_hi, re_lo, im_lo}; consecutive ri: no bank conflicts
       const float2 v = j < K ? V[k * XC_LD + j] : make_float2(0.f, 0.f);
       df_mac_f(rh0, rl0, w.x, w.z, v.x);     // re += wr vr
       df_mac_f(rh0, rl0, -w.y, -w.w, v.y);   //       - wi vi
@@ -360,17 +360,20 @@ __global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim,
     Rs[ri * XR_W + cq] = make_float4(rr.hi, -wi.hi, rr.lo, -wi.lo);
   }
   __syncthreads();
-  // V1 = V0 + V0 R on the slab (R is small: its FP32 rounding suffices)
+  // V1 = V0 + V0 R on the slab (R is small: its FP32 rounding suffices).
+  // Threads take (row tid / XR_W, column tid % XR_W) here, so a warp reads 4
+  // rows of V0 (a 4-way bank conflict, not 32) and consecutive R entries.
+  const int ri2 = tid / XR_W, cq2 = tid % XR_W, j2 = j0 + cq2;
   float4 v1 = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (ri < K) {
+  if (ri2 < K) {
     float2 s = make_float2(0.f, 0.f);
-    for (int k = 0; k < K; ++k) s = fcfma(V[ri * XC_LD + k], hi2(Rs[k * XR_W + cq]), s);
-    const float2 v0 = j < K ? V[ri * XC_LD + j] : make_float2(0.f, 0.f);
+    for (int k = 0; k < K; ++k) s = fcfma(V[ri2 * XC_LD + k], hi2(Rs[k * XR_W + cq2]), s);
+    const float2 v0 = j2 < K ? V[ri2 * XC_LD + j2] : make_float2(0.f, 0.f);
     const df a = two_sum(v0.x, s.x), b = two_sum(v0.y, s.y);
     v1 = make_float4(a.hi, b.hi, a.lo, b.lo);
   }
   __syncthreads();
-  if (ri < K) Rs[ri * XR_W + cq] = v1;
+  if (ri2 < K) Rs[ri2 * XR_W + cq2] = v1;
   __syncthreads();
   // M = Delta_S V1 block row by block row
   for (int it = tid; it < nb * XR_W; it += XR_THREADS) {

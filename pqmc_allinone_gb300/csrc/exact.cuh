@@ -39,7 +39,7 @@ struct XDesc {
   const int* kcount;       // panel columns of the round (written by the scan)
   int* acc_site;           // (kmax) accepted sites, dim per move, in acceptance order
   float4* acc_delta;       // (kmax) 16 entries per accepted move: its Delta (double-float)
-  float4* wdf;             // (kmax x kmax) W in double-float, row i at wdf + i*kmax
+  float4* wdf;             // (kmax x kmax) W in double-float, column j at wdf + j*kmax
   float2* v0;              // (kmax x kmax) FP32 inverse of W
   unsigned char* img;      // slice images (oz_chain_bytes)
   DevScalars* sc;

@@ -82,8 +82,11 @@ __device__ __forceinline__ void dot2_mac(d2acc& acc, float xh, float xl, float y
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) k_dfgemm2(const GemmArgs* args, int m, int n, int k, int accumulate) {
   const GemmArgs g = args[blockIdx.z];
-  __shared__ float4 sA[DG_BK][DG_BM];   // (re.hi, re.lo, im.hi, im.lo)
-  __shared__ float4 sB[DG_BK][DG_BN];
+  // (re.hi, re.lo, im.hi, im.lo); one float4 of padding per row, so that the
+  // staging of a conjugate-transposed operand (consecutive threads on
+  // consecutive rows q) does not put a quarter-warp on one bank group
+  __shared__ float4 sA[DG_BK][DG_BM + 1];
+  __shared__ float4 sB[DG_BK][DG_BN + 1];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int row0 = blockIdx.x * DG_BM, col0 = blockIdx.y * DG_BN;
   if (g.shape == 1 && row0 + DG_BM <= col0) return;   // tile strictly above the diagonal

@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--graphs", type=int, default=1, choices=[0, 1],
                    help="replay each slice's family steps from a captured CUDA graph (mixed batches)")
+    p.add_argument("--gemm-engine", type=int, default=1, choices=[0, 1],
+                   help="engine of the recompute's GEMMs (mixed batches): 0 double-float on the FP32 pipe, "
+                        "1 Ozaki-split BF16 on the tensor cores")
     p.add_argument("--profile-block", type=int, default=0, metavar="C",
                    help="profiling run instead of the benchmark: C chains of the workload's model in one "
                         "group (delay depth 64, no graphs, the --flush round update), one warm-up block of "
@@ -324,6 +327,7 @@ def run_profile_block(args) -> None:
     b.set_graphs(False)
     b.set_flush(args.flush)
     b.set_delay(args.delay or 64)
+    b.set_gemm_engine(args.gemm_engine)
     b.init()
     b.sweep_slices(1, 1, m.ngroup)
     torch.cuda.synchronize()
@@ -407,6 +411,7 @@ def run_mixed(args, world, rank, local):
     b = PqmcBatch([m] * C, fields, [seed_words(s) for s in seeds], precision=1)
     b.set_graphs(bool(args.graphs))
     b.set_flush(args.flush)
+    b.set_gemm_engine(args.gemm_engine)
     t0 = time.perf_counter()
     b.init()
     t_init = time.perf_counter() - t0
@@ -453,6 +458,8 @@ def run_mixed(args, world, rank, local):
     launches = kernel_launches() - n0
     binfo = b.info()
     binfo["slice_graphs"] = bool(args.graphs)
+    binfo["recompute_gemm_engine"] = ("Ozaki-split BF16, tensor cores" if b.gemm_engine() == 1
+                                      else "double-float, FP32 pipe")
     t_step = max_over_ranks(world, ev0.elapsed_time(ev1) / 1000.0 / args.steps)
     per_gpu = C * (m.ngroup / m.ntime) / t_step
     value = world * per_gpu
@@ -675,6 +682,7 @@ def run_uneven(args, world, rank, local):
     t_models = time.perf_counter() - t0
     b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
     b.set_graphs(bool(args.graphs))
+    b.set_gemm_engine(args.gemm_engine)
     t0 = time.perf_counter()
     b.init()
     t_init = time.perf_counter() - t0

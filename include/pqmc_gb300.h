@@ -431,6 +431,19 @@ int pqmc_batch_get_wrap_tile(pqmc_batch* batch, int* ci);
  * (~2^-40 of the update), not bit for bit. */
 int pqmc_batch_set_flush_tile(pqmc_batch* batch, int ct);
 int pqmc_batch_get_flush_tile(pqmc_batch* batch, int* ct);
+/* Engine of the stabilised recompute's complex GEMMs (Gram matrices,
+ * X R^-1, L R, R (L R)^-1, the new G; the zgemm calls of
+ * src/mod_evolution.f90 cal_g_and_det_T0 / get_g_scratch_T0 and
+ * src/mod_matrix.f90 qdr): 1 the Ozaki-split BF16 product on the tensor
+ * cores (default; ozgemm.cu: six slices per operand, 21 slice products into
+ * six FP32 level accumulators, levels 0-4 exact, summed in double-float;
+ * ~1e-14 on an orthonormal Gram matrix), 0 the compensated double-float
+ * product on the FP32 pipe (k_dfgemm2; Dot2, whose FP32 low-order sum grows
+ * like K^1.5 u^2: ~1e-12 there).  The environment variable
+ * PQMC_RECOMPUTE_GEMM=0 makes 0 the default.  Chains of the two engines
+ * agree to the products' rounding, not bit for bit.  Mixed batches only. */
+int pqmc_batch_set_gemm_engine(pqmc_batch* batch, int engine);
+int pqmc_batch_get_gemm_engine(pqmc_batch* batch, int* engine);
 /* Autotune the tile shapes at the batch's delay depth: every wrap tile
  * (0, 1, 2), then, with the exact round update, every flush tile (64, 32),
  * each timed over n_slices slices of sweep `loop` from first_tc with plain
@@ -557,6 +570,15 @@ int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const doub
 /* The same with the flush tile chosen: 64 (k_xgemm<1>) or 32 (k_xflush2). */
 int pqmc_exact_update_check_tile(int ns, int k, int dim, const int* sites, const double* delta, double* g,
                                  int flush_tile);
+
+/* ---- validation of the recompute's GEMMs ------------------------------- */
+/* No counterpart in the reference (zgemm there).  C_i = op(A_i) op(B_i) for
+ * i < count, complex FP64 on the HOST, column-major, the count matrices of
+ * each operand consecutive (lda x cols, ldb x cols, ldc x n each); ta, tb
+ * 'N' (as is) or 'C' (conjugate transpose); op(A) m x k, op(B) k x n.
+ * engine as pqmc_batch_set_gemm_engine. */
+int pqmc_recompute_gemm_check(char ta, char tb, int m, int n, int k, int count, const double* a, int lda,
+                              const double* b, int ldb, double* c, int ldc, int engine);
 
 /* ---- introspection --------------------------------------------------- */
 const char* pqmc_version(void);

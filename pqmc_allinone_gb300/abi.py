@@ -249,6 +249,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                                       ctypes.c_int),
         "pqmc_batch_set_flush_tile": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_get_flush_tile": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "pqmc_batch_set_gemm_engine": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_get_gemm_engine": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "pqmc_batch_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "pqmc_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "pqmc_set_field_slices": ([vp, ctypes.c_int, ctypes.c_int, _f64p], ctypes.c_int),
@@ -269,6 +271,9 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "pqmc_exact_update_check": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _f64p, _f64p], ctypes.c_int),
         "pqmc_exact_update_check_tile": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _f64p, _f64p, ctypes.c_int],
                                          ctypes.c_int),
+        "pqmc_recompute_gemm_check": ([ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, _f64p, ctypes.c_int, _f64p, ctypes.c_int, _f64p, ctypes.c_int,
+                                       ctypes.c_int], ctypes.c_int),
         "pqmc_version": ([], ctypes.c_char_p),
         "pqmc_last_error": ([], ctypes.c_char_p),
         "pqmc_kernel_launches": ([], ctypes.c_int64),

@@ -2207,6 +2207,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       std::vector<pqmc_chain*> sub(b->chains.begin() + b->g_first[g],
                                    b->chains.begin() + b->g_first[g] + b->g_count[g]);
       PQMC_TRY(b->rec[g].setup(sub, b->g_stream[g]));
+      b->rec[g].err = b->d_err;
     }
   PQMC_TRY(batch_refresh(b));
   PQMC_CUDA(cudaStreamSynchronize(b->stream));
@@ -2307,6 +2308,30 @@ int pqmc_batch_set_flush_tile(pqmc_batch* b, int ct) {
 int pqmc_batch_get_flush_tile(pqmc_batch* b, int* ct) {
   if (!b || !ct) { set_error("null argument"); return PQMC_ERR_ARG; }
   *ct = b->parts.empty() ? b->xflush_ct : b->parts[0]->xflush_ct;
+  return PQMC_OK;
+}
+
+int pqmc_batch_set_gemm_engine(pqmc_batch* b, int engine) {
+  if (!b || (engine != 0 && engine != 1)) {
+    set_error("batch_set_gemm_engine: 0 (double-float, FP32 pipe) or 1 (Ozaki, tensor cores)");
+    return PQMC_ERR_ARG;
+  }
+  if (b->precision != PQMC_PREC_MIXED) {
+    set_error("batch_set_gemm_engine: mixed batches only (the FP64 batch recomputes with its chains' own path)");
+    return PQMC_ERR_ARG;
+  }
+  if (!b->parts.empty()) {   // the classes hold the recomputes
+    for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_gemm_engine(p, engine));
+    return PQMC_OK;
+  }
+  PQMC_CUDA(cudaStreamSynchronize(b->stream));
+  for (int g = 0; g < b->n_groups; ++g) PQMC_TRY(b->rec[g].set_engine(engine));
+  return PQMC_OK;
+}
+
+int pqmc_batch_get_gemm_engine(pqmc_batch* b, int* engine) {
+  if (!b || !engine) { set_error("null argument"); return PQMC_ERR_ARG; }
+  *engine = b->parts.empty() ? b->rec[0].engine : b->parts[0]->rec[0].engine;
   return PQMC_OK;
 }
 

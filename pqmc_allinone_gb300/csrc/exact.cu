@@ -6,43 +6,16 @@
 #include <vector>
 #include "df32.cuh"
 #include "exact.cuh"
+#include "ozaki.cuh"
 
 namespace pqmc {
 
 // ---------------------------------------------------------------------------
-// Ozaki slices.  A row (column) whose entries have magnitude below 2^e is
-// cut into OZ_S pieces on the grids 2^(e-8), 2^(e-16), ...: piece s is an
-// integer of at most 256 (129 after the first) times 2^(e-8(s+1)), exact in
-// BF16.  Two pieces multiply exactly, and the products of one level (i + j)
-// of pieces share a grid, so up to 128 of them (the real inner dimension of
-// a flush) sum exactly in FP32: |sum| < 2^24 grid units.
-__device__ __forceinline__ int oz_exp(float vmax) {
-  const int b = (__float_as_int(vmax) >> 23) & 0xff;   // vmax >= 0
-  return vmax > 0.f ? max(b - 126, -80) : -80;         // vmax < 2^(b-126)
-}
-__device__ __forceinline__ float oz_pow2(int k) { return __int_as_float((127 + k) << 23); }   // |k| <= 126
-
-// the OZ_S pieces of the double-float value (h, l) for the exponent e
-__device__ __forceinline__ void oz_split(float h, float l, int e, float* q) {
-#pragma unroll
-  for (int s = 0; s < OZ_S; ++s) {
-    const int sh = 8 * (s + 1) - e;
-    const float v = rintf(__fmul_rn(h, oz_pow2(sh)));
-    const float qs = __fmul_rn(v, oz_pow2(-sh));
-    q[s] = qs;
-    h = __fsub_rn(h, qs);   // exact: h and qs lie within half a grid step
-    const df n = two_sum(h, l);
-    h = n.hi;
-    l = n.lo;
-  }
-}
-__device__ __forceinline__ uint32_t oz_pack2(float a, float b) {
-  __nv_bfloat162 t = __floats2bfloat162_rn(a, b);   // a at the lower address
-  return *reinterpret_cast<uint32_t*>(&t);
-}
-__device__ __forceinline__ uint4 oz_pack8(const float* v) {
-  return make_uint4(oz_pack2(v[0], v[1]), oz_pack2(v[2], v[3]), oz_pack2(v[4], v[5]), oz_pack2(v[6], v[7]));
-}
+// Ozaki slices (ozaki.cuh) with OZ_S = 5 pieces: the exponent floor -80 keeps
+// the deepest grid 2^(e-40) a normal FP32 power of two.
+static_assert(-80 >= 8 * OZ_S - 126, "exponent floor");
+__device__ __forceinline__ int oz_exp(float vmax) { return oz_exp_f<-80>(vmax); }
+__device__ __forceinline__ void oz_split(float h, float l, int e, float* q) { oz_split_n<OZ_S>(h, l, e, q); }
 // three accumulator levels (exact, exact, rounded) combined in double-float
 __device__ __forceinline__ df oz_combine(float l0, float l1, float l2) {
   const df s = two_sum(l0, l1);

@@ -10,10 +10,12 @@
 // chains.  CholeskyQR gives the Householder Q up to column phases and
 // |diag R| for D; G and Re ln_cw do not depend on those phases.
 #include <cooperative_groups.h>
+#include <stdlib.h>
 #include <string.h>
 #include <vector>
 #include "chain.cuh"
 #include "df32.cuh"
+#include "ozgemm.cuh"
 #include "recompute_b.cuh"
 
 namespace pqmc {
@@ -934,7 +936,7 @@ __global__ void k_bweight(const WeightArgs* args, int ndcount, long ng, int comp
 // ---------------------------------------------------------------------------
 BatchRecompute::~BatchRecompute() {
   void* ps[] = {d_gemm, d_chol, d_gj, d_prop, d_weight, work_df, tmpX, gram, rinv, pbp, wmat, logdet, piv, perm,
-                status, ekv_df, d_conv, split_a, split_b};
+                status, ekv_df, d_conv, split_a, split_b, d_og, og_img};
   for (void* p : ps)
     if (p) cudaFree(p);
 }
@@ -999,14 +1001,39 @@ int BatchRecompute::setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s
       PQMC_CUDA(raise_dyn_smem(k_chol_cluster, (int)gsm));
     }
   }
-  return PQMC_OK;
+  // the GEMM engine: the tensor cores unless PQMC_RECOMPUTE_GEMM=0
+  const char* ev = getenv("PQMC_RECOMPUTE_GEMM");
+  return set_engine(ev && ev[0] == '0' ? 0 : 1);
 }
 
 static inline cplx* qblk(pqmc_chain* c, int b1) { return c->q_string + (size_t)c->ns * c->nelec * (b1 - 1); }
 static inline cplx* dblk(pqmc_chain* c, int b1) { return c->d_string + (size_t)c->nelec * (b1 - 1); }
 
+int BatchRecompute::set_engine(int e) {
+  if (e != 0 && e != 1) {
+    set_error("recompute GEMM engine: 0 (double-float, FP32 pipe) or 1 (Ozaki, tensor cores)");
+    return PQMC_ERR_ARG;
+  }
+  if (e == 1 && !og_img) {
+    PQMC_TRY(ozgemm_setup());
+    og_stride = ozgemm_img_bytes(ns, ns);   // the largest product: ns x ns
+    PQMC_CUDA(cudaMalloc((void**)&og_img, og_stride * C));
+    PQMC_CUDA(cudaMalloc((void**)&d_og, sizeof(OgDesc) * C * 8));
+  }
+  engine = e;
+  return PQMC_OK;
+}
+
 int BatchRecompute::gemm(char ta, char tb, int m, int n, int k, const std::vector<GemmArgs>& a, int slot,
                          int accumulate) {
+  if (engine == 1 && !accumulate) {
+    std::vector<OgDesc> od(C);
+    for (int i = 0; i < C; ++i)
+      od[i] = OgDesc{a[i].A, a[i].B, reinterpret_cast<float4*>(a[i].C), og_img + og_stride * i, err};
+    OgDesc* dd = d_og + (size_t)slot * C;
+    PQMC_CUDA(cudaMemcpyAsync(dd, od.data(), sizeof(OgDesc) * C, cudaMemcpyHostToDevice, stream));
+    return ozgemm_batched(stream, ta, tb, m, n, k, a[0].lda, a[0].ldb, a[0].ldc, dd, C, a[0].out_df ? 0 : 1);
+  }
   // split A and B of every chain into double-float once (B shares A's split
   // when they are the same matrix, as in the Gram matrix X^H X)
   const long na = (long)a[0].lda * (ta == 'C' ? m : k), nb = (long)a[0].ldb * (tb == 'C' ? k : n);
@@ -1230,3 +1257,62 @@ int BatchRecompute::scratch(int time, bool forward, int parity) {
 }
 
 }  // namespace pqmc
+
+// ---------------------------------------------------------------------------
+extern "C" int pqmc_recompute_gemm_check(char ta, char tb, int m, int n, int k, int count, const double* a, int lda,
+                                         const double* b, int ldb, double* c, int ldc, int engine) {
+  using namespace pqmc;
+  const bool TA = ta == 'C', TB = tb == 'C';
+  if (!a || !b || !c || (ta != 'N' && !TA) || (tb != 'N' && !TB) || m < 1 || n < 1 || k < 1 || count < 1 ||
+      lda < (TA ? k : m) || ldb < (TB ? n : k) || ldc < m || (engine != 0 && engine != 1)) {
+    set_error("recompute_gemm_check: need ta, tb in {N, C}, m, n, k, count >= 1, lda, ldb, ldc at least the rows "
+              "of A, B, C, engine 0 or 1");
+    return PQMC_ERR_ARG;
+  }
+  const size_t na = (size_t)lda * (TA ? m : k), nb = (size_t)ldb * (TB ? k : n), nc = (size_t)ldc * n;
+  cplx *d_a = nullptr, *d_b = nullptr, *d_c = nullptr;
+  GemmArgs* d_ga = nullptr;
+  OgDesc* d_od = nullptr;
+  unsigned char* d_img = nullptr;
+  int* d_err = nullptr;
+  auto run = [&]() -> int {
+    PQMC_CUDA(cudaMalloc((void**)&d_a, sizeof(cplx) * na * count));
+    PQMC_CUDA(cudaMalloc((void**)&d_b, sizeof(cplx) * nb * count));
+    PQMC_CUDA(cudaMalloc((void**)&d_c, sizeof(cplx) * nc * count));
+    PQMC_CUDA(cudaMalloc((void**)&d_err, sizeof(int)));
+    PQMC_CUDA(cudaMemset(d_err, 0, sizeof(int)));
+    PQMC_CUDA(cudaMemcpy(d_a, a, sizeof(cplx) * na * count, cudaMemcpyHostToDevice));
+    PQMC_CUDA(cudaMemcpy(d_b, b, sizeof(cplx) * nb * count, cudaMemcpyHostToDevice));
+    if (engine == 0) {
+      std::vector<GemmArgs> ga(count);
+      for (int i = 0; i < count; ++i) ga[i] = GemmArgs{d_a + na * i, d_b + nb * i, d_c + nc * i, lda, ldb, ldc, 0, 0};
+      PQMC_CUDA(cudaMalloc((void**)&d_ga, sizeof(GemmArgs) * count));
+      PQMC_CUDA(cudaMemcpy(d_ga, ga.data(), sizeof(GemmArgs) * count, cudaMemcpyHostToDevice));
+      PQMC_TRY(dfgemm_batched(0, ta, tb, m, n, k, d_ga, count, 0));
+    } else {
+      PQMC_TRY(ozgemm_setup());
+      const size_t ib = ozgemm_img_bytes(m, n);
+      PQMC_CUDA(cudaMalloc((void**)&d_img, ib * count));
+      std::vector<OgDesc> od(count);
+      for (int i = 0; i < count; ++i)
+        od[i] = OgDesc{d_a + na * i, d_b + nb * i, reinterpret_cast<float4*>(d_c + nc * i), d_img + ib * i, d_err};
+      PQMC_CUDA(cudaMalloc((void**)&d_od, sizeof(OgDesc) * count));
+      PQMC_CUDA(cudaMemcpy(d_od, od.data(), sizeof(OgDesc) * count, cudaMemcpyHostToDevice));
+      PQMC_TRY(ozgemm_batched(0, ta, tb, m, n, k, lda, ldb, ldc, d_od, count, 1));
+    }
+    PQMC_CUDA(cudaDeviceSynchronize());
+    int herr = 0;
+    PQMC_CUDA(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+      set_error("recompute_gemm_check: a wait of the tensor-core product gave up");
+      return PQMC_ERR_TIMEOUT;
+    }
+    PQMC_CUDA(cudaMemcpy(c, d_c, sizeof(cplx) * nc * count, cudaMemcpyDeviceToHost));
+    return PQMC_OK;
+  };
+  const int st = run();
+  void* ps[] = {d_a, d_b, d_c, d_ga, d_od, d_img, d_err};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  return st;
+}

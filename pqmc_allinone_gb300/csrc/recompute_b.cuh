@@ -12,6 +12,7 @@ struct CholArgs;
 struct GJArgs;
 struct PropArgs;
 struct WeightArgs;
+struct OgDesc;
 
 struct BatchRecompute {
   int C = 0, ns = 0, ne = 0;
@@ -39,9 +40,18 @@ struct BatchRecompute {
   size_t ekv_stride = 0;
   int ekv_slices = 0;
   bool gj_cluster = false;   // (L R)^-1 on a cluster of blocks with the matrix in shared memory
+  // the GEMMs' engine: 0 the compensated double-float product on the FP32
+  // pipe (k_dfgemm2), 1 the Ozaki-split product on the tensor cores
+  // (ozgemm.cu; set by setup unless PQMC_RECOMPUTE_GEMM=0)
+  int engine = 0;
+  OgDesc* d_og = nullptr;
+  unsigned char* og_img = nullptr;   // slice images, og_stride bytes per chain
+  size_t og_stride = 0;
+  int* err = nullptr;                // device error word for a wait that gives up (may be null)
 
   ~BatchRecompute();
   int setup(const std::vector<pqmc_chain*>& chains, cudaStream_t s);
+  int set_engine(int e);
   int gemm(char ta, char tb, int m, int n, int k, const std::vector<GemmArgs>& a, int slot, int accumulate);
   int cholqr2(const std::vector<cplx*>& X, const std::vector<cplx*>& D);
   int g_and_det(const std::vector<cplx*>& XL, const std::vector<cplx*>& R, const std::vector<cplx*>& Gcur,

@@ -408,6 +408,16 @@ class PqmcBatch:
         check(self.lib, self.lib.pqmc_batch_get_flush_tile(self.h, ctypes.byref(v)), "pqmc_batch_get_flush_tile")
         return int(v.value)
 
+    def set_gemm_engine(self, engine: int):
+        """Engine of the recompute's GEMMs: 0 double-float on the FP32 pipe,
+        1 Ozaki-split BF16 on the tensor cores."""
+        check(self.lib, self.lib.pqmc_batch_set_gemm_engine(self.h, engine), "pqmc_batch_set_gemm_engine")
+
+    def gemm_engine(self) -> int:
+        v = ctypes.c_int(0)
+        check(self.lib, self.lib.pqmc_batch_get_gemm_engine(self.h, ctypes.byref(v)), "pqmc_batch_get_gemm_engine")
+        return int(v.value)
+
     def autotune_tiles(self, loop: int, first_tc: int, n_slices: int):
         """Tile-shape autotuner at the current delay depth: every wrap tile,
         then (exact round update) every flush tile, each timed over n_slices
@@ -495,6 +505,29 @@ class PqmcBatch:
             self.close()
         except Exception:
             pass
+
+
+def recompute_gemm_check(ta: str, tb: str, a: np.ndarray, b: np.ndarray, engine: int) -> np.ndarray:
+    """The recompute's batched GEMM on host operands (validation):
+    C_i = op(A_i) op(B_i) for a (count, rows, cols) stack of each, op 'N' or
+    'C' (conjugate transpose); engine 0 (double-float, FP32 pipe) or 1
+    (Ozaki, tensor cores).  Returns C (count, m, n)."""
+    lib = load_library()
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    count = a.shape[0]
+    m = a.shape[2] if ta == "C" else a.shape[1]
+    k = a.shape[1] if ta == "C" else a.shape[2]
+    n = b.shape[1] if tb == "C" else b.shape[2]
+    af = np.ascontiguousarray(a.transpose(0, 2, 1))   # column-major per matrix
+    bf = np.ascontiguousarray(b.transpose(0, 2, 1))
+    cf = np.zeros((count, n, m), dtype=np.complex128)
+    check(lib, lib.pqmc_recompute_gemm_check(ta.encode(), tb.encode(), m, n, k, count,
+                                              af.view(np.float64).ctypes.data_as(_f64p), a.shape[1],
+                                              bf.view(np.float64).ctypes.data_as(_f64p), b.shape[1],
+                                              cf.view(np.float64).ctypes.data_as(_f64p), m, int(engine)),
+          "pqmc_recompute_gemm_check")
+    return cf.transpose(0, 2, 1)
 
 
 def exact_update_check(g: np.ndarray, sites, delta, flush_tile: int = 64) -> np.ndarray:

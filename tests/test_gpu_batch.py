@@ -100,6 +100,41 @@ def test_mixed_batch_drift_and_recompute_8x8(mode):
         assert rel_fro(ch.g(), o.g()) < MIXED_RECOMPUTE_TOL
 
 
+@pytest.mark.parametrize("engine", [1, 0])
+@pytest.mark.parametrize("L", [8, 14])
+def test_recompute_gemm_engines_match_oracle(L, engine):
+    """The recompute's GEMMs on either engine (1: Ozaki-split BF16 on the
+    tensor cores, the default; 0: compensated double-float on the FP32 pipe):
+    the fast-path drift and the recompute against the FP64 oracle within the
+    mixed batch's bounds; at 14x14 the products have the benchmark's shapes
+    (Ns 392, nelec 196)."""
+    from oracle.oracle import OracleChain
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(2):
+        m, f = epsocz_small(L=L, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=60 + i)
+        ms.append((m, f, seed_words(600 + i)))
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    assert b.gemm_engine() == 1
+    b.set_gemm_engine(engine)
+    assert b.gemm_engine() == engine
+    b.init()
+    for (m, _, w), ch in zip(ms, b.chains):
+        o = OracleChain(m, field=ch.field(), seed_words=w, meas=False)
+        o.init_expkv()
+        o.init_g(1)
+        assert rel_fro(ch.g(), o.g()) < MIXED_RECOMPUTE_TOL
+    for loop in (1, 2):
+        b.sweep(loop)
+    for (m, _, w), ch in zip(ms, b.chains):
+        s = ch.state()
+        assert 0.0 < s["err_g_rel_max"] < MIXED_DRIFT_TOL[2], s
+        o = OracleChain(m, field=ch.field(), seed_words=w, meas=False)
+        o.init_expkv()
+        o.init_g(1)
+        assert rel_fro(ch.g(), o.g()) < MIXED_RECOMPUTE_TOL
+
+
 @pytest.mark.parametrize("L", [8, 14])
 def test_tcgen05_flush_matches_mma_sync(L):
     """The two rank-K flush engines (tcgen05 with the accumulator in tensor

@@ -59,97 +59,87 @@ __device__ __forceinline__ dfc og_b(const cplx* B, int ld, int k, int c, int tra
   return dfc{df_make(v.x), df_make(trans ? -v.y : v.y)};
 }
 
-// Slices of one chunk (inner indices k0 .. k0 + kn - 1, kn <= 64):
-//   CTAs 0 .. n_a - 1: a thread per row r of op(A) (m rows), A' row r =
-//     [Ar | Ai] at image k and 64 + k;
-//   CTAs n_a ..: a thread per column c of op(B) (n columns), B' re row
-//     c = [Br | -Bi], im row 8 ncg + c = [Bi | Br] of its 32-column tile.
+// Slices of one chunk (inner indices k0 .. k0 + kn - 1, kn <= 64).  A CTA
+// takes 32 rows of op(A) (CTAs 0 .. n_a - 1) or 32 columns of op(B) (the
+// rest): lane = row (column), warp w = inner indices 8w .. 8w + 7, so a
+// warp's image stores are 512 contiguous bytes.  The row's (column's)
+// exponent comes from the largest |hi| over its kn entries (a maximum over
+// the eight warps in shared memory).
+//   A' row r = [Ar | Ai] at image k and 64 + k;
+//   B' re row c = [Br | -Bi], im row 8 ncg + c = [Bi | Br] of its
+//   32-column tile.
+// Entries past kn (to the chunk's multiple of 16) are written as zeros.
 // Images: the A images of row tile t at (t OG_S + slice) UM_IMG, then the
 // B images of column tile t at (t OG_S + slice) OG_BIMG.
-// Entries past kn (to the chunk's multiple of 16) are written as zeros.
+constexpr int OG_SL_ROWS = 32;                    // rows (columns) per slicing CTA
+static_assert(OG_THREADS / 32 * 8 == UM_KP, "a warp per k group of the chunk");
 __global__ void __launch_bounds__(OG_THREADS) k_og_slice(const OgDesc* D, int m, int n, int k0, int kn, int lda,
                                                         int ldb, int ta, int tb, int n_a) {
-  const OgDesc d = D[blockIdx.y];
+  __shared__ float s_mx[OG_THREADS / 32][OG_SL_ROWS];
+  __shared__ OgDesc sd;
+  const int lane = threadIdx.x & 31, kg = threadIdx.x >> 5;
+  if (threadIdx.x == 0) sd = D[blockIdx.y];
+  __syncthreads();
+  const OgDesc& d = sd;
+  const bool is_a = (int)blockIdx.x < n_a;
+  const int idx = (is_a ? (int)blockIdx.x : (int)blockIdx.x - n_a) * OG_SL_ROWS + lane;
+  const int lim = is_a ? m : n;
   const int kn16 = (kn + 15) & ~15;
-  const int RT = um_rtiles(m);
-  if ((int)blockIdx.x < n_a) {
-    const int r = blockIdx.x * OG_THREADS + threadIdx.x;
-    if (r >= m) return;
-    float mx = 0.f;
-    for (int k = 0; k < kn; ++k) {
-      const dfc v = og_a(d.A, lda, r, k0 + k, ta);
-      mx = fmaxf(mx, fmaxf(fabsf(v.re.hi), fabsf(v.im.hi)));
+  dfc v[8];
+  float mx = 0.f;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int k = kg * 8 + u;
+    v[u] = dfc_zero();
+    if (idx < lim && k < kn) v[u] = is_a ? og_a(d.A, lda, idx, k0 + k, ta) : og_b(d.B, ldb, k0 + k, idx, tb);
+    mx = fmaxf(mx, fmaxf(fabsf(v[u].re.hi), fabsf(v[u].im.hi)));
+  }
+  s_mx[kg][lane] = mx;
+  __syncthreads();
+  if (idx >= lim || kg * 8 >= kn16) return;   // no barrier follows
+  float rm = 0.f;
+#pragma unroll
+  for (int w = 0; w < OG_THREADS / 32; ++w) rm = fmaxf(rm, s_mx[w][lane]);
+  const int e = oz_exp_f<OG_FLOOR>(rm);
+  uint32_t wr[OG_S][4], wi[OG_S][4];
+#pragma unroll
+  for (int h = 0; h < 4; ++h) {
+    float r0[OG_S], r1[OG_S], i0[OG_S], i1[OG_S];
+    oz_split_n<OG_S>(v[2 * h].re.hi, v[2 * h].re.lo, e, r0);
+    oz_split_n<OG_S>(v[2 * h + 1].re.hi, v[2 * h + 1].re.lo, e, r1);
+    oz_split_n<OG_S>(v[2 * h].im.hi, v[2 * h].im.lo, e, i0);
+    oz_split_n<OG_S>(v[2 * h + 1].im.hi, v[2 * h + 1].im.lo, e, i1);
+#pragma unroll
+    for (int sl = 0; sl < OG_S; ++sl) {
+      wr[sl][h] = oz_pack2(r0[sl], r1[sl]);
+      wi[sl][h] = oz_pack2(i0[sl], i1[sl]);
     }
-    const int e = oz_exp_f<OG_FLOOR>(mx);
-    const int t = r / 128, row = r % 128, nrg = um_rg(m, t);
-    for (int kg = 0; kg < kn16 / 8; ++kg) {
-      uint32_t wr[OG_S][4], wi[OG_S][4];
+  }
+  if (is_a) {
+    const int t = idx / 128, row = idx % 128, nrg = um_rg(m, t);
 #pragma unroll
-      for (int h = 0; h < 4; ++h) {
-        float r0[OG_S], r1[OG_S], i0[OG_S], i1[OG_S];
-        const int ka = kg * 8 + 2 * h, kb = ka + 1;
-        const dfc va = ka < kn ? og_a(d.A, lda, r, k0 + ka, ta) : dfc_zero();
-        const dfc vb = kb < kn ? og_a(d.A, lda, r, k0 + kb, ta) : dfc_zero();
-        oz_split_n<OG_S>(va.re.hi, va.re.lo, e, r0);
-        oz_split_n<OG_S>(vb.re.hi, vb.re.lo, e, r1);
-        oz_split_n<OG_S>(va.im.hi, va.im.lo, e, i0);
-        oz_split_n<OG_S>(vb.im.hi, vb.im.lo, e, i1);
-#pragma unroll
-        for (int sl = 0; sl < OG_S; ++sl) {
-          wr[sl][h] = oz_pack2(r0[sl], r1[sl]);
-          wi[sl][h] = oz_pack2(i0[sl], i1[sl]);
-        }
-      }
-#pragma unroll
-      for (int sl = 0; sl < OG_S; ++sl) {
-        unsigned char* im = d.img + (size_t)(t * OG_S + sl) * UM_IMG;
-        *reinterpret_cast<uint4*>(im + um_off(row, kg * 8, nrg)) = make_uint4(wr[sl][0], wr[sl][1], wr[sl][2], wr[sl][3]);
-        *reinterpret_cast<uint4*>(im + um_off(row, UM_KP + kg * 8, nrg)) =
-            make_uint4(wi[sl][0], wi[sl][1], wi[sl][2], wi[sl][3]);
-      }
+    for (int sl = 0; sl < OG_S; ++sl) {
+      unsigned char* im = d.img + (size_t)(t * OG_S + sl) * UM_IMG;
+      *reinterpret_cast<uint4*>(im + um_off(row, kg * 8, nrg)) = make_uint4(wr[sl][0], wr[sl][1], wr[sl][2], wr[sl][3]);
+      *reinterpret_cast<uint4*>(im + um_off(row, UM_KP + kg * 8, nrg)) =
+          make_uint4(wi[sl][0], wi[sl][1], wi[sl][2], wi[sl][3]);
     }
     return;
   }
-  const int c = ((int)blockIdx.x - n_a) * OG_THREADS + threadIdx.x;
-  if (c >= n) return;
-  float mx = 0.f;
-  for (int k = 0; k < kn; ++k) {
-    const dfc v = og_b(d.B, ldb, k0 + k, c, tb);
-    mx = fmaxf(mx, fmaxf(fabsf(v.re.hi), fabsf(v.im.hi)));
-  }
-  const int e = oz_exp_f<OG_FLOOR>(mx);
-  const int tj = c / OG_BN, cc = c % OG_BN, ncg = og_cg(n, tj), nrg = 2 * ncg;
+  const int RT = um_rtiles(m);
+  const int tj = idx / OG_BN, cc = idx % OG_BN, ncg = og_cg(n, tj), nrg = 2 * ncg;
   unsigned char* bimg = d.img + (size_t)RT * OG_S * UM_IMG;
-  for (int kg = 0; kg < kn16 / 8; ++kg) {
-    uint32_t wr[OG_S][4], wi[OG_S][4], wn[OG_S][4];
+  constexpr uint32_t NEG2 = 0x80008000u;   // the sign bits of two BF16: -x exactly
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
-      float r0[OG_S], r1[OG_S], i0[OG_S], i1[OG_S];
-      const int ka = kg * 8 + 2 * h, kb = ka + 1;
-      const dfc va = ka < kn ? og_b(d.B, ldb, k0 + ka, c, tb) : dfc_zero();
-      const dfc vb = kb < kn ? og_b(d.B, ldb, k0 + kb, c, tb) : dfc_zero();
-      oz_split_n<OG_S>(va.re.hi, va.re.lo, e, r0);
-      oz_split_n<OG_S>(vb.re.hi, vb.re.lo, e, r1);
-      oz_split_n<OG_S>(va.im.hi, va.im.lo, e, i0);
-      oz_split_n<OG_S>(vb.im.hi, vb.im.lo, e, i1);
-#pragma unroll
-      for (int sl = 0; sl < OG_S; ++sl) {
-        wr[sl][h] = oz_pack2(r0[sl], r1[sl]);
-        wi[sl][h] = oz_pack2(i0[sl], i1[sl]);
-        wn[sl][h] = oz_pack2(-i0[sl], -i1[sl]);
-      }
-    }
-#pragma unroll
-    for (int sl = 0; sl < OG_S; ++sl) {
-      unsigned char* im = bimg + (size_t)(tj * OG_S + sl) * OG_BIMG;
-      const uint4 r4 = make_uint4(wr[sl][0], wr[sl][1], wr[sl][2], wr[sl][3]);
-      const uint4 i4 = make_uint4(wi[sl][0], wi[sl][1], wi[sl][2], wi[sl][3]);
-      *reinterpret_cast<uint4*>(im + um_off(cc, kg * 8, nrg)) = r4;
-      *reinterpret_cast<uint4*>(im + um_off(cc, UM_KP + kg * 8, nrg)) =
-          make_uint4(wn[sl][0], wn[sl][1], wn[sl][2], wn[sl][3]);
-      *reinterpret_cast<uint4*>(im + um_off(8 * ncg + cc, kg * 8, nrg)) = i4;
-      *reinterpret_cast<uint4*>(im + um_off(8 * ncg + cc, UM_KP + kg * 8, nrg)) = r4;
-    }
+  for (int sl = 0; sl < OG_S; ++sl) {
+    unsigned char* im = bimg + (size_t)(tj * OG_S + sl) * OG_BIMG;
+    const uint4 r4 = make_uint4(wr[sl][0], wr[sl][1], wr[sl][2], wr[sl][3]);
+    const uint4 i4 = make_uint4(wi[sl][0], wi[sl][1], wi[sl][2], wi[sl][3]);
+    *reinterpret_cast<uint4*>(im + um_off(cc, kg * 8, nrg)) = r4;
+    *reinterpret_cast<uint4*>(im + um_off(cc, UM_KP + kg * 8, nrg)) =
+        make_uint4(i4.x ^ NEG2, i4.y ^ NEG2, i4.z ^ NEG2, i4.w ^ NEG2);
+    *reinterpret_cast<uint4*>(im + um_off(8 * ncg + cc, kg * 8, nrg)) = i4;
+    *reinterpret_cast<uint4*>(im + um_off(8 * ncg + cc, UM_KP + kg * 8, nrg)) = r4;
   }
 }
 
@@ -310,7 +300,7 @@ int ozgemm_batched(cudaStream_t s, char ta, char tb, int m, int n, int k, int ld
     set_error("ozgemm: empty product (m %d, n %d, k %d, count %d)", m, n, k, count);
     return PQMC_ERR_ARG;
   }
-  const int n_a = (m + OG_THREADS - 1) / OG_THREADS, n_b = (n + OG_THREADS - 1) / OG_THREADS;
+  const int n_a = (m + OG_SL_ROWS - 1) / OG_SL_ROWS, n_b = (n + OG_SL_ROWS - 1) / OG_SL_ROWS;
   const int tiles = um_rtiles(m) * og_ctiles(n);
   for (int k0 = 0; k0 < k; k0 += UM_KP) {
     const int kn = std::min(UM_KP, k - k0);

@@ -397,6 +397,17 @@ def run_plain(m, steps: int, rank: int) -> dict:
             "steps": steps, "accept_ratio": acc / max(1, prop), "err_g_rel_max": s1["err_g_rel_max"]}
 
 
+def mixed_dtype(args) -> str:
+    """The arithmetic of the mixed batch, as the dtype string of its lines."""
+    rec = ("recompute GEMMs bf16 Ozaki slices x6 with exact level sums, summed in double-float; "
+           "Cholesky, triangular inverse and Gauss-Jordan in double-float"
+           if args.gemm_engine == 1 else "double-float recompute (compensated FP32-pipe GEMMs)")
+    if args.flush == 2:
+        return ("double-float (48-bit) G and wraps; fp32 scan ratios; round update from G: fp32 inverse + "
+                "double-float Newton step, bf16 Ozaki slices x5 with exact level sums; " + rec)
+    return "bf16x3 tensor products + fp32 (fast path) on a double-float G; " + rec
+
+
 def run_mixed(args, world, rank, local):
     import torch
     from pqmc_allinone_gb300 import model as M
@@ -569,10 +580,7 @@ def run_mixed(args, world, rank, local):
            "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None,
-           "dtype": ("double-float (48-bit) G, wraps and recompute; fp32 scan ratios; round update from G: "
-                     "fp32 inverse + double-float Newton step, bf16 Ozaki slices x5 with exact level sums"
-                     if args.flush == 2 else
-                     "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute"),
+           "dtype": mixed_dtype(args),
            "data": "synthetic (x ~ N(0,0.5^2), seeds 3000+i)",
            "config": config_of(args.workload, m, world, C, {"autotune": tune, **binfo}),
            "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "clocks": clocks,
@@ -809,10 +817,7 @@ def run_uneven(args, world, rank, local):
            "value": world * C / t_step, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None,
-           "dtype": ("double-float (48-bit) G, wraps and recompute; fp32 scan ratios; round update from G: "
-                     "fp32 inverse + double-float Newton step, bf16 Ozaki slices x5 with exact level sums"
-                     if args.flush == 2 else
-                     "bf16x3 tensor products + fp32 (fast path) on a double-float G; double-float recompute"),
+           "dtype": mixed_dtype(args),
            "data": "synthetic (per chain i: seed 1000+i draws L, Lt, lambda~U(0.5,1); x ~ N(0,0.5^2))",
            "config": {"workload": f"{C} chains of uneven size, mixed precision, one batch per GPU",
                       "chains_by_L": {L: Ls.count(L) for L in (8, 10, 12)},

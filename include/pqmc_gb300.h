@@ -538,17 +538,16 @@ int pqmc_batch_graph_count(pqmc_batch* batch, int* n);
  * are Ns x nelec complex, column-major; g_out is Ns x Ns; logdet_out holds 2
  * doubles.  `stream` is a cudaStream_t (NULL: legacy default stream); the
  * call copies the pivot flag of its LU to the host and synchronises the
- * stream before it returns.  On PQMC_ERR_SINGULAR (an exact zero pivot)
- * g_out and logdet_out have been overwritten and hold no meaningful values.
- * Work space: one file-scope device array of about 3.2 MB, reserved when the
- * library loads and held by every GPU that loads it until the process exits.
- * Sizes above PQMC_NOALLOC_MAX_NS / PQMC_NOALLOC_MAX_NELEC return
- * PQMC_ERR_ARG.  Every call shares that array, which keeps the last call's
- * contents: calls that overlap on the GPU race.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that
- * device current and keeps it for the life of the process; make that first
- * call before any stream capture begins, and do not call the entry point
- * after cudaDeviceReset on that device (the kept address is then stale). */
+ * stream before it returns, so it cannot be recorded into a CUDA graph: on a
+ * stream that is being captured it returns PQMC_ERR_ARG without touching
+ * the GPU (the capture stays valid).  On PQMC_ERR_SINGULAR (an exact zero
+ * pivot) g_out and logdet_out have been overwritten and hold no meaningful
+ * values.  Work space: one file-scope device array of about 3.2 MB, reserved
+ * when the library loads and held by every GPU that loads it until the
+ * process exits; its device address is looked up on every call with the
+ * caller's device current.  Sizes above PQMC_NOALLOC_MAX_NS /
+ * PQMC_NOALLOC_MAX_NELEC return PQMC_ERR_ARG.  Every call shares that array,
+ * which keeps the last call's contents: calls that overlap on the GPU race. */
 #define PQMC_NOALLOC_MAX_NS 512
 #define PQMC_NOALLOC_MAX_NELEC 256
 int pqmc_cal_g_and_det_noalloc(const double* x_left, const double* rmat, int ns, int nelec, double* g_out,

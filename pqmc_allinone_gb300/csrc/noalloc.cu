@@ -16,8 +16,9 @@
 // contents; this routine writes every word it reads before reading it.  The
 // call ends by copying the LU pivot flag to the host and synchronising the
 // stream; on PQMC_ERR_SINGULAR the outputs have been overwritten with
-// meaningless values.
-#include <mutex>
+// meaningless values.  Because of that read-back the call cannot be
+// recorded into a CUDA graph: on a capturing stream it returns PQMC_ERR_ARG
+// before it touches the GPU, and the capture stays valid.
 #include "chain.cuh"
 #include "linalg.cuh"
 
@@ -33,35 +34,17 @@ constexpr size_t kScratchBytes = kCplxWords * sizeof(double2) + kIntWords * size
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-std::mutex g_mu;
-void* g_addr[64] = {nullptr};
-
 // The host-side name g_noalloc_scratch is only a stand-in for the device
-// array; its device address is looked up on the first call on each device,
-// with that device current, and kept for the life of the process (a
-// cudaDeviceReset of that device leaves the kept address stale).
+// array; its device address is looked up on every call, with the caller's
+// device current (a cheap query, and never stale after a cudaDeviceReset).
 int scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    pqmc::set_error("cal_g_and_det_noalloc: cudaGetDevice -> %s", cudaGetErrorString(e));
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    pqmc::set_error("cal_g_and_det_noalloc: cudaGetSymbolAddress -> %s", cudaGetErrorString(e));
     return PQMC_ERR_CUDA;
   }
-  if (dev < 0 || dev >= 64) {
-    pqmc::set_error("cal_g_and_det_noalloc: device index %d unsupported", dev);
-    return PQMC_ERR_CUDA;
-  }
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      pqmc::set_error("cal_g_and_det_noalloc: cudaGetSymbolAddress -> %s", cudaGetErrorString(e));
-      return PQMC_ERR_CUDA;
-    }
-    g_addr[dev] = p;
-  }
-  *out = g_addr[dev];
+  *out = p;
   return PQMC_OK;
 }
 
@@ -78,9 +61,16 @@ extern "C" int pqmc_cal_g_and_det_noalloc(const double* x_left, const double* rm
                     nelec, kMaxNs, kMaxNe);
     return PQMC_ERR_ARG;
   }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  PQMC_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone) {
+    pqmc::set_error("cal_g_and_det_noalloc: the stream is being captured; the call reads its LU pivot flag back "
+                    "and synchronises the stream, which a capture does not allow");
+    return PQMC_ERR_ARG;
+  }
   void* base = nullptr;
   PQMC_TRY(scratch_address(&base));
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   cplx* pbp = reinterpret_cast<cplx*>(base);
   cplx* lmat = pbp + (size_t)kMaxNe * kMaxNe;
   cplx* lcol = lmat + (size_t)kMaxNe * kMaxNs;

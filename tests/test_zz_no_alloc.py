@@ -76,3 +76,33 @@ def test_noalloc_rejects_oversize():
     assert fn(p, p, 513, 8, p, p, None) == 1
     assert fn(p, p, 600, 300, p, p, None) == 1
     assert b"ns=" in lib.pqmc_last_error()
+
+
+def test_noalloc_refuses_stream_capture():
+    """The call reads its pivot flag back and synchronises, which a CUDA-graph
+    capture does not allow: on a capturing stream it returns PQMC_ERR_ARG
+    before touching the GPU, and the capture (here of one other kernel)
+    stays valid and replays."""
+    torch = pytest.importorskip("torch")
+    from pqmc_allinone_gb300.abi import load_library
+    lib = load_library()
+    fn = lib.pqmc_cal_g_and_det_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    buf = torch.zeros(64, dtype=torch.float64, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.float64, device="cuda")
+    p = buf.data_ptr()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    cnt.add_(0.0)   # the add kernel loaded before the capture
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        st = fn(p, p, 8, 4, p, p, ctypes.c_void_p(s.cuda_stream))
+        cnt.add_(1.0)
+    assert st == 1
+    assert b"captured" in lib.pqmc_last_error()
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(cnt[0]) == 2.0

@@ -120,7 +120,7 @@ class ClockSampler:
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_power_cap,utilization.gpu,utilization.memory")
 
     def __init__(self, index: int):
         self.index = index
@@ -149,7 +149,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, pw, reasons = [], [], [], set()
+        sm, smax, pw, reasons, ug, um = [], [], [], set(), [], []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
@@ -164,9 +164,16 @@ class ClockSampler:
             for nm, v in zip(names, parts[4:8]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
+            try:   # percent of the sample period with a kernel running / with device memory read or written
+                ug.append(float(parts[8]))
+                um.append(float(parts[9]))
+            except (IndexError, ValueError):
+                pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "power_w_median": float(np.median(pw)) if pw else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "gpu_util_pct_median": float(np.median(ug)) if ug else None,
+                "mem_util_pct_median": float(np.median(um)) if um else None}
 
 
 # ---------------------------------------------------------------------------
@@ -439,14 +446,16 @@ def run_mixed(args, world, rank, local):
         depth, table = b.autotune(cur.loop, cur.tc, m.ngroup, cands)
         for _ in cands:
             cur.next()
-        (tile, ftile), ttable, ftable = b.autotune_tiles(cur.loop, cur.tc, m.ngroup)
-        for _ in range(b.tiles_timed(ttable, ftable)):   # the blocks the timed tiles ran
+        (tile, ftile, qc), ttable, ftable, qtable = b.autotune_tiles(cur.loop, cur.tc, m.ngroup)
+        for _ in range(b.tiles_timed(ttable, ftable, qtable)):   # the blocks the timed tiles ran
             cur.next()
         tune = {"candidates_ms_per_slice": table, "chosen": depth,
                 "wrap_tile_ms_per_slice": {b.WRAP_TILES[k]: v for k, v in ttable.items()},
                 "wrap_tile_chosen": b.WRAP_TILES[tile],
                 "flush_tile_ms_per_slice": {f"{k} columns per CTA": v for k, v in ftable.items()},
-                "flush_tile_chosen": f"{ftile} columns per CTA"}
+                "flush_tile_chosen": f"{ftile} columns per CTA",
+                "scan_chunk_ms_per_slice": [[f"{k} panel columns", v] for k, v in qtable],
+                "scan_chunk_chosen": f"{qc} panel columns"}
     for _ in range(args.warmup):
         b.sweep_slices(*cur.next(), m.ngroup)
     torch.cuda.synchronize()
@@ -703,8 +712,8 @@ def run_uneven(args, world, rank, local):
         cands = (16, 32, 48, 64) if args.flush in (1, 2) else (32, 64, 96)
     best, table = b.autotune(1, 1, 10, cands)
     tc = 1 + 10 * sum(1 for v in table.values() if v >= 0)
-    (tile, ftile), ttable, ftable = b.autotune_tiles(1, tc, 10)
-    tc += 10 * b.tiles_timed(ttable, ftable)
+    (tile, ftile, qc), ttable, ftable, qtable = b.autotune_tiles(1, tc, 10)
+    tc += 10 * b.tiles_timed(ttable, ftable, qtable)
     b.sweep_slices(1, tc, max(m.ntime for m, _, _ in ms))
     loop = 2
     for _ in range(args.warmup):
@@ -829,7 +838,10 @@ def run_uneven(args, world, rank, local):
                                    "class0_wrap_tile": b.WRAP_TILES[tile],
                                    "flush_tile_ms_per_slice_summed_over_classes":
                                        {f"{k} columns per CTA": v for k, v in ftable.items()},
-                                   "class0_flush_tile": f"{ftile} columns per CTA"},
+                                   "class0_flush_tile": f"{ftile} columns per CTA",
+                                   "scan_chunk_ms_per_slice_summed_over_classes":
+                                       [[f"{k} panel columns", v] for k, v in qtable],
+                                   "class0_scan_chunk": f"{qc} panel columns"},
                       "step": "one sweep of every chain (its own Lt slices, one recompute per 10 slices)",
                       "l2": "no flush: the batch's G, expKV and Q strings (tens of GB) far exceed the 129 MB L2",
                       "parallelism": f"replicas x{world}"},

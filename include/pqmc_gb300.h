@@ -444,14 +444,28 @@ int pqmc_batch_get_flush_tile(pqmc_batch* batch, int* ct);
  * agree to the products' rounding, not bit for bit.  Mixed batches only. */
 int pqmc_batch_set_gemm_engine(pqmc_batch* batch, int engine);
 int pqmc_batch_get_gemm_engine(pqmc_batch* batch, int* engine);
+/* Panel columns per streamed chunk of the scan (k_bscan's TMA stream of the
+ * delayed panels through three shared-memory stages): 1 .. qc_max, the
+ * largest chunk that fits (at most 8; the default).  The chunking does not
+ * change the arithmetic, so the chains are bit-identical whichever runs.
+ * qc_max may be NULL.  Uneven batches: set for every class, get the first
+ * class's. */
+int pqmc_batch_set_scan_chunk(pqmc_batch* batch, int qc);
+int pqmc_batch_get_scan_chunk(pqmc_batch* batch, int* qc, int* qc_max);
 /* Autotune the tile shapes at the batch's delay depth: every wrap tile
  * (0, 1, 2), then, with the exact round update, every flush tile (64, 32),
- * each timed over n_slices slices of sweep `loop` from first_tc with plain
- * launches (CUDA events on the batch stream; the chains advance meanwhile);
- * the fastest of each is kept.  best (2 entries) receives the wrap tile and
- * the flush tile; ms_out (5 entries: wrap 0, 1, 2, flush 64, 32; may be
- * NULL) the ms per slice of each, -1 where a shape does not fit or does not
- * apply.  Uneven batches tune each class; best is the first class's. */
+ * then the scan chunks qc_max, (3 qc_max + 3) / 4 and (qc_max + 1) / 2,
+ * each timed over n_slices slices
+ * of sweep `loop` from first_tc with plain launches (CUDA events on the
+ * batch stream; the chains advance meanwhile); the fastest of each is kept.
+ * Every wrap and scan-chunk slot runs its n_slices (a wrap tile that does
+ * not fit runs them at the best so far), and the two flush slots run with
+ * the exact round update only: 8 or 6 blocks of n_slices in all.
+ * best (3 entries) receives the wrap tile, the flush tile and the scan
+ * chunk; ms_out (8 entries: wrap 0, 1, 2, flush 64, 32, the three scan
+ * chunks in that order; may be NULL) the ms per slice of each, -1 where a
+ * shape does not fit or does not apply.  Uneven batches tune each class; best is the first
+ * class's. */
 int pqmc_batch_autotune_tiles(pqmc_batch* batch, int loop, int first_tc, int n_slices,
                               int* best, double* ms_out);
 /* slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain */

@@ -249,6 +249,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                                       ctypes.c_int),
         "pqmc_batch_set_flush_tile": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_get_flush_tile": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "pqmc_batch_set_scan_chunk": ([vp, ctypes.c_int], ctypes.c_int),
+        "pqmc_batch_get_scan_chunk": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "pqmc_batch_set_gemm_engine": ([vp, ctypes.c_int], ctypes.c_int),
         "pqmc_batch_get_gemm_engine": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "pqmc_batch_sweep_slices": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),

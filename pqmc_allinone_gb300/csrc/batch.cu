@@ -1362,6 +1362,7 @@ struct pqmc_batch {
   int parity = 0;
   int kd = 64;            // delay depth (panel columns per flush)
   int qc = 8;             // panel columns per streamed chunk of the scan
+  int qc_max = 8;         // the largest chunk whose staging fits in shared memory
   // 2: exact round update (exact.cuh; delay depth <= 64), 1: tcgen05 flush of
   // the scan's FP32 panels (delay depth <= 64), 0: mma.sync flush of them
   int flush_mode = 2;
@@ -2020,6 +2021,7 @@ int pqmc_batch_create(const pqmc_model* const* models, int n_chains, int precisi
       return PQMC_ERR_ARG;
     }
     b->qc = qc;
+    b->qc_max = qc;
     // tensor maps over every chain's two G buffers (double-float: 4 FP32 per element)
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -2335,26 +2337,58 @@ int pqmc_batch_get_gemm_engine(pqmc_batch* b, int* engine) {
   return PQMC_OK;
 }
 
+int pqmc_batch_set_scan_chunk(pqmc_batch* b, int qc) {
+  if (!b || qc < 1) {
+    set_error("batch_set_scan_chunk: a chunk of at least one panel column");
+    return PQMC_ERR_ARG;
+  }
+  if (!b->parts.empty()) {
+    for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_scan_chunk(p, qc));
+    return PQMC_OK;
+  }
+  if (qc > b->qc_max) {
+    set_error("batch_set_scan_chunk: %d panel columns per chunk do not fit in shared memory (at most %d)", qc,
+              b->qc_max);
+    return PQMC_ERR_ARG;
+  }
+  if (b->qc != qc) {   // the slice graphs hold the old launches
+    PQMC_CUDA(cudaStreamSynchronize(b->stream));
+    drop_graphs(b);
+  }
+  b->qc = qc;
+  return PQMC_OK;
+}
+
+int pqmc_batch_get_scan_chunk(pqmc_batch* b, int* qc, int* qc_max) {
+  if (!b || !qc) { set_error("null argument"); return PQMC_ERR_ARG; }
+  const pqmc_batch* p = b->parts.empty() ? b : b->parts[0];
+  *qc = p->qc;
+  if (qc_max) *qc_max = p->qc_max;
+  return PQMC_OK;
+}
+
 // candidates of pqmc_batch_autotune_tiles, in ms_out order
 static const int TILE_WRAP[3] = {0, 1, 2};
 static const int TILE_FLUSH[2] = {64, 32};
+// the scan chunks tried: the largest that fits, about three quarters and half of it
+static inline int tile_qc(int qc_max, int i) { return i == 0 ? qc_max : i == 1 ? (3 * qc_max + 3) / 4 : (qc_max + 1) / 2; }
+constexpr int TILE_N = 8;   // entries of ms_out
 
 int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slices, int* best, double* ms_out) {
   if (!b || n_slices < 1 || !best) { set_error("batch_autotune_tiles: bad arguments"); return PQMC_ERR_ARG; }
   if (b->precision != PQMC_PREC_MIXED) { set_error("batch_autotune_tiles: mixed batches only"); return PQMC_ERR_ARG; }
   if (!b->parts.empty()) {   // every class tunes its own tiles; ms_out sums the classes
-    double part_ms[5];
+    double part_ms[TILE_N];
     if (ms_out)
-      for (int i = 0; i < 5; ++i) ms_out[i] = 0.0;
+      for (int i = 0; i < TILE_N; ++i) ms_out[i] = 0.0;
     for (size_t k = 0; k < b->parts.size(); ++k) {
-      int bk[2] = {0, 0};
+      int bk[3] = {0, 0, 0};
       PQMC_TRY(pqmc_batch_autotune_tiles(b->parts[k], loop, first_tc, n_slices, bk, part_ms));
-      if (k == 0) {
-        best[0] = bk[0];
-        best[1] = bk[1];
-      }
+      if (k == 0)
+        for (int i = 0; i < 3; ++i) best[i] = bk[i];
       if (ms_out)
-        for (int i = 0; i < 5; ++i) ms_out[i] = (ms_out[i] < 0.0 || part_ms[i] < 0.0) ? -1.0 : ms_out[i] + part_ms[i];
+        for (int i = 0; i < TILE_N; ++i)
+          ms_out[i] = (ms_out[i] < 0.0 || part_ms[i] < 0.0) ? -1.0 : ms_out[i] + part_ms[i];
     }
     return PQMC_OK;
   }
@@ -2382,14 +2416,16 @@ int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slice
   // the wrap tile, then the exact round update's flush tile at the best wrap
   double best_ms = 1e300;
   int best_ci = b->wrap_ci;
+  // every candidate slot runs its n_slices, so that every class of an uneven
+  // batch ends on the same slice: a shape that does not fit runs them at the
+  // best shape so far and reports -1
   for (int i = 0; i < 3 && st == PQMC_OK; ++i) {
     double v = -1.0;
-    if (TILE_WRAP[i] <= max_ci) {
-      b->wrap_ci = TILE_WRAP[i];
-      time_slices(&v);
-      if (v < best_ms) { best_ms = v; best_ci = TILE_WRAP[i]; }
-    }
-    if (ms_out) ms_out[i] = v;
+    const bool fits = TILE_WRAP[i] <= max_ci;
+    b->wrap_ci = fits ? TILE_WRAP[i] : best_ci;
+    time_slices(&v);
+    if (fits && v < best_ms) { best_ms = v; best_ci = TILE_WRAP[i]; }
+    if (ms_out) ms_out[i] = fits ? v : -1.0;
   }
   b->wrap_ci = best_ci;
   best_ms = 1e300;
@@ -2404,6 +2440,17 @@ int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slice
     if (ms_out) ms_out[3 + i] = v;
   }
   b->xflush_ct = best_ct;
+  // the scan's panel chunk at the best wrap and flush tiles
+  best_ms = 1e300;
+  int best_qc = b->qc;
+  for (int i = 0; i < 3 && st == PQMC_OK; ++i) {
+    double v = -1.0;
+    b->qc = tile_qc(b->qc_max, i);
+    time_slices(&v);
+    if (v < best_ms) { best_ms = v; best_qc = b->qc; }
+    if (ms_out) ms_out[5 + i] = v;
+  }
+  b->qc = best_qc;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->graphs = graphs;
@@ -2412,6 +2459,7 @@ int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slice
   drop_graphs(b);
   best[0] = best_ci;
   best[1] = best_ct;
+  best[2] = best_qc;
   return PQMC_OK;
 }
 

@@ -418,22 +418,46 @@ class PqmcBatch:
         check(self.lib, self.lib.pqmc_batch_get_gemm_engine(self.h, ctypes.byref(v)), "pqmc_batch_get_gemm_engine")
         return int(v.value)
 
+    def set_scan_chunk(self, qc: int):
+        """Panel columns per streamed chunk of the scan (1 .. the largest that fits)."""
+        check(self.lib, self.lib.pqmc_batch_set_scan_chunk(self.h, qc), "pqmc_batch_set_scan_chunk")
+
+    def scan_chunk(self, with_max: bool = False):
+        """The scan's panel chunk (and, with_max, the largest that fits)."""
+        v, mx = ctypes.c_int(0), ctypes.c_int(0)
+        check(self.lib, self.lib.pqmc_batch_get_scan_chunk(self.h, ctypes.byref(v), ctypes.byref(mx)),
+              "pqmc_batch_get_scan_chunk")
+        return (int(v.value), int(mx.value)) if with_max else int(v.value)
+
+    TILE_FLUSH = (64, 32)
+
+    @staticmethod
+    def scan_chunk_candidates(qc_max: int):
+        """The scan chunks the tile autotuner times, in its ms_out order."""
+        return (qc_max, (3 * qc_max + 3) // 4, (qc_max + 1) // 2)
+
     def autotune_tiles(self, loop: int, first_tc: int, n_slices: int):
         """Tile-shape autotuner at the current delay depth: every wrap tile,
-        then (exact round update) every flush tile, each timed over n_slices
-        slices from (loop, first_tc); keeps the fastest of each.  Returns
-        ((best wrap tile, best flush tile), {wrap tile: ms}, {flush tile: ms})
+        then (exact round update) every flush tile, then every scan chunk,
+        each timed over n_slices slices from (loop, first_tc); keeps the
+        fastest of each.  Returns ((best wrap tile, best flush tile, best
+        scan chunk), {wrap tile: ms}, {flush tile: ms}, {scan chunk: ms})
         with None where a shape does not fit or does not apply."""
-        ms = np.zeros(5)
-        best = (ctypes.c_int * 2)()
+        ms = np.zeros(8)
+        best = (ctypes.c_int * 3)()
+        _, qmax = self.scan_chunk(with_max=True)
         check(self.lib, self.lib.pqmc_batch_autotune_tiles(self.h, loop, first_tc, n_slices, best,
                                                             ms.ctypes.data_as(_f64p)), "pqmc_batch_autotune_tiles")
         val = [float(v) if v >= 0 else None for v in ms]
-        return (int(best[0]), int(best[1])), dict(zip((0, 1, 2), val[:3])), dict(zip((64, 32), val[3:]))
+        # the scan slots as a list of (chunk, ms): two slots can hold the same chunk when qc_max is small
+        scan = list(zip(self.scan_chunk_candidates(qmax), val[5:8]))
+        return ((int(best[0]), int(best[1]), int(best[2])), dict(zip((0, 1, 2), val[:3])),
+                dict(zip(self.TILE_FLUSH, val[3:5])), scan)
 
-    def tiles_timed(self, wrap_table: dict, flush_table: dict) -> int:
-        """Blocks of slices an autotune_tiles call ran (one per timed shape)."""
-        return sum(v is not None for v in wrap_table.values()) + sum(v is not None for v in flush_table.values())
+    def tiles_timed(self, wrap_table: dict, flush_table: dict, scan_slots: list) -> int:
+        """Blocks of slices an autotune_tiles call ran: every wrap and scan
+        chunk slot, and the flush slots with the exact round update."""
+        return len(wrap_table) + sum(v is not None for v in flush_table.values()) + len(scan_slots)
 
     def set_measure(self, warmup: int, meas_interval: int = 1, meas_number: int = 0):
         """Equal-time measurements in batched sweeps (chains built with meas=True)."""

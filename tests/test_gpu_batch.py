@@ -296,16 +296,52 @@ def test_wrap_tiles_bit_identical_and_autotuned():
             assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
     b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
     b.init()
-    (best, fbest), table, ftable = b.autotune_tiles(1, 1, 4)
+    (best, fbest, qbest), table, ftable, qtable = b.autotune_tiles(1, 1, 2)
     assert best in (0, 1, 2) and b.wrap_tile() == best
     assert fbest in (64, 32) and b.flush_tile() == fbest
+    assert b.scan_chunk() == qbest and qbest in [q for q, _ in qtable]
     assert all(v is not None and v > 0 for v in table.values())
     assert all(v is not None and v > 0 for v in ftable.values())
+    assert all(v is not None and v > 0 for _, v in qtable)
     assert table[best] == min(table.values()) and ftable[fbest] == min(ftable.values())
-    assert b.tiles_timed(table, ftable) == 5
-    b.sweep_slices(1, 21, 0)
+    assert min(qtable, key=lambda t: t[1])[0] == qbest
+    assert b.tiles_timed(table, ftable, qtable) == 8
+    b.sweep_slices(1, 17, 4)   # the rest of sweep 1
     b.sweep(2)
     assert all(0.0 < c.state()["err_g_rel_max"] < 1e-8 for c in b.chains)
+    b.close()
+
+
+def test_scan_chunks_bit_identical():
+    """The scan's panel chunk (the largest that fits, 6 or 4 columns per stage) changes only
+    how the panels stream through shared memory: the chains are bit-identical
+    whichever runs."""
+    from pqmc_allinone_gb300.engine import PqmcBatch
+    ms = []
+    for i in range(3):
+        m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=170 + i)
+        ms.append((m, f, seed_words(1700 + i)))
+    runs = []
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    qmax = b.scan_chunk(with_max=True)[1]
+    b.close()
+    assert qmax >= 4
+    for qc in sorted({qmax, min(qmax, 6), 4}, reverse=True):
+        b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+        b.set_scan_chunk(qc)
+        assert b.scan_chunk() == qc
+        b.init()
+        for loop in (1, 2):
+            b.sweep(loop)
+        runs.append([(c.field(), c.g(), c.state()) for c in b.chains])
+        b.close()
+    for other in runs[1:]:
+        for (f0, g0, s0), (f1, g1, s1) in zip(runs[0], other):
+            assert np.array_equal(f0, f1) and np.array_equal(g0, g1)
+            assert s0["ln_cw"] == s1["ln_cw"] and s0["positive_accept"] == s1["positive_accept"]
+    b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
+    with pytest.raises(RuntimeError, match="shared memory"):
+        b.set_scan_chunk(10 ** 6)
     b.close()
 
 
@@ -406,8 +442,8 @@ def test_uneven_batch_autotune_then_sweeps():
     best, table = b.autotune(1, 1, 10, (16, 32, 64, 96))
     assert table[96] < 0 and best in (16, 32, 64)   # 96 columns exceed the exact round update
     tc = 1 + 10 * sum(1 for v in table.values() if v >= 0)
-    (tile, ftile), ttable, ftable = b.autotune_tiles(1, tc, 5)
-    tc += 5 * b.tiles_timed(ttable, ftable)
+    (tile, ftile, qc), ttable, ftable, qtable = b.autotune_tiles(1, tc, 5)
+    tc += 5 * b.tiles_timed(ttable, ftable, qtable)
     assert tc <= 80
     b.sweep_slices(1, tc, 80 - tc + 1)
     b.sweep(2)

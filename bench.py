@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--gemm-engine", type=int, default=1, choices=[0, 1],
                    help="engine of the recompute's GEMMs (mixed batches): 0 double-float on the FP32 pipe, "
                         "1 Ozaki-split BF16 on the tensor cores")
+    p.add_argument("--flush-tile", type=int, default=0, choices=[0, 64, 32, 2, 1],
+                   help="flush of the exact round update in --profile-block runs (0: the library default)")
     p.add_argument("--profile-block", type=int, default=0, metavar="C",
                    help="profiling run instead of the benchmark: C chains of the workload's model in one "
                         "group (delay depth 64, no graphs, the --flush round update), one warm-up block of "
@@ -335,6 +337,8 @@ def run_profile_block(args) -> None:
     b.set_flush(args.flush)
     b.set_delay(args.delay or 64)
     b.set_gemm_engine(args.gemm_engine)
+    if args.flush_tile:
+        b.set_flush_tile(args.flush_tile)
     b.init()
     b.sweep_slices(1, 1, m.ngroup)
     torch.cuda.synchronize()
@@ -452,8 +456,8 @@ def run_mixed(args, world, rank, local):
         tune = {"candidates_ms_per_slice": table, "chosen": depth,
                 "wrap_tile_ms_per_slice": {b.WRAP_TILES[k]: v for k, v in ttable.items()},
                 "wrap_tile_chosen": b.WRAP_TILES[tile],
-                "flush_tile_ms_per_slice": {f"{k} columns per CTA": v for k, v in ftable.items()},
-                "flush_tile_chosen": f"{ftile} columns per CTA",
+                "flush_tile_ms_per_slice": {b.flush_tile_name(k): v for k, v in ftable.items()},
+                "flush_tile_chosen": b.flush_tile_name(ftile),
                 "scan_chunk_ms_per_slice": [[f"{k} panel columns", v] for k, v in qtable],
                 "scan_chunk_chosen": f"{qc} panel columns"}
     for _ in range(args.warmup):
@@ -837,8 +841,8 @@ def run_uneven(args, world, rank, local):
                                        {b.WRAP_TILES[k]: v for k, v in ttable.items()},
                                    "class0_wrap_tile": b.WRAP_TILES[tile],
                                    "flush_tile_ms_per_slice_summed_over_classes":
-                                       {f"{k} columns per CTA": v for k, v in ftable.items()},
-                                   "class0_flush_tile": f"{ftile} columns per CTA",
+                                       {b.flush_tile_name(k): v for k, v in ftable.items()},
+                                   "class0_flush_tile": b.flush_tile_name(ftile),
                                    "scan_chunk_ms_per_slice_summed_over_classes":
                                        [[f"{k} panel columns", v] for k, v in qtable],
                                    "class0_scan_chunk": f"{qc} panel columns"},

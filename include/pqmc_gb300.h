@@ -423,12 +423,17 @@ int pqmc_batch_autotune(pqmc_batch* batch, int loop, int first_tc, int n_slices,
  * that fits.  Default 1 (0 with PQMC_WRAP_COLS=0). */
 int pqmc_batch_set_wrap_tile(pqmc_batch* batch, int ci);
 int pqmc_batch_get_wrap_tile(pqmc_batch* batch, int* ci);
-/* Flush tile of the exact round update: 64 columns of G per CTA (one CTA
- * per SM: 3 x 128 tensor-memory columns, 160 KB of slice images in two
- * stages) or 32 (two CTAs per SM: 3 x 64 columns, 60 KB stages of a quarter
- * of the inner dimension).  Default 64.  The two sum the rounded level of
- * the Ozaki products in another order, so chains agree to its rounding
- * (~2^-40 of the update), not bit for bit. */
+/* Flush of the exact round update: 64 columns of G per CTA (k_xgemm<1>, one
+ * CTA per SM: 3 x 128 tensor-memory columns, 160 KB of slice images in two
+ * stages), 32 (k_xflush2, two CTAs per SM: 3 x 64 columns, 60 KB stages of a
+ * quarter of the inner dimension), or the pipeline k_xflushp with 2 or 1
+ * CTAs per 128-row tile of G (the row tile's X slices resident, Z's 32-column
+ * tiles streamed in quarter stages, two tensor-memory accumulator buffers so
+ * one tile's G read-modify-write overlaps the next tile's products).
+ * Default 64.  k_xflush2 and k_xflushp sum the rounded level of the Ozaki
+ * products stage by stage and agree bit for bit; k_xgemm<1> sums it in
+ * another order, so its chains agree with theirs to that rounding (~2^-40
+ * of the update). */
 int pqmc_batch_set_flush_tile(pqmc_batch* batch, int ct);
 int pqmc_batch_get_flush_tile(pqmc_batch* batch, int* ct);
 /* Engine of the stabilised recompute's complex GEMMs (Gram matrices,
@@ -453,19 +458,18 @@ int pqmc_batch_get_gemm_engine(pqmc_batch* batch, int* engine);
 int pqmc_batch_set_scan_chunk(pqmc_batch* batch, int qc);
 int pqmc_batch_get_scan_chunk(pqmc_batch* batch, int* qc, int* qc_max);
 /* Autotune the tile shapes at the batch's delay depth: every wrap tile
- * (0, 1, 2), then, with the exact round update, every flush tile (64, 32),
+ * (0, 1, 2), then, with the exact round update, every flush (64, 32, 2, 1),
  * then the scan chunks qc_max, (3 qc_max + 3) / 4 and (qc_max + 1) / 2,
- * each timed over n_slices slices
- * of sweep `loop` from first_tc with plain launches (CUDA events on the
- * batch stream; the chains advance meanwhile); the fastest of each is kept.
- * Every wrap and scan-chunk slot runs its n_slices (a wrap tile that does
- * not fit runs them at the best so far), and the two flush slots run with
- * the exact round update only: 8 or 6 blocks of n_slices in all.
- * best (3 entries) receives the wrap tile, the flush tile and the scan
- * chunk; ms_out (8 entries: wrap 0, 1, 2, flush 64, 32, the three scan
- * chunks in that order; may be NULL) the ms per slice of each, -1 where a
- * shape does not fit or does not apply.  Uneven batches tune each class; best is the first
- * class's. */
+ * each timed over n_slices slices of sweep `loop` from first_tc with plain
+ * launches (CUDA events on the batch stream; the chains advance
+ * meanwhile); the fastest of each is kept.  Every wrap and scan-chunk slot
+ * runs its n_slices (a wrap tile that does not fit runs them at the best so
+ * far), and the four flush slots run with the exact round update only: 10
+ * or 6 blocks of n_slices in all.  best (3 entries) receives the wrap tile,
+ * the flush and the scan chunk; ms_out (10 entries: wrap 0, 1, 2, flush 64,
+ * 32, 2, 1, the three scan chunks in that order; may be NULL) the ms per
+ * slice of each, -1 where a shape does not fit or does not apply.  Uneven
+ * batches tune each class; best is the first class's. */
 int pqmc_batch_autotune_tiles(pqmc_batch* batch, int loop, int first_tc, int n_slices,
                               int* best, double* ms_out);
 /* slices tc = first_tc .. first_tc+n_slices-1 of sweep `loop` of every chain */
@@ -580,7 +584,8 @@ int pqmc_cal_g_and_det_noalloc(const double* x_left, const double* rmat, int ns,
  * Ozaki-split BF16 tensor-core products.
  * Limits: 1 <= dim <= 4, k <= 64, k % dim == 0, k <= ns <= 4096. */
 int pqmc_exact_update_check(int ns, int k, int dim, const int* sites, const double* delta, double* g);
-/* The same with the flush tile chosen: 64 (k_xgemm<1>) or 32 (k_xflush2). */
+/* The same with the flush chosen: 64 (k_xgemm<1>), 32 (k_xflush2), or 2 / 1
+ * (the pipeline k_xflushp, CTAs per row tile). */
 int pqmc_exact_update_check_tile(int ns, int k, int dim, const int* sites, const double* delta, double* g,
                                  int flush_tile);
 

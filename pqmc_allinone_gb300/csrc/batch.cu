@@ -1403,7 +1403,8 @@ struct pqmc_batch {
   bool graphs = false;
   std::vector<char> wrap_cols;   // per family: the most column items per k_bwrap_cols CTA whose columns fit (0: k_bwrap)
   int wrap_ci = 1;               // wrap tile: column items per k_bwrap_cols CTA (1, 2), 0 for the gather form k_bwrap
-  int xflush_ct = 64;            // flush tile of the exact round update: 64 (k_xgemm<1>) or 32 (k_xflush2) columns
+  int xflush_ct = 64;            // flush of the exact round update: 64 (k_xgemm<1>) or 32 (k_xflush2) columns per
+                                 // CTA, or 2 / 1 (k_xflushp: ranges of Z tiles per row tile)
   std::deque<SliceGraph> gcache;
   // proposal records of every family per chain (n_pf x max_pla); when the
   // families' bosons are disjoint, a slice's draws and proposals of all
@@ -2294,8 +2295,8 @@ int pqmc_batch_get_wrap_tile(pqmc_batch* b, int* ci) {
 }
 
 int pqmc_batch_set_flush_tile(pqmc_batch* b, int ct) {
-  if (!b || (ct != 32 && ct != 64)) {
-    set_error("batch_set_flush_tile: 64 (one CTA per SM) or 32 (two CTAs per SM) columns");
+  if (!b || (ct != 32 && ct != 64 && ct != 1 && ct != 2)) {
+    set_error("batch_set_flush_tile: 64 or 32 columns per CTA, or the pipeline with 1 or 2 CTAs per row tile");
     return PQMC_ERR_ARG;
   }
   for (auto* p : b->parts) PQMC_TRY(pqmc_batch_set_flush_tile(p, ct));
@@ -2369,10 +2370,10 @@ int pqmc_batch_get_scan_chunk(pqmc_batch* b, int* qc, int* qc_max) {
 
 // candidates of pqmc_batch_autotune_tiles, in ms_out order
 static const int TILE_WRAP[3] = {0, 1, 2};
-static const int TILE_FLUSH[2] = {64, 32};
+static const int TILE_FLUSH[4] = {64, 32, 2, 1};
 // the scan chunks tried: the largest that fits, about three quarters and half of it
 static inline int tile_qc(int qc_max, int i) { return i == 0 ? qc_max : i == 1 ? (3 * qc_max + 3) / 4 : (qc_max + 1) / 2; }
-constexpr int TILE_N = 8;   // entries of ms_out
+constexpr int TILE_N = 10;   // entries of ms_out: 3 wrap, 4 flush, 3 scan-chunk slots
 
 int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slices, int* best, double* ms_out) {
   if (!b || n_slices < 1 || !best) { set_error("batch_autotune_tiles: bad arguments"); return PQMC_ERR_ARG; }
@@ -2430,7 +2431,7 @@ int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slice
   b->wrap_ci = best_ci;
   best_ms = 1e300;
   int best_ct = b->xflush_ct;
-  for (int i = 0; i < 2 && st == PQMC_OK; ++i) {
+  for (int i = 0; i < 4 && st == PQMC_OK; ++i) {
     double v = -1.0;
     if (b->flush_mode == 2) {
       b->xflush_ct = TILE_FLUSH[i];
@@ -2448,7 +2449,7 @@ int pqmc_batch_autotune_tiles(pqmc_batch* b, int loop, int first_tc, int n_slice
     b->qc = tile_qc(b->qc_max, i);
     time_slices(&v);
     if (v < best_ms) { best_ms = v; best_qc = b->qc; }
-    if (ms_out) ms_out[5 + i] = v;
+    if (ms_out) ms_out[7 + i] = v;
   }
   b->qc = best_qc;
   cudaEventDestroy(e0);

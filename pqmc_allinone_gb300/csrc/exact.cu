@@ -764,6 +764,10 @@ __global__ void __launch_bounds__(256, 2) k_xflush2(const XDesc* X, int parity) 
     for (int ch = 0; ch < 2; ++ch) {
       const int c0 = ch * 8;
       if (ncol <= c0) break;   // warp-uniform
+      float4 gv[8];   // the chunk's G entries, all loads issued before the first use
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (r < ns && c0 + c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c0 + c)];
       float re[3][8], im[3][8];
 #pragma unroll
       for (int l = 0; l < 3; ++l) {
@@ -775,12 +779,11 @@ __global__ void __launch_bounds__(256, 2) k_xflush2(const XDesc* X, int parity) 
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           if (c0 + c >= ncol) continue;
-          float4* p = G + r + (size_t)ns * (col0 + c0 + c);
-          const float4 g = *p;
+          const float4 g = gv[c];
           const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
           const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
           const df nr = df_add(df{g.x, g.z}, vr), ni = df_add(df{g.y, g.w}, vi);
-          *p = make_float4(nr.hi, ni.hi, nr.lo, ni.lo);
+          G[r + (size_t)ns * (col0 + c0 + c)] = make_float4(nr.hi, ni.hi, nr.lo, ni.lo);
         }
       }
     }
@@ -792,19 +795,224 @@ __global__ void __launch_bounds__(256, 2) k_xflush2(const XDesc* X, int parity) 
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(taddr) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// k_xflushp: the flush G += X Z as a pipeline.  A CTA takes one 128-row tile
+// of G and a range of its 32-column tiles (nsplit ranges per row tile).  The
+// X slices of the row tile (5 slices x 2 halves of the inner dimension, at
+// most 160 KB) stay resident in shared memory; the Z slices stream through
+// three stages of a quarter of the inner dimension (20 KB each), and the
+// three level accumulators of a tile alternate between two tensor-memory
+// buffers (2 x 3 x 64 of 512 columns), so that one tile's epilogue (the G
+// read-modify-write) overlaps the next tile's copies and products.
+// Warps 0-7: epilogue (lane quarter warp & 3, 16 columns each); warp 8,
+// lane 0: the bulk copies; warp 9, lane 0: the products.  The stages and
+// the product order are those of k_xflush2, so the two give the same G bit
+// for bit.  Every wait is bounded; a role that gives up sets the CTA's fail
+// flag and the others stop at their next wait.
+constexpr int XP_HS = 8 * 16 * 128;                 // one A slice half: 8 k groups x 16 row groups (16 KB)
+constexpr int XP_A = OZ_S * 2 * XP_HS;              // resident A: 160 KB
+static_assert(OZ_S * 2 * XP_HS + 3 * OZ_S * XF_B + 2048 <= 227 * 1024, "shared memory");
+constexpr int XP_ST = OZ_S * XF_B;                  // one B stage: 5 slices x 4 k groups x 8 row groups (20 KB)
+constexpr int XP_NB = 3;                            // B stages in flight
+constexpr int XP_SMEM = XP_A + XP_NB * XP_ST;       // 220 KB
+constexpr int XP_EPI = 8;                           // epilogue warps
+constexpr int XP_THREADS = (XP_EPI + 2) * 32;
+constexpr uint32_t XP_TBUF = 256;                   // tensor-memory columns per accumulator buffer
+
+__global__ void __launch_bounds__(XP_THREADS, 1) k_xflushp(const XDesc* X, int parity, int nsplit) {
+  __shared__ XDesc sd;
+  __shared__ __align__(8) uint64_t s_afull, s_bfull[XP_NB], s_bempty[XP_NB], s_tfull[2], s_tempty[2], s_done;
+  __shared__ uint32_t s_taddr;
+  __shared__ volatile int s_fail;
+  extern __shared__ __align__(1024) unsigned char xp_dyn[];   // resident A, then XP_NB B stages
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int RT0 = (int)gridDim.x / nsplit;                   // row tiles (the grid is RT x nsplit)
+  const int ti = (int)blockIdx.x % RT0, sp = (int)blockIdx.x / RT0;
+  if (tid == 0) {
+    sd = X[blockIdx.y];
+    s_fail = 0;
+    mbar_init(&s_afull, 1);
+    for (int b = 0; b < XP_NB; ++b) {
+      mbar_init(&s_bfull[b], 1);
+      mbar_init(&s_bempty[b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&s_tfull[b], 1);
+      mbar_init(&s_tempty[b], XP_EPI);
+    }
+    mbar_init(&s_done, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const XDesc& d = sd;
+  const int K = *d.kcount;
+  const int ns = d.ns, CT = oz_ztiles(ns);
+  const int tj0 = sp * CT / nsplit, tj1 = (sp + 1) * CT / nsplit, ntile = tj1 - tj0;
+  if (K == 0 || ntile <= 0) return;   // uniform: no tensor memory taken
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_addr(&s_taddr))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  um_fence_before();
+  __syncthreads();
+  um_fence_after();
+  const uint32_t taddr = s_taddr;
+  const int nrg_a = um_rg(ns, ti);
+  const int nkg = ((K + 15) & ~15) / 8;       // k groups of one half (even, <= 8)
+  const int nq = (nkg + XF_QK - 1) / XF_QK;   // stages per half (1 or 2)
+  const int nst = 2 * nq;                     // stages per tile
+  const uint32_t ka = (uint32_t)nrg_a * 128, kb = 8u * 128u;   // bytes per k group of A and of B
+  if (warp == XP_EPI) {
+    // ---- copies ----
+    if (lane == 0) {
+      if (blockIdx.x == 0 && blockIdx.y == 0) atomicAdd(d.nflush, 1ull);
+      mbar_arrive_tx(&s_afull, (uint32_t)(OZ_S * 2 * nkg) * ka);
+      for (int sl = 0; sl < OZ_S; ++sl)
+        for (int h = 0; h < 2; ++h)
+          bulk_g2s(xp_dyn + (size_t)(sl * 2 + h) * XP_HS,
+                   d.img + (size_t)oz_slot_a2(ns, ti, sl) * UM_IMG + (size_t)h * (UM_KP / 8) * ka, (uint32_t)nkg * ka,
+                   &s_afull);
+      const int total = ntile * nst;
+      int last = -1;   // the last stage issued
+      for (int g = 0; g < total && !s_fail; ++g) {
+        const int buf = g % XP_NB, u = g / XP_NB;
+        if (u >= 1 && !mbar_wait_bounded(&s_bempty[buf], (u - 1) & 1)) {
+          s_fail = 1;
+          break;
+        }
+        const int tj = tj0 + g / nst, sidx = g % nst, h = sidx / nq, qk = sidx % nq;
+        const int nk = min(XF_QK, nkg - XF_QK * qk);
+        unsigned char* dst = xp_dyn + XP_A + (size_t)buf * XP_ST;
+        mbar_arrive_tx(&s_bfull[buf], (uint32_t)(OZ_S * nk) * kb);
+        for (int sl = 0; sl < OZ_S; ++sl)
+          bulk_g2s(dst + (size_t)sl * XF_B,
+                   d.img + (size_t)oz_slot_b2(ns, tj, sl) * UM_IMG + (size_t)(h * (UM_KP / 8) + XF_QK * qk) * kb,
+                   (uint32_t)nk * kb, &s_bfull[buf]);
+        last = g;
+      }
+      // copies still in flight complete before the CTA exits: the last
+      // XP_NB stages issued, one per buffer
+      mbar_wait_bounded(&s_afull, 0);
+      for (int g = max(0, last - XP_NB + 1); g <= last; ++g) mbar_wait_bounded(&s_bfull[g % XP_NB], (g / XP_NB) & 1);
+    }
+  } else if (warp == XP_EPI + 1) {
+    // ---- products ----
+    if (lane == 0) {
+      const uint32_t base = smem_addr(xp_dyn), idesc = um_idesc(64u);
+      if (!mbar_wait_bounded(&s_afull, 0)) s_fail = 1;
+      um_fence_after();
+      int g = 0;
+      for (int lt = 0; lt < ntile && !s_fail; ++lt) {
+        const int tb = lt & 1, v = lt >> 1;
+        if (v >= 1) {
+          if (!mbar_wait_bounded(&s_tempty[tb], (v - 1) & 1)) {
+            s_fail = 1;
+            break;
+          }
+          um_fence_after();
+        }
+        const uint32_t tacc = taddr + (uint32_t)tb * XP_TBUF;
+        uint32_t started = 0;
+        for (int sidx = 0; sidx < nst && !s_fail; ++sidx, ++g) {
+          const int buf = g % XP_NB, u = g / XP_NB, h = sidx / nq, qk = sidx % nq;
+          const int nk = min(XF_QK, nkg - XF_QK * qk);
+          if (!mbar_wait_bounded(&s_bfull[buf], u & 1)) {
+            s_fail = 1;
+            break;
+          }
+          um_fence_after();
+          const uint32_t bbase = base + XP_A + (uint32_t)buf * XP_ST;
+          for (int i = 0; i < OZ_S; ++i)
+            for (int j = 0; i + j < OZ_S; ++j) {
+              const int l = min(i + j, 2);
+              for (int kk = 0; kk < nk / 2; ++kk) {
+                const uint64_t ad =
+                    um_desc(base + (uint32_t)(i * 2 + h) * XP_HS + (uint32_t)(XF_QK * qk + 2 * kk) * ka, ka, 128);
+                const uint64_t bd = um_desc(bbase + (uint32_t)j * XF_B + (uint32_t)(2 * kk) * kb, kb, 128);
+                um_mma(tacc + (uint32_t)(l * 64), ad, bd, idesc, (started >> l) & 1u);
+                started |= 1u << l;
+              }
+            }
+          um_commit(&s_bempty[buf]);   // the stage's buffer is free once these products finish
+        }
+        if (!s_fail) um_commit(&s_tfull[tb]);   // the tile's accumulators are complete
+      }
+      // every product issued has finished before the tensor memory goes
+      um_commit(&s_done);
+      mbar_wait_bounded(&s_done, 0);
+    }
+  } else {
+    // ---- epilogue: G += the tile's level sums, 16 columns per warp ----
+    const int q = warp & 3, hf = warp >> 2;
+    const int r = ti * 128 + q * 32 + lane;
+    float4* G = parity ? d.g_alt : d.g;
+    const uint32_t tl = taddr + ((uint32_t)(q * 32) << 16);
+    for (int lt = 0; lt < ntile; ++lt) {
+      const int tb = lt & 1, v = lt >> 1;
+      const int col0 = (tj0 + lt) * 32 + hf * 16, ncol = min(16, ns - col0);
+      // this tile's 16 G entries of the row, loaded while its products run
+      // (all issued before the first use: 16 loads in flight, not a chain of
+      // load-add-store)
+      float4 gv[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (r < ns && c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c)];
+      if (s_fail || !mbar_wait_bounded(&s_tfull[tb], v & 1)) {
+        s_fail = 1;
+        break;
+      }
+      um_fence_after();
+      const uint32_t tacc = tl + (uint32_t)tb * XP_TBUF;
+#pragma unroll
+      for (int ch = 0; ch < 2; ++ch) {
+        const int c0 = ch * 8;
+        if (ncol <= c0) break;   // warp-uniform
+        float re[3][8], im[3][8];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          um_ld8_nw(tacc + l * 64 + hf * 16 + c0, re[l]);
+          um_ld8_nw(tacc + l * 64 + 32 + hf * 16 + c0, im[l]);
+        }
+        um_wait_ld();
+        if (r < ns) {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            if (c0 + c >= ncol) continue;
+            const float4 g = gv[c0 + c];
+            const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
+            const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
+            const df nr = df_add(df{g.x, g.z}, vr), ni = df_add(df{g.y, g.w}, vi);
+            G[r + (size_t)ns * (col0 + c0 + c)] = make_float4(nr.hi, ni.hi, nr.lo, ni.lo);
+          }
+        }
+      }
+      um_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&s_tempty[tb])) : "memory");
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && s_fail) atomicExch(d.err, PQMC_ERR_TIMEOUT);
+  um_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(taddr) : "memory");
+}
+
 int exact_setup() {
   PQMC_CUDA(raise_dyn_smem(k_xinv, (int)XI_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xres, (int)XR_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xgemm<0>, XG_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xgemm<1>, XG_SMEM));
   PQMC_CUDA(raise_dyn_smem(k_xflush2, XF_SMEM_LAUNCH));
+  PQMC_CUDA(raise_dyn_smem(k_xflushp, XP_SMEM));
   return PQMC_OK;
 }
 
 int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, int ct, cudaStream_t st, bool prio,
                int prio_hi) {
   const int n_r = (ns + XS_ROWS - 1) / XS_ROWS, n_c = (ns + XS_COLS - 1) / XS_COLS;
-  PQMC_CUDA(launch_at(k_xslice, dim3(n_r + n_c, C), dim3(XS_THREADS), 0, st, prio, prio_hi, d_x, parity, n_r, ct));
+  const int zw = ct == 64 ? 64 : 32;   // Z's tile width: 64 for k_xgemm<1>, 32 for k_xflush2 and k_xflushp
+  PQMC_CUDA(launch_at(k_xslice, dim3(n_r + n_c, C), dim3(XS_THREADS), 0, st, prio, prio_hi, d_x, parity, n_r, zw));
   PQMC_LAUNCHED();
   PQMC_CUDA(launch_at(k_xinv, dim3(1, C), dim3(XC_THREADS), XI_SMEM, st, prio, prio_hi, d_x, dim, parity));
   PQMC_LAUNCHED();
@@ -817,7 +1025,10 @@ int exact_products(const XDesc* d_x, int C, int ns, int parity, int ct, cudaStre
   const int RT = um_rtiles(ns);
   PQMC_CUDA(launch_at(k_xgemm<0>, dim3(RT, C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
   PQMC_LAUNCHED();
-  if (ct == 32)
+  if (ct == 1 || ct == 2)   // the pipeline: ct ranges of Z tiles per row tile
+    PQMC_CUDA(launch_at(k_xflushp, dim3(RT * ct, C), dim3(XP_THREADS), (size_t)XP_SMEM, st, prio, prio_hi, d_x,
+                        parity, ct));
+  else if (ct == 32)
     PQMC_CUDA(launch_at(k_xflush2, dim3(RT * oz_ztiles(ns), C), dim3(256), (size_t)XF_SMEM_LAUNCH, st, prio, prio_hi,
                         d_x, parity));
   else
@@ -851,9 +1062,9 @@ extern "C" int pqmc_exact_update_check_tile(int ns, int k, int dim, const int* s
                                             int flush_tile) {
   using namespace pqmc;
   if (!sites || !delta || !g || dim < 1 || dim > 4 || k < dim || k > UM_KP || k % dim || ns < k ||
-      ns > 4096 || (flush_tile != 32 && flush_tile != 64)) {
+      ns > 4096 || (flush_tile != 32 && flush_tile != 64 && flush_tile != 1 && flush_tile != 2)) {
     set_error("exact_update_check: need 1 <= dim <= 4, dim <= k <= %d, k %% dim == 0, k <= ns <= 4096, "
-              "flush tile 32 or 64", UM_KP);
+              "flush tile 64, 32, 2 or 1", UM_KP);
     return PQMC_ERR_ARG;
   }
   for (int i = 0; i < k; ++i)

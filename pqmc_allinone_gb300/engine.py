@@ -400,7 +400,8 @@ class PqmcBatch:
         return int(v.value)
 
     def set_flush_tile(self, ct: int):
-        """Flush tile of the exact round update: 64 or 32 columns of G per CTA."""
+        """Flush of the exact round update: 64 or 32 columns of G per CTA, or
+        the pipeline with 2 or 1 CTAs per row tile."""
         check(self.lib, self.lib.pqmc_batch_set_flush_tile(self.h, ct), "pqmc_batch_set_flush_tile")
 
     def flush_tile(self) -> int:
@@ -429,7 +430,11 @@ class PqmcBatch:
               "pqmc_batch_get_scan_chunk")
         return (int(v.value), int(mx.value)) if with_max else int(v.value)
 
-    TILE_FLUSH = (64, 32)
+    TILE_FLUSH = (64, 32, 2, 1)
+
+    @staticmethod
+    def flush_tile_name(ct: int) -> str:
+        return f"{ct} columns per CTA" if ct in (64, 32) else f"pipeline, {ct} CTA(s) per row tile"
 
     @staticmethod
     def scan_chunk_candidates(qc_max: int):
@@ -443,16 +448,16 @@ class PqmcBatch:
         fastest of each.  Returns ((best wrap tile, best flush tile, best
         scan chunk), {wrap tile: ms}, {flush tile: ms}, {scan chunk: ms})
         with None where a shape does not fit or does not apply."""
-        ms = np.zeros(8)
+        ms = np.zeros(10)
         best = (ctypes.c_int * 3)()
         _, qmax = self.scan_chunk(with_max=True)
         check(self.lib, self.lib.pqmc_batch_autotune_tiles(self.h, loop, first_tc, n_slices, best,
                                                             ms.ctypes.data_as(_f64p)), "pqmc_batch_autotune_tiles")
         val = [float(v) if v >= 0 else None for v in ms]
         # the scan slots as a list of (chunk, ms): two slots can hold the same chunk when qc_max is small
-        scan = list(zip(self.scan_chunk_candidates(qmax), val[5:8]))
+        scan = list(zip(self.scan_chunk_candidates(qmax), val[7:10]))
         return ((int(best[0]), int(best[1]), int(best[2])), dict(zip((0, 1, 2), val[:3])),
-                dict(zip(self.TILE_FLUSH, val[3:5])), scan)
+                dict(zip(self.TILE_FLUSH, val[3:7])), scan)
 
     def tiles_timed(self, wrap_table: dict, flush_table: dict, scan_slots: list) -> int:
         """Blocks of slices an autotune_tiles call ran: every wrap and scan
@@ -558,7 +563,7 @@ def exact_update_check(g: np.ndarray, sites, delta, flush_tile: int = 64) -> np.
     """The batch's exact round update applied to a host G (validation):
     returns G + G(:,S) Delta_S W^-1 (E_S - G(S,:)), sites in acceptance
     order (dim per move), delta (n_moves, dim, dim); flush_tile 64
-    (k_xgemm<1>) or 32 (k_xflush2)."""
+    (k_xgemm<1>), 32 (k_xflush2), or 2 / 1 (the pipeline k_xflushp)."""
     lib = load_library()
     ns = g.shape[0]
     d = np.asarray(delta, dtype=np.complex128)

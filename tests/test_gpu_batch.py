@@ -298,15 +298,14 @@ def test_wrap_tiles_bit_identical_and_autotuned():
     b.init()
     (best, fbest, qbest), table, ftable, qtable = b.autotune_tiles(1, 1, 2)
     assert best in (0, 1, 2) and b.wrap_tile() == best
-    assert fbest in (64, 32) and b.flush_tile() == fbest
+    assert fbest in (64, 32, 2, 1) and b.flush_tile() == fbest
     assert b.scan_chunk() == qbest and qbest in [q for q, _ in qtable]
     assert all(v is not None and v > 0 for v in table.values())
     assert all(v is not None and v > 0 for v in ftable.values())
     assert all(v is not None and v > 0 for _, v in qtable)
     assert table[best] == min(table.values()) and ftable[fbest] == min(ftable.values())
     assert min(qtable, key=lambda t: t[1])[0] == qbest
-    assert b.tiles_timed(table, ftable, qtable) == 8
-    b.sweep_slices(1, 17, 4)   # the rest of sweep 1
+    assert b.tiles_timed(table, ftable, qtable) == 10   # 10 slots of 2 slices: all of sweep 1
     b.sweep(2)
     assert all(0.0 < c.state()["err_g_rel_max"] < 1e-8 for c in b.chains)
     b.close()
@@ -346,18 +345,20 @@ def test_scan_chunks_bit_identical():
 
 
 def test_flush_tiles_agree():
-    """The two flush tiles of the exact round update (128 x 64 tiles, one CTA
-    per SM; 128 x 32, two CTAs per SM) sum the rounded level of the Ozaki
-    products in another order, so their chains agree to that rounding: the
-    same accept/reject sequence here, G within 1e-12, both within the drift
-    bound."""
+    """The flushes of the exact round update: 128 x 64 tiles at one CTA per
+    SM (k_xgemm<1>), 128 x 32 at two (k_xflush2), and the pipeline
+    (k_xflushp, 2 or 1 CTAs per row tile).  The last three sum the rounded
+    level of the Ozaki products stage by stage, so their chains are bit for
+    bit the same; k_xgemm<1> sums it in another order, so it agrees with them
+    to that rounding: the same accept/reject sequence here, G within 1e-12,
+    all within the drift bound."""
     from pqmc_allinone_gb300.engine import PqmcBatch
     ms = []
     for i in range(3):
         m, f = epsocz_small(L=6, ntime=20, ngroup=10, lam=0.8, alpha=0.3, seed=160 + i)
         ms.append((m, f, seed_words(1600 + i)))
     runs = []
-    for ct in (64, 32):
+    for ct in (64, 32, 2, 1):
         b = PqmcBatch([m for m, _, _ in ms], [f for _, f, _ in ms], [w for _, _, w in ms], precision=1)
         b.set_flush_tile(ct)
         assert b.flush_tile() == ct
@@ -366,10 +367,15 @@ def test_flush_tiles_agree():
             b.sweep(loop)
         runs.append([(c.field(), c.g(), c.state()) for c in b.chains])
         b.close()
-    for (f0, g0, s0), (f1, g1, s1) in zip(*runs):
-        assert np.array_equal(f0, f1) and s0["positive_accept"] == s1["positive_accept"]
-        assert rel_fro(g1, g0) < 1e-12
-        assert 0.0 < s1["err_g_rel_max"] < MIXED_DRIFT_TOL[2]
+    for other in runs[1:]:
+        for (f0, g0, s0), (f1, g1, s1) in zip(runs[0], other):
+            assert np.array_equal(f0, f1) and s0["positive_accept"] == s1["positive_accept"]
+            assert rel_fro(g1, g0) < 1e-12
+            assert 0.0 < s1["err_g_rel_max"] < MIXED_DRIFT_TOL[2]
+    for other in runs[2:]:   # the pipeline against k_xflush2: bit for bit
+        for (f1, g1, s1), (f2, g2, s2) in zip(runs[1], other):
+            assert np.array_equal(f1, f2) and np.array_equal(g1, g2)
+            assert s1["ln_cw"] == s2["ln_cw"]
 
 
 def test_launch_priorities_bit_identical(monkeypatch):
@@ -442,8 +448,8 @@ def test_uneven_batch_autotune_then_sweeps():
     best, table = b.autotune(1, 1, 10, (16, 32, 64, 96))
     assert table[96] < 0 and best in (16, 32, 64)   # 96 columns exceed the exact round update
     tc = 1 + 10 * sum(1 for v in table.values() if v >= 0)
-    (tile, ftile, qc), ttable, ftable, qtable = b.autotune_tiles(1, tc, 5)
-    tc += 5 * b.tiles_timed(ttable, ftable, qtable)
+    (tile, ftile, qc), ttable, ftable, qtable = b.autotune_tiles(1, tc, 4)
+    tc += 4 * b.tiles_timed(ttable, ftable, qtable)
     assert tc <= 80
     b.sweep_slices(1, tc, 80 - tc + 1)
     b.sweep(2)

@@ -55,7 +55,7 @@ def _case(ns, dim, nmoves, scale, seed):
     (130, 2, 13, 0.2),     # ragged row and column tiles (130 = 128 + 2)
     (77, 1, 40, 0.2),      # one site per move, one row tile
 ])
-@pytest.mark.parametrize("flush_tile", [64, 32])
+@pytest.mark.parametrize("flush_tile", [64, 32, 2, 1])
 def test_exact_update_matches_sequential_fp64(ns, dim, nmoves, scale, flush_tile):
     from pqmc_allinone_gb300.engine import exact_update_check
     g0, sites, deltas = _case(ns, dim, nmoves, scale, seed=ns + dim + nmoves)
@@ -69,6 +69,20 @@ def test_exact_update_matches_sequential_fp64(ns, dim, nmoves, scale, flush_tile
     # FP32-accurate arithmetic would leave ~1e-7 of the update: the test
     # resolves the difference
     assert err < 1e-6 * upd
+
+
+@pytest.mark.parametrize("ns,dim,nmoves", [(392, 4, 16), (130, 2, 13), (77, 1, 40), (200, 4, 5)])
+def test_pipelined_flush_bit_identical_to_quarter_stages(ns, dim, nmoves):
+    """The pipeline (k_xflushp: X resident, Z's 32-column tiles streamed,
+    two accumulator buffers) issues the products of k_xflush2 in the same
+    order, stage by stage: the updated G is the same bit for bit, with one
+    or two CTAs per row tile."""
+    from pqmc_allinone_gb300.engine import exact_update_check
+    g0, sites, deltas = _case(ns, dim, nmoves, 0.2, seed=3 * ns + nmoves)
+    ref = exact_update_check(g0, sites.reshape(-1), deltas, 32)
+    for ct in (2, 1):
+        got = exact_update_check(g0, sites.reshape(-1), deltas, ct)
+        assert np.array_equal(got, ref), ct
 
 
 def test_exact_update_two_calls_and_zero_rows():

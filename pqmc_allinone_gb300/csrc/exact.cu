@@ -437,6 +437,15 @@ __device__ __forceinline__ void um_ld16_nw(uint32_t taddr, float* v) {
 __device__ __forceinline__ void um_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // the three levels of 16 re and 16 im columns from accumulator column col
+__device__ __forceinline__ void um_ld8_nw(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void xg_load(uint32_t tbase, int col, int im_off, float (*re)[16], float (*im)[16]) {
 #pragma unroll
   for (int l = 0; l < 3; ++l) {
@@ -446,8 +455,12 @@ __device__ __forceinline__ void xg_load(uint32_t tbase, int col, int im_off, flo
   um_wait_ld();
 }
 
+// MODE 1 runs its epilogue (the G read-modify-write) on 16 warps, 16
+// columns each in chunks of 8; MODE 0 (the X slicing) on 8
+__host__ __device__ constexpr int xg_threads(int mode) { return mode == 1 ? 512 : 256; }
+
 template <int MODE>
-__global__ void __launch_bounds__(256, 1) k_xgemm(const XDesc* X, int parity) {
+__global__ void __launch_bounds__(xg_threads(MODE), 1) k_xgemm(const XDesc* X, int parity) {
   __shared__ XDesc sd;
   __shared__ __align__(8) uint64_t s_load[2], s_mma[2];
   __shared__ uint32_t s_taddr;
@@ -527,14 +540,15 @@ __global__ void __launch_bounds__(256, 1) k_xgemm(const XDesc* X, int parity) {
       s_last = half;
     }
   }
-  const int q = warp & 3, hf = warp >> 2;
+  const int q = warp & 3, hf = warp >> 2;   // lane quarter; column block (of 16 in MODE 1, 32 in MODE 0)
+  constexpr int XG_WC = MODE == 1 ? 16 : 32;  // columns per warp
   const int r = ti * 128 + q * 32 + lane;
   if (MODE == 1 && r < ns) {
     // the epilogue's G entries into L2 while thread 0 runs the copies and
     // products (a prefetch holds no registers and cannot fault: every
     // address is inside the chain's Ns x Ns tile)
     const float4* G = parity ? d.g_alt : d.g;
-    const int col0 = tj * 64 + hf * 32, ncol = min(32, ns - col0);
+    const int col0 = tj * 64 + hf * XG_WC, ncol = min(XG_WC, ns - col0);
     for (int c = 0; c < ncol; ++c)
       asm volatile("prefetch.global.L2 [%0];" ::"l"(G + r + (size_t)ns * (col0 + c)));
   }
@@ -550,23 +564,28 @@ __global__ void __launch_bounds__(256, 1) k_xgemm(const XDesc* X, int parity) {
     if (MODE == 1) {
       // G tile += (level 0 + level 1 + level 2) in double-float
       float4* G = parity ? d.g_alt : d.g;
-      const int col0 = tj * 64 + hf * 32;
-      const int ncol = min(32, ns - col0);
+      const int col0 = tj * 64 + hf * XG_WC;
+      const int ncol = min(XG_WC, ns - col0);
 #pragma unroll 1
       for (int ch = 0; ch < 2; ++ch) {
-        const int c0 = ch * 16;
+        const int c0 = ch * 8;
         if (ncol <= c0) break;   // warp-uniform
-        float4 gv[16];
+        float4 gv[8];
         if (r < ns) {
 #pragma unroll
-          for (int c = 0; c < 16; ++c)
+          for (int c = 0; c < 8; ++c)
             if (c0 + c < ncol) gv[c] = G[r + (size_t)ns * (col0 + c0 + c)];
         }
-        float re[3][16], im[3][16];
-        xg_load(tbase, hf * 32 + c0, 8 * ncg, re, im);
+        float re[3][8], im[3][8];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          um_ld8_nw(tbase + l * 128 + hf * XG_WC + c0, re[l]);
+          um_ld8_nw(tbase + l * 128 + 8 * ncg + hf * XG_WC + c0, im[l]);
+        }
+        um_wait_ld();
         if (r < ns) {
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
+          for (int c = 0; c < 8; ++c) {
             if (c0 + c >= ncol) continue;
             const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
             const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
@@ -655,15 +674,6 @@ constexpr int XF_SMEM = OZ_S * (XF_A + XF_B);     // 60 KB of stages
 // would fit by registers and by 60 KB each, but 3 x 256 tensor-memory
 // columns exceed the SM's 512 and the third allocation would wait)
 constexpr int XF_SMEM_LAUNCH = 80 * 1024;
-
-__device__ __forceinline__ void um_ld8_nw(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 __global__ void __launch_bounds__(256, 2) k_xflush2(const XDesc* X, int parity) {
   __shared__ XDesc sd;
@@ -1023,7 +1033,7 @@ int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, int ct, cud
 
 int exact_products(const XDesc* d_x, int C, int ns, int parity, int ct, cudaStream_t st, bool prio, int prio_hi) {
   const int RT = um_rtiles(ns);
-  PQMC_CUDA(launch_at(k_xgemm<0>, dim3(RT, C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
+  PQMC_CUDA(launch_at(k_xgemm<0>, dim3(RT, C), dim3(xg_threads(0)), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
   PQMC_LAUNCHED();
   if (ct == 1 || ct == 2)   // the pipeline: ct ranges of Z tiles per row tile
     PQMC_CUDA(launch_at(k_xflushp, dim3(RT * ct, C), dim3(XP_THREADS), (size_t)XP_SMEM, st, prio, prio_hi, d_x,
@@ -1032,8 +1042,8 @@ int exact_products(const XDesc* d_x, int C, int ns, int parity, int ct, cudaStre
     PQMC_CUDA(launch_at(k_xflush2, dim3(RT * oz_ztiles(ns), C), dim3(256), (size_t)XF_SMEM_LAUNCH, st, prio, prio_hi,
                         d_x, parity));
   else
-    PQMC_CUDA(launch_at(k_xgemm<1>, dim3(RT * um_ctiles(ns), C), dim3(256), (size_t)XG_SMEM, st, prio, prio_hi, d_x,
-                        parity));
+    PQMC_CUDA(launch_at(k_xgemm<1>, dim3(RT * um_ctiles(ns), C), dim3(xg_threads(1)), (size_t)XG_SMEM, st, prio,
+                        prio_hi, d_x, parity));
   PQMC_LAUNCHED();
   return PQMC_OK;
 }

@@ -424,19 +424,9 @@ __global__ void __launch_bounds__(XR_THREADS, 1) k_xres(const XDesc* X, int dim,
 // over a 128 x 64 tile of G.
 constexpr int XG_SMEM = 2 * OZ_S * (UM_IMG / 2);
 
-__device__ __forceinline__ void um_ld16_nw(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
 __device__ __forceinline__ void um_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// the three levels of 16 re and 16 im columns from accumulator column col
+// 32 lanes x 8 consecutive FP32 columns of tensor memory (no wait)
 __device__ __forceinline__ void um_ld8_nw(uint32_t taddr, float* v) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
@@ -446,26 +436,18 @@ __device__ __forceinline__ void um_ld8_nw(uint32_t taddr, float* v) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ void xg_load(uint32_t tbase, int col, int im_off, float (*re)[16], float (*im)[16]) {
-#pragma unroll
-  for (int l = 0; l < 3; ++l) {
-    um_ld16_nw(tbase + l * 128 + col, re[l]);
-    um_ld16_nw(tbase + l * 128 + im_off + col, im[l]);
-  }
-  um_wait_ld();
-}
-
-// MODE 1 runs its epilogue (the G read-modify-write) on 16 warps, 16
-// columns each in chunks of 8; MODE 0 (the X slicing) on 8
-__host__ __device__ constexpr int xg_threads(int mode) { return mode == 1 ? 512 : 256; }
+// both modes run their epilogue (MODE 1: the G read-modify-write, MODE 0:
+// the slicing of X) on 16 warps, 16 columns each in chunks of 8
+constexpr int XG_THREADS = 512;
+constexpr int XG_WB = 4;   // column blocks of 16 (warps per lane quarter)
 
 template <int MODE>
-__global__ void __launch_bounds__(xg_threads(MODE), 1) k_xgemm(const XDesc* X, int parity) {
+__global__ void __launch_bounds__(XG_THREADS, 1) k_xgemm(const XDesc* X, int parity) {
   __shared__ XDesc sd;
   __shared__ __align__(8) uint64_t s_load[2], s_mma[2];
   __shared__ uint32_t s_taddr;
   __shared__ int s_fail, s_last;
-  __shared__ float s_rmax[2][128];
+  __shared__ float s_rmax[XG_WB][128];
   extern __shared__ __align__(1024) unsigned char xg_dyn[];   // OZ_S A half-images, then OZ_S B half-images
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
@@ -540,8 +522,8 @@ __global__ void __launch_bounds__(xg_threads(MODE), 1) k_xgemm(const XDesc* X, i
       s_last = half;
     }
   }
-  const int q = warp & 3, hf = warp >> 2;   // lane quarter; column block (of 16 in MODE 1, 32 in MODE 0)
-  constexpr int XG_WC = MODE == 1 ? 16 : 32;  // columns per warp
+  const int q = warp & 3, hf = warp >> 2;   // lane quarter; column block of 16
+  constexpr int XG_WC = 64 / XG_WB;           // columns per warp
   const int r = ti * 128 + q * 32 + lane;
   if (MODE == 1 && r < ns) {
     // the epilogue's G entries into L2 while thread 0 runs the copies and
@@ -596,53 +578,72 @@ __global__ void __launch_bounds__(xg_threads(MODE), 1) k_xgemm(const XDesc* X, i
         }
       }
     } else {
-      // X tile (128 rows x 64 complex columns): row exponent over both
-      // column halves, then the slices of the flush's A operand [Xr | Xi]
+      // X tile (128 rows x 64 complex columns): row exponent over the four
+      // column blocks, then the slices of the flush's A operand [Xr | Xi]
       float mx = 0.f;
 #pragma unroll 1
       for (int ch = 0; ch < 2; ++ch) {
-        float re[3][16], im[3][16];
-        xg_load(tbase, hf * 32 + ch * 16, 64, re, im);
+        const int c0 = hf * XG_WC + ch * 8;
+        float re[3][8], im[3][8];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
+        for (int l = 0; l < 3; ++l) {
+          um_ld8_nw(tbase + l * 128 + c0, re[l]);
+          um_ld8_nw(tbase + l * 128 + 64 + c0, im[l]);
+        }
+        um_wait_ld();
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
           const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
           const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
           mx = fmaxf(mx, fmaxf(fabsf(vr.hi), fabsf(vi.hi)));
         }
       }
-      s_rmax[hf][q * 32 + lane] = mx;
-      __syncthreads();
-      const int e = oz_exp(fmaxf(s_rmax[0][q * 32 + lane], s_rmax[1][q * 32 + lane]));
       const int row = q * 32 + lane;
+      s_rmax[hf][row] = mx;
+      __syncthreads();
+      float rmx = s_rmax[0][row];
+#pragma unroll
+      for (int h = 1; h < XG_WB; ++h) rmx = fmaxf(rmx, s_rmax[h][row]);
+      const int e = oz_exp(rmx);
 #pragma unroll 1
       for (int ch = 0; ch < 2; ++ch) {
-        float re[3][16], im[3][16];
-        xg_load(tbase, hf * 32 + ch * 16, 64, re, im);
+        const int k = hf * XG_WC + ch * 8;   // the 8 columns of X are 8 inner indices of the flush
+        float re[3][8], im[3][8];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          um_ld8_nw(tbase + l * 128 + k, re[l]);
+          um_ld8_nw(tbase + l * 128 + 64 + k, im[l]);
+        }
+        um_wait_ld();
         if (r < ns) {
+          uint32_t wr[OZ_S][4], wi[OZ_S][4];   // slices packed two BF16 per word as they are cut
 #pragma unroll
-          for (int g8 = 0; g8 < 2; ++g8) {
-            float rs[OZ_S][8], is[OZ_S][8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              const int c = g8 * 8 + u;
-              const df vr = oz_combine(re[0][c], re[1][c], re[2][c]);
-              const df vi = oz_combine(im[0][c], im[1][c], im[2][c]);
-              float qr[OZ_S], qi[OZ_S];
-              oz_split(vr.hi, vr.lo, e, qr);
-              oz_split(vi.hi, vi.lo, e, qi);
-#pragma unroll
-              for (int s = 0; s < OZ_S; ++s) {
-                rs[s][u] = qr[s];
-                is[s][u] = qi[s];
-              }
+          for (int u2 = 0; u2 < 4; ++u2) {
+            float qr0[OZ_S], qi0[OZ_S], qr1[OZ_S], qi1[OZ_S];
+            {
+              const df vr = oz_combine(re[0][2 * u2], re[1][2 * u2], re[2][2 * u2]);
+              const df vi = oz_combine(im[0][2 * u2], im[1][2 * u2], im[2][2 * u2]);
+              oz_split(vr.hi, vr.lo, e, qr0);
+              oz_split(vi.hi, vi.lo, e, qi0);
             }
-            const int k = hf * 32 + ch * 16 + g8 * 8;
-#pragma unroll
-            for (int s = 0; s < OZ_S; ++s) {
-              unsigned char* im2 = d.img + (size_t)oz_slot_a2(ns, ti, s) * UM_IMG;
-              *reinterpret_cast<uint4*>(im2 + um_off(row, k, nrg_a)) = oz_pack8(rs[s]);
-              *reinterpret_cast<uint4*>(im2 + um_off(row, UM_KP + k, nrg_a)) = oz_pack8(is[s]);
+            {
+              const df vr = oz_combine(re[0][2 * u2 + 1], re[1][2 * u2 + 1], re[2][2 * u2 + 1]);
+              const df vi = oz_combine(im[0][2 * u2 + 1], im[1][2 * u2 + 1], im[2][2 * u2 + 1]);
+              oz_split(vr.hi, vr.lo, e, qr1);
+              oz_split(vi.hi, vi.lo, e, qi1);
             }
+#pragma unroll
+            for (int sl = 0; sl < OZ_S; ++sl) {
+              wr[sl][u2] = oz_pack2(qr0[sl], qr1[sl]);
+              wi[sl][u2] = oz_pack2(qi0[sl], qi1[sl]);
+            }
+          }
+#pragma unroll
+          for (int sl = 0; sl < OZ_S; ++sl) {
+            unsigned char* im2 = d.img + (size_t)oz_slot_a2(ns, ti, sl) * UM_IMG;
+            *reinterpret_cast<uint4*>(im2 + um_off(row, k, nrg_a)) = make_uint4(wr[sl][0], wr[sl][1], wr[sl][2], wr[sl][3]);
+            *reinterpret_cast<uint4*>(im2 + um_off(row, UM_KP + k, nrg_a)) =
+                make_uint4(wi[sl][0], wi[sl][1], wi[sl][2], wi[sl][3]);
           }
         }
       }
@@ -674,6 +675,7 @@ constexpr int XF_SMEM = OZ_S * (XF_A + XF_B);     // 60 KB of stages
 // would fit by registers and by 60 KB each, but 3 x 256 tensor-memory
 // columns exceed the SM's 512 and the third allocation would wait)
 constexpr int XF_SMEM_LAUNCH = 80 * 1024;
+static_assert(XF_SMEM <= XF_SMEM_LAUNCH, "the stages fit in the requested shared memory");
 
 __global__ void __launch_bounds__(256, 2) k_xflush2(const XDesc* X, int parity) {
   __shared__ XDesc sd;
@@ -1033,7 +1035,7 @@ int exact_core(const XDesc* d_x, int C, int ns, int dim, int parity, int ct, cud
 
 int exact_products(const XDesc* d_x, int C, int ns, int parity, int ct, cudaStream_t st, bool prio, int prio_hi) {
   const int RT = um_rtiles(ns);
-  PQMC_CUDA(launch_at(k_xgemm<0>, dim3(RT, C), dim3(xg_threads(0)), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
+  PQMC_CUDA(launch_at(k_xgemm<0>, dim3(RT, C), dim3(XG_THREADS), (size_t)XG_SMEM, st, prio, prio_hi, d_x, parity));
   PQMC_LAUNCHED();
   if (ct == 1 || ct == 2)   // the pipeline: ct ranges of Z tiles per row tile
     PQMC_CUDA(launch_at(k_xflushp, dim3(RT * ct, C), dim3(XP_THREADS), (size_t)XP_SMEM, st, prio, prio_hi, d_x,
@@ -1042,7 +1044,7 @@ int exact_products(const XDesc* d_x, int C, int ns, int parity, int ct, cudaStre
     PQMC_CUDA(launch_at(k_xflush2, dim3(RT * oz_ztiles(ns), C), dim3(256), (size_t)XF_SMEM_LAUNCH, st, prio, prio_hi,
                         d_x, parity));
   else
-    PQMC_CUDA(launch_at(k_xgemm<1>, dim3(RT * um_ctiles(ns), C), dim3(xg_threads(1)), (size_t)XG_SMEM, st, prio,
+    PQMC_CUDA(launch_at(k_xgemm<1>, dim3(RT * um_ctiles(ns), C), dim3(XG_THREADS), (size_t)XG_SMEM, st, prio,
                         prio_hi, d_x, parity));
   PQMC_LAUNCHED();
   return PQMC_OK;
